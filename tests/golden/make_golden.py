@@ -1,0 +1,99 @@
+"""Regenerate the golden vectors in this folder from the reference's own code.
+
+Builds the reference's USE_CPU_ONLY sources into oracle/_ref/ with the recipe
+in oracle/Makefile (needs the reference checkout; run in the development
+container, not on the GPU machine), drives them on small meshes and stores what
+they compute as compressed .npz files:
+
+  ref_<mesh>_N<order>.npz   reference-element matrices, discretisation arrays,
+                            one RHS and 1 / 10 classical-RK4 steps of the
+                            advection (a = (1,1)) and TM-Maxwell examples, one
+                            laplace_2d apply (homogeneous Dirichlet, tau = 1)
+  ref_known_answers.json    mean-square nodal errors of the reference drivers'
+                            runs on the reference's coarse mesh (10000 RK4
+                            steps of advection, Maxwell to T = 1)
+
+usage: python tests/golden/make_golden.py [/path/to/reference]
+"""
+from __future__ import annotations
+
+import json
+import os
+import struct
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.abspath(os.path.join(HERE, "..", ".."))
+sys.path.insert(0, os.path.join(ROOT, "dg-on-cuda_gb300"))
+from dgc_gb300 import meshes  # noqa: E402
+
+
+def read_dump(path: str) -> dict:
+    out = {}
+    with open(path, "rb") as f:
+        data = f.read()
+    i = 0
+    while i < len(data):
+        (ln,) = struct.unpack_from("<i", data, i); i += 4
+        name = data[i:i + ln].decode(); i += ln
+        kind, cnt = struct.unpack_from("<iq", data, i); i += 12
+        if kind == 0:
+            out[name] = np.frombuffer(data, "<f8", cnt, i).copy(); i += 8 * cnt
+        else:
+            out[name] = np.frombuffer(data, "<i4", cnt, i).copy(); i += 4 * cnt
+    return out
+
+
+def main() -> None:
+    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    oracle_dir = os.path.join(ROOT, "oracle")
+    subprocess.run(["make", "-s", "-C", oracle_dir, "ref", f"REF={ref}"], check=True)
+    dump = os.path.join(oracle_dir, "_ref", "ref_dump")
+    timer = os.path.join(oracle_dir, "_ref", "ref_time")
+    cases = []
+    with tempfile.TemporaryDirectory() as tmp:
+        jit = meshes.jittered_square(4, seed=7)
+        jpath = os.path.join(tmp, "jit4.bin")
+        meshes.write_bin(jit, jpath)
+        for N in range(1, 7):
+            cases.append(("jit4", ["--bin", jpath], N))
+        coarse = os.path.join(ref, "examples", "square_domain_coarse.msh")
+        for N in range(1, 7):
+            cases.append(("coarse", ["--msh", coarse], N))
+        four = os.path.join(ref, "tests", "square_domain_4cells.msh")
+        for N in (1, 2, 3):
+            cases.append(("cells4", ["--msh", four], N))
+        coarse_bin = None
+        for name, src, N in cases:
+            out = os.path.join(tmp, f"{name}_{N}.bin")
+            subprocess.run([dump, *src, str(N), out], check=True)
+            d = read_dump(out)
+            np.savez_compressed(os.path.join(HERE, f"ref_{name}_N{N}.npz"), **d)
+            if name == "coarse" and coarse_bin is None:
+                coarse_bin = os.path.join(tmp, "coarse.bin")
+                m = meshes.Mesh(xy=d["mesh_xy"].reshape(-1, 2), cells=d["mesh_cells"].reshape(-1, 3))
+                meshes.write_bin(m, coarse_bin)
+        known = {"advection_10000_steps": {}, "maxwell_T1": {}}
+        for N in range(1, 5):
+            r = subprocess.run([timer, coarse_bin, str(N), "adv", "10000"], check=True,
+                               capture_output=True, text=True)
+            known["advection_10000_steps"][str(N)] = json.loads(r.stdout)
+        for N in range(1, 7):
+            r = subprocess.run([timer, coarse_bin, str(N), "mx", "0", "1.0"], check=True,
+                               capture_output=True, text=True)
+            known["maxwell_T1"][str(N)] = json.loads(r.stdout)
+        for v in known.values():
+            for rec in v.values():
+                rec.pop("seconds", None)
+                rec.pop("gdof_per_s", None)
+        with open(os.path.join(HERE, "ref_known_answers.json"), "w") as f:
+            json.dump(known, f, indent=1, sort_keys=True)
+    print(f"wrote {len(cases)} golden cases + known answers to {HERE}")
+
+
+if __name__ == "__main__":
+    main()
