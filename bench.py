@@ -1,0 +1,381 @@
+#!/usr/bin/env python
+"""Headline benchmark: 2D Maxwell TE in a PEC cavity, mixed precision.
+
+Workload (one "step" = one LSERK4 time step = 5 fused RHS+stage launches):
+  jittered 128x128 square mesh (K = 32768 triangles), order N = 6 (Np = 28),
+  TE cavity mode Hz = cos(pi x) cos(pi y), Ex = Ey = 0 at t = 0,
+  dt = 0.5 min(edge) / (N+1)^2.  State and element contractions in FP32,
+  geometric factors stored in FP64.  Metric: GDOF/s = 3 Np K RHS-evaluations
+  per second / 1e9.
+
+Timing: W warm-up steps, then K timed steps; before every timed step L2 is
+flushed by writing a 512 MiB buffer (outside the timed events); each stage
+launch is bracketed by CUDA events on the launching stream; max over ranks.
+Replicas only: under torchrun every rank runs the same workload on its own GPU
+and `value` is the sum of the ranks' throughput at the slowest rank's time.
+
+--impl reference times the reference's CPU implementation of the same path
+(the oracle's serial C port of maxwell_2d + LSERK4, one core) on this host.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "dg-on-cuda_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+ORDER = 6
+NSIDE = 128
+SEED = 2026
+METRIC = "GDOF/s (Maxwell TE N=6 K=32768, LSERK4, mixed FP32 vs FP64 plain)"
+UNIT = "GDOF/s"
+WORKLOAD = "maxwell_te_pec_cavity_k32768_n6_lserk4"
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def te_initial(x, y):
+    q = np.zeros((3,) + x.shape)
+    q[2] = np.cos(np.pi * x) * np.cos(np.pi * y)
+    return q
+
+
+def te_exact(x, y, t):
+    s2 = np.sqrt(2.0)
+    q = np.zeros((3,) + x.shape)
+    q[0] = -np.cos(np.pi * x) * np.sin(np.pi * y) * np.sin(s2 * np.pi * t) / s2
+    q[1] = np.sin(np.pi * x) * np.cos(np.pi * y) * np.sin(s2 * np.pi * t) / s2
+    q[2] = np.cos(np.pi * x) * np.cos(np.pi * y) * np.cos(s2 * np.pi * t)
+    return q
+
+
+def config_dict(n_gpus):
+    return {"workload": WORKLOAD, "mesh": f"jittered {NSIDE}x{NSIDE} squares split into triangles",
+            "num_cells": 2 * NSIDE * NSIDE, "order": ORDER, "fields": 3,
+            "integrator": "LSERK4 (Carpenter-Kennedy 5-stage), one fused launch per stage",
+            "precision": "fp32 state and contractions, fp64 geometric factors",
+            "l2": "flushed between timed steps (512 MiB write)",
+            "parallelism": f"replicas x{n_gpus}"}
+
+
+def cpu_model():
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return "unknown"
+
+
+def oracle_sample(steps: int, warm: int):
+    """Serial oracle (C port of the reference CPU path): LSERK4 steps on the
+    full workload.  Returns (GDOF/s, seconds per step)."""
+    import oracle
+    from dgc_gb300 import meshes
+    m = meshes.jittered_square(NSIDE, SEED)
+    o = oracle.Oracle(m.xy, m.cells, ORDER)
+    p = oracle.problem(oracle.MAXWELL_TE)
+    x, y = o.node_xy()
+    q = te_initial(x, y).reshape(-1)
+    res = np.zeros_like(q)
+    dt = 0.5 * meshes.min_edge_length(m) / (ORDER + 1) ** 2
+    for _ in range(warm):
+        q, res = o.lserk4_step(p, 0.0, dt, q, res)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        q, res = o.lserk4_step(p, 0.0, dt, q, res)
+    sec = (time.perf_counter() - t0) / max(steps, 1)
+    dofs = 3 * o.Np * o.K
+    return dofs * 5 / sec / 1e9, sec
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thr = threading.Thread(target=self._read, daemon=True)
+            self.thr.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm = [float(r[1]) for r in self.rows if len(r) >= 9 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) >= 9 and r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            if len(r) < 9:
+                continue
+            for nm, v in zip(names, r[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def read_traffic():
+    """DRAM bytes per launch of the stage kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "dg_rhs_maxwell_te_n6_fp32.md")
+    try:
+        txt = open(path).read()
+        m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", txt)
+        return float(m.group(1)) if m else None
+    except OSError:
+        return None
+
+
+def measured_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    gdofs, sec = None, None
+    try:
+        # each step is one full LSERK4 step of the workload on one core
+        gdofs, sec = oracle_sample(args.steps, args.warmup)
+    except Exception as e:  # pragma: no cover
+        print(json.dumps({"impl": "reference", "unavailable": f"oracle port failed: {e}"}))
+        return
+    line = {"metric": METRIC, "value": gdofs, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config_dict(args.gpus),
+            "impl": "reference",
+            "cpu_baseline": {"value": gdofs, "unit": UNIT, "cores": 1, "kind": "port",
+                             "sample": f"{args.steps} full LSERK4 steps of the workload (serial C port of "
+                                       "the reference CPU operator, FP64), host " + cpu_model()},
+            "e2e": {"value": gdofs, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    import dgc_gb300 as dg
+    from dgc_gb300 import meshes
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as tdist
+        tdist.init_process_group("nccl")
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as tdist
+            tdist.barrier()
+        torch.cuda.synchronize()
+
+    m = meshes.jittered_square(NSIDE, SEED)
+    D32 = dg.Discretization(m, "maxwell_te", ORDER, dg.F32)
+    K, Np = D32.K, D32.Np
+    x, y = D32.node_xy()
+    q_init = te_initial(x, y)
+    dt = 0.5 * D32.info.min_edge / (ORDER + 1) ** 2
+    dofs = 3 * Np * K
+    stream = torch.cuda.current_stream()
+
+    qa = D32.upload(q_init)
+    qb, res = D32.empty_state(), D32.empty_state()
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def step_stages(bufs, t, evs=None):
+        for s in range(5):
+            D32.lserk4_stage(s, bufs[s & 1], bufs[(s + 1) & 1], res, t, dt)
+            if evs is not None:
+                evs[s + 1].record(stream)
+
+    bufs = [qa, qb]
+    t = 0.0
+    for _ in range(args.warmup):
+        step_stages(bufs, t)
+        bufs.reverse()
+        t += dt
+    barrier()
+    sampler = ClockSampler(local)
+    sampler.start()
+    launches0 = D32.launch_count()
+    events = [[torch.cuda.Event(enable_timing=True) for _ in range(6)] for _ in range(args.steps)]
+    wall0 = time.perf_counter()
+    for it in range(args.steps):
+        flush.fill_(float(it))
+        events[it][0].record(stream)
+        step_stages(bufs, t, events[it])
+        bufs.reverse()
+        t += dt
+    barrier()
+    wall = time.perf_counter() - wall0
+    launches = D32.launch_count() - launches0
+    step_ms = np.array([events[i][0].elapsed_time(events[i][5]) for i in range(args.steps)])
+    stage_ms = np.array([[events[i][s].elapsed_time(events[i][s + 1]) for s in range(5)]
+                         for i in range(args.steps)])
+    clocks = sampler.stop()
+    D32.check()
+    my_ms = float(step_ms.mean())
+    if ws > 1:
+        import torch.distributed as tdist
+        tt = torch.tensor([my_ms], device="cuda")
+        tdist.all_reduce(tt, op=tdist.ReduceOp.MAX)
+        my_ms = float(tt.item())
+    value = ws * dofs * 5 / (my_ms * 1e-3) / 1e9
+
+    # ---- end to end through the C ABI with host buffers (pinned), per step:
+    # H2D of the state, one LSERK4 step (dgc_lserk4_step), D2H of the new state
+    h_state = torch.empty(D32.state_len, dtype=torch.float32, pin_memory=True)
+    h_state.copy_(bufs[0].cpu())
+    h_out = torch.empty_like(h_state)
+    ev_e2e = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(args.steps)]
+    barrier()
+    for it in range(args.steps):
+        flush.fill_(float(it))
+        ev_e2e[it][0].record(stream)
+        bufs[0].copy_(h_state, non_blocking=True)
+        D32.lserk4_step(bufs[0], bufs[1], res, t, dt)
+        h_out.copy_(bufs[1], non_blocking=True)
+        ev_e2e[it][1].record(stream)
+    barrier()
+    e2e_ms = float(np.mean([a.elapsed_time(b) for a, b in ev_e2e]))
+    if ws > 1:
+        import torch.distributed as tdist
+        tt = torch.tensor([e2e_ms], device="cuda")
+        tdist.all_reduce(tt, op=tdist.ReduceOp.MAX)
+        e2e_ms = float(tt.item())
+    nbytes_state = D32.state_len * 4
+    e2e = {"value": ws * dofs * 5 / (e2e_ms * 1e-3) / 1e9, "unit": UNIT,
+           "h2d_bytes_per_step": nbytes_state, "d2h_bytes_per_step": nbytes_state,
+           "ms_per_step": e2e_ms, "path": "dgc_lserk4_step via ctypes, pinned host state in/out"}
+
+    # ---- roofline of the dominant kernel (the fused RHS + LSERK4 stage)
+    s = 4
+    alg_bytes_elem = 4 * 3 * Np * s + 14 * 8 + 3 * 4
+    alg_bytes = alg_bytes_elem * K
+    launch_ms = float(stage_ms.mean())
+    achieved = alg_bytes / (launch_ms * 1e-3) / 1e9
+    peak, peak_kind = measured_peak()
+    traffic = read_traffic()
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                "kernel": "dgk::dg_rhs_kernel<float,6,PHYS_TE> (LSERK4 stage)",
+                "alg_bytes_per_launch": alg_bytes, "launch_ms": launch_ms,
+                "stage_ms": [float(v) for v in stage_ms.mean(axis=0)]}
+
+    # ---- FP64 plain path on the same workload
+    D64 = dg.Discretization(m, "maxwell_te", ORDER, dg.F64)
+    a64 = D64.upload(q_init)
+    b64, r64 = D64.empty_state(), D64.empty_state()
+    for _ in range(3):
+        D64.lserk4_step(a64, b64, r64, 0.0, dt)
+        a64, b64 = b64, a64
+    n64 = max(3, min(args.steps, 10))
+    ev64 = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n64)]
+    for it in range(n64):
+        flush.fill_(float(it))
+        ev64[it][0].record(stream)
+        D64.lserk4_step(a64, b64, r64, 0.0, dt)
+        ev64[it][1].record(stream)
+        a64, b64 = b64, a64
+    torch.cuda.synchronize()
+    ms64 = float(np.mean([a.elapsed_time(b) for a, b in ev64]))
+    fp64 = {"value": dofs * 5 / (ms64 * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": ms64}
+
+    # ---- accuracy at T = 1 (both precisions, same initial data), rank 0 only
+    accuracy = None
+    if rank == 0 and not args.no_accuracy:
+        nsteps = int(np.ceil(1.0 / dt))
+        dtT = 1.0 / nsteps
+        res32 = D32.empty_state()
+        f32 = D32.lserk4_run(D32.upload(q_init), D32.empty_state(), res32, 0.0, dtT, nsteps, graph=True)
+        r64b = D64.empty_state()
+        t0 = time.perf_counter()
+        f64 = D64.lserk4_run(D64.upload(q_init), D64.empty_state(), r64b, 0.0, dtT, nsteps, graph=True)
+        torch.cuda.synchronize()
+        ex = te_exact(x, y, 1.0).reshape(-1)
+        u32, u64 = D32.download(f32), D64.download(f64)
+        nrm = np.linalg.norm(ex)
+        accuracy = {"T": 1.0, "steps": nsteps, "rel_l2_fp32_vs_exact": float(np.linalg.norm(u32 - ex) / nrm),
+                    "rel_l2_fp64_vs_exact": float(np.linalg.norm(u64 - ex) / nrm),
+                    "rel_l2_fp32_vs_fp64": float(np.linalg.norm(u32 - u64) / np.linalg.norm(u64)),
+                    "fp64_run_s": time.perf_counter() - t0}
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        csteps = 10
+        cg, csec = oracle_sample(csteps, 1)
+        cpu = {"value": cg, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"{csteps} full LSERK4 steps (serial C port of the reference CPU operator, FP64, "
+                         f"{csec:.2f} s/step), host {cpu_model()}"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": my_ms, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config_dict(ws),
+                "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu,
+                "clocks": clocks, "fp64_plain": fp64, "speedup_mixed_vs_fp64": value / ws / fp64["value"],
+                "accuracy": accuracy, "wall_s_timed_region": wall}
+        print(json.dumps(line))
+    if ws > 1:
+        import torch.distributed as tdist
+        tdist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

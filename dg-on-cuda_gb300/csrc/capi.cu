@@ -1,0 +1,589 @@
+// capi.cu -- C ABI of the GB300 nodal-DG hot path (declared in include/dgc_gb300.h).
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "dgc_gb300.h"
+#include "dgc_internal.hpp"
+#include "rhs_launch.cuh"
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  std::vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  return fail(DGC_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CK(call)                                        \
+  do {                                                  \
+    cudaError_t e_ = (call);                            \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+  } while (0)
+
+bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+// Low-storage RK4 coefficients, Carpenter & Kennedy (1994), NASA TM-109112,
+// five-stage fourth-order 2N-storage scheme ("solution 3").
+const double kRkA[5] = {0.0, -567301805773.0 / 1357537059087.0, -2404267990393.0 / 2016746695238.0,
+                        -3550918686646.0 / 2091501179385.0, -1275806237668.0 / 842570457699.0};
+const double kRkB[5] = {1432997174477.0 / 9575080441755.0, 5161836677717.0 / 13612068292357.0,
+                        1720146321549.0 / 2090206949498.0, 3134564353537.0 / 4481467310338.0,
+                        2277821191437.0 / 14882151754819.0};
+const double kRkC[5] = {0.0, 1432997174477.0 / 9575080441755.0, 2526269341429.0 / 6820363962896.0,
+                        2006345519317.0 / 3224310063776.0, 2802321613138.0 / 2924317926251.0};
+
+// ------------------------------------------------------------------ small kernels
+template <typename R>
+__global__ void k_axpy(size_t n, R a, const R* __restrict__ x, const R* __restrict__ y, R* __restrict__ out) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    out[i] = a * x[i] + y[i];
+}
+
+// native q[k][f][NpP] <-> reference CPU q[f][k][Np] / GPU q[f][j][k]
+template <typename R>
+__global__ void k_layout(int K, int Nf, int Np, int NpP, int layout, int to_native, const R* __restrict__ src,
+                         R* __restrict__ dst) {
+  const size_t n = (size_t)K * Nf * NpP;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n; idx += (size_t)gridDim.x * blockDim.x) {
+    const int j = (int)(idx % NpP);
+    const size_t kf = idx / NpP;
+    const int f = (int)(kf % Nf);
+    const size_t k = kf / Nf;
+    if (j >= Np) {
+      if (to_native) dst[idx] = (R)0;
+      continue;
+    }
+    const size_t r = layout == DGC_LAYOUT_REF_CPU ? ((size_t)f * K + k) * Np + j : ((size_t)f * Np + j) * K + k;
+    if (to_native) dst[idx] = src[r];
+    else dst[r] = src[idx];
+  }
+}
+
+__global__ void k_clock(double* t, double dt) { t[0] += dt; }
+
+template <typename R>
+std::vector<R> pack_mats(const dgc::RefElement& re, const std::vector<double>& Dr, const std::vector<double>& Ds,
+                         const std::vector<double>& L) {
+  const int Np = re.Np, NF = 3 * re.Nfp;
+  const int kD = (Np * Np + 3) / 4 * 4, kL = (NF * Np + 3) / 4 * 4;
+  std::vector<R> m((size_t)2 * kD + kL, (R)0);
+  for (int i = 0; i < Np; ++i)
+    for (int j = 0; j < Np; ++j) {
+      m[(size_t)j * Np + i] = (R)Dr[(size_t)i * Np + j];
+      m[(size_t)kD + j * Np + i] = (R)Ds[(size_t)i * Np + j];
+    }
+  for (int i = 0; i < Np; ++i)
+    for (int c = 0; c < NF; ++c) m[(size_t)2 * kD + c * Np + i] = (R)L[(size_t)i * NF + c];
+  return m;
+}
+
+}  // namespace
+
+namespace dgc {
+
+int set_error(int code, const char* msg) {
+  g_err = msg;
+  return code;
+}
+
+int upload_operators(dgc_handle_s* h, int form) {
+  const dgc::RefElement& re = h->re;
+  const std::vector<double>& Dr = form == 0 ? re.Drw : re.Drs;
+  const std::vector<double>& Ds = form == 0 ? re.Dsw : re.Dss;
+  const std::vector<double>& L = form == 0 ? re.Lw : re.Ls;
+  std::vector<double> m64 = pack_mats<double>(re, Dr, Ds, L);
+  std::vector<float> m32 = pack_mats<float>(re, Dr, Ds, L);
+  if (!h->d_mats64[form]) CK(cudaMalloc(&h->d_mats64[form], m64.size() * sizeof(double)));
+  if (!h->d_mats32[form]) CK(cudaMalloc(&h->d_mats32[form], m32.size() * sizeof(float)));
+  CK(cudaMemcpy(h->d_mats64[form], m64.data(), m64.size() * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(h->d_mats32[form], m32.data(), m32.size() * sizeof(float), cudaMemcpyHostToDevice));
+  return DGC_OK;
+}
+
+}  // namespace dgc
+
+
+extern "C" const char* dgc_last_error(void) { return g_err.c_str(); }
+
+extern "C" int dgc_create(int nv, const double* vxy, int K, const int32_t* cells, const dgc_problem_desc* desc,
+                          dgc_handle* out) {
+  if (!out || !desc) return fail(DGC_ERR_ARG, "null argument");
+  *out = nullptr;
+  if (desc->physics < DGC_ADVECTION || desc->physics > DGC_LAPLACE)
+    return fail(DGC_ERR_ARG, "unknown physics %d", desc->physics);
+  if (desc->precision != DGC_F64 && desc->precision != DGC_F32)
+    return fail(DGC_ERR_ARG, "unknown precision %d", desc->precision);
+  if (desc->order < 1 || desc->order > dgc::kMaxOrder)
+    return fail(DGC_ERR_ARG, "order %d outside [1, %d]", desc->order, dgc::kMaxOrder);
+  if (desc->physics == DGC_ADVECTION && (desc->bc < DGC_BC_SINSIN || desc->bc > DGC_BC_ZERO))
+    return fail(DGC_ERR_ARG, "unknown advection boundary kind %d", desc->bc);
+  if (desc->physics == DGC_ADVECTION && desc->bc == DGC_BC_GAUSS && !(desc->gw > 0.0))
+    return fail(DGC_ERR_ARG, "gaussian width must be positive");
+  auto* h = new dgc_handle_s();
+  h->desc = *desc;
+  std::string err;
+  if (!dgc::build_ref_element(desc->order, h->re, err)) {
+    delete h;
+    return fail(DGC_ERR_ARG, "%s", err.c_str());
+  }
+  if (!dgc::build_mesh(vxy, nv, cells, K, h->re, h->mesh, err)) {
+    delete h;
+    return fail(DGC_ERR_MESH, "%s", err.c_str());
+  }
+  h->K = K;
+  h->N = desc->order;
+  h->Np = h->re.Np;
+  h->Nfp = h->re.Nfp;
+  h->NpP = dgc::padded_nodes(h->N);
+  h->Nf = (desc->physics == DGC_MAXWELL_TM || desc->physics == DGC_MAXWELL_TE) ? 3 : 1;
+  h->prec = desc->precision;
+  int rc = dgc::device_init(h);
+  if (rc != DGC_OK) {
+    dgc::device_free(h);
+    delete h;
+    return rc;
+  }
+  *out = h;
+  return DGC_OK;
+}
+
+namespace dgc {
+
+int device_init(dgc_handle_s* h) {
+  CK(cudaGetDevice(&h->device));
+  CK(cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, h->device));
+  const MeshData& m = h->mesh;
+  CK(cudaMalloc(&h->d_geom, m.geom.size() * sizeof(double)));
+  CK(cudaMemcpy(h->d_geom, m.geom.data(), m.geom.size() * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMalloc(&h->d_nbr, (size_t)h->K * sizeof(int4)));
+  CK(cudaMemcpy(h->d_nbr, m.nbr.data(), (size_t)h->K * sizeof(int4), cudaMemcpyHostToDevice));
+  const size_t nb = m.bxy.size() ? m.bxy.size() : 2;
+  CK(cudaMalloc(&h->d_bxy, nb * sizeof(double)));
+  if (!m.bxy.empty()) CK(cudaMemcpy(h->d_bxy, m.bxy.data(), m.bxy.size() * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMalloc(&h->d_tau, m.tau.size() * sizeof(double)));
+  CK(cudaMemcpy(h->d_tau, m.tau.data(), m.tau.size() * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMalloc(&h->d_status, 64));
+  CK(cudaMemset(h->d_status, 0, 64));
+  CK(cudaMalloc(&h->d_time, 64));
+  CK(cudaMemset(h->d_time, 0, 64));
+  int rc = upload_operators(h, 0);
+  if (rc != DGC_OK) return rc;
+  rc = upload_operators(h, 1);
+  if (rc != DGC_OK) return rc;
+  if (h->desc.physics != DGC_LAPLACE) {
+    dgk::LaunchInfo li;
+    cudaError_t e = h->prec == DGC_F64
+                        ? dgk::rhs_dispatch<double>(h->N, h->desc.physics, dgk::RhsParams{}, h->sm_count, 0, &li)
+                        : dgk::rhs_dispatch<float>(h->N, h->desc.physics, dgk::RhsParams{}, h->sm_count, 0, &li);
+    if (e != cudaSuccess) return cuda_fail(e, "configure rhs kernel");
+    h->rhs_info = li;
+  }
+  return ipdg_init(h);
+}
+
+void device_free(dgc_handle_s* h) {
+  if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
+  cudaFree(h->d_geom);
+  cudaFree(h->d_nbr);
+  cudaFree(h->d_bxy);
+  cudaFree(h->d_tau);
+  cudaFree(h->d_status);
+  cudaFree(h->d_time);
+  for (int f = 0; f < 2; ++f) {
+    cudaFree(h->d_mats64[f]);
+    cudaFree(h->d_mats32[f]);
+  }
+  ipdg_free(h);
+}
+
+}  // namespace dgc
+
+extern "C" int dgc_destroy(dgc_handle h) {
+  if (!h) return fail(DGC_ERR_ARG, "null handle");
+  dgc::device_free(h);
+  delete h;
+  return DGC_OK;
+}
+
+extern "C" int dgc_get_info(dgc_handle h, dgc_info* o) {
+  if (!h || !o) return fail(DGC_ERR_ARG, "null argument");
+  std::memset(o, 0, sizeof *o);
+  o->num_cells = h->K;
+  o->order = h->N;
+  o->np = h->Np;
+  o->np_padded = h->NpP;
+  o->nfp = h->Nfp;
+  o->num_fields = h->Nf;
+  o->precision = h->prec;
+  o->state_len = (int64_t)h->K * h->Nf * h->NpP;
+  o->scalar_bytes = h->prec == DGC_F64 ? 8 : 4;
+  o->num_boundary_faces = h->mesh.num_bfaces;
+  o->min_edge = h->mesh.min_edge;
+  o->min_altitude = h->mesh.min_altitude;
+  o->rhs_tile = h->rhs_info.tile;
+  o->rhs_threads = h->rhs_info.threads;
+  o->rhs_smem = h->rhs_info.smem;
+  o->rhs_blocks_per_sm = h->rhs_info.blocks_per_sm;
+  o->sm_count = h->sm_count;
+  return DGC_OK;
+}
+
+extern "C" int dgc_node_coordinates(dgc_handle h, double* x, double* y) {
+  if (!h || !x || !y) return fail(DGC_ERR_ARG, "null argument");
+  const dgc::MeshData& m = h->mesh;
+  for (int k = 0; k < h->K; ++k) {
+    const int32_t* c = &m.cells[3 * (size_t)k];
+    for (int j = 0; j < h->Np; ++j) {
+      const double r = h->re.r[j], s = h->re.s[j];
+      const double l1 = 0.5 * (s + 1.0), l2 = -0.5 * (r + s), l3 = 0.5 * (r + 1.0);
+      x[(size_t)k * h->Np + j] = l2 * m.vx[c[0]] + l3 * m.vx[c[1]] + l1 * m.vx[c[2]];
+      y[(size_t)k * h->Np + j] = l2 * m.vy[c[0]] + l3 * m.vy[c[1]] + l1 * m.vy[c[2]];
+    }
+  }
+  return DGC_OK;
+}
+
+extern "C" int dgc_get_operator(dgc_handle h, int which, double* out) {
+  if (!h || !out) return fail(DGC_ERR_ARG, "null argument");
+  const dgc::RefElement& re = h->re;
+  const std::vector<double>* src = nullptr;
+  switch (which) {
+    case DGC_OP_DR_WEAK: src = &re.Drw; break;
+    case DGC_OP_DS_WEAK: src = &re.Dsw; break;
+    case DGC_OP_LIFT: src = &re.Lw; break;
+    case DGC_OP_DR_STRONG: src = &re.Drs; break;
+    case DGC_OP_DS_STRONG: src = &re.Dss; break;
+    case DGC_OP_MASS: src = &re.M; break;
+    case DGC_OP_V: src = &re.V; break;
+    default: return fail(DGC_ERR_ARG, "unknown operator %d", which);
+  }
+  std::memcpy(out, src->data(), src->size() * sizeof(double));
+  return DGC_OK;
+}
+
+extern "C" int dgc_set_operators(dgc_handle h, int form, const double* Dr, const double* Ds, const double* L) {
+  if (!h || !Dr || !Ds || !L) return fail(DGC_ERR_ARG, "null argument");
+  if (form != 0 && form != 1) return fail(DGC_ERR_ARG, "form must be 0 (weak) or 1 (strong)");
+  const size_t nn = (size_t)h->Np * h->Np, nl = (size_t)h->Np * 3 * h->Nfp;
+  dgc::RefElement& re = h->re;
+  (form == 0 ? re.Drw : re.Drs).assign(Dr, Dr + nn);
+  (form == 0 ? re.Dsw : re.Dss).assign(Ds, Ds + nn);
+  (form == 0 ? re.Lw : re.Ls).assign(L, L + nl);
+  CK(cudaDeviceSynchronize());
+  const int rc = dgc::upload_operators(h, form);
+  if (rc == DGC_OK) dgc::ipdg_operators_changed(h);
+  return rc;
+}
+
+static int layout_convert(dgc_handle h, int layout, const void* src, void* dst, void* stream, int to_native) {
+  if (!h || !src || !dst) return fail(DGC_ERR_ARG, "null argument");
+  if (src == dst) return fail(DGC_ERR_ARG, "layout conversion cannot run in place");
+  if (layout != DGC_LAYOUT_REF_CPU && layout != DGC_LAYOUT_REF_GPU)
+    return fail(DGC_ERR_ARG, "unknown layout %d", layout);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const size_t n = (size_t)h->K * h->Nf * h->NpP;
+  const int grid = (int)std::min<size_t>((n + 255) / 256, (size_t)h->sm_count * 16);
+  if (h->prec == DGC_F64)
+    k_layout<double><<<grid, 256, 0, s>>>(h->K, h->Nf, h->Np, h->NpP, layout, to_native,
+                                          static_cast<const double*>(src), static_cast<double*>(dst));
+  else
+    k_layout<float><<<grid, 256, 0, s>>>(h->K, h->Nf, h->Np, h->NpP, layout, to_native,
+                                         static_cast<const float*>(src), static_cast<float*>(dst));
+  CK(cudaGetLastError());
+  return DGC_OK;
+}
+
+extern "C" int dgc_to_native(dgc_handle h, int layout, const void* src, void* dst, void* stream) {
+  return layout_convert(h, layout, src, dst, stream, 1);
+}
+extern "C" int dgc_from_native(dgc_handle h, int layout, const void* src, void* dst, void* stream) {
+  return layout_convert(h, layout, src, dst, stream, 0);
+}
+
+extern "C" int dgc_axpy(dgc_handle h, double a, const void* x, const void* y, void* out, void* stream) {
+  if (!h || !x || !y || !out) return fail(DGC_ERR_ARG, "null argument");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const size_t n = (size_t)h->K * h->Nf * h->NpP;
+  const int grid = (int)std::min<size_t>((n + 255) / 256, (size_t)h->sm_count * 8);
+  if (h->prec == DGC_F64)
+    k_axpy<double><<<grid, 256, 0, s>>>(n, a, static_cast<const double*>(x), static_cast<const double*>(y),
+                                        static_cast<double*>(out));
+  else
+    k_axpy<float><<<grid, 256, 0, s>>>(n, (float)a, static_cast<const float*>(x), static_cast<const float*>(y),
+                                       static_cast<float*>(out));
+  CK(cudaGetLastError());
+  return DGC_OK;
+}
+
+namespace {
+
+dgk::RhsParams base_params(dgc_handle h) {
+  dgk::RhsParams p{};
+  p.K = h->K;
+  p.geom = h->d_geom;
+  p.nbr = reinterpret_cast<const int4*>(h->d_nbr);
+  p.bxy = h->d_bxy;
+  p.mats = h->prec == DGC_F64 ? h->d_mats64[0] : h->d_mats32[0];
+  p.ax = h->desc.ax;
+  p.ay = h->desc.ay;
+  p.gx0 = h->desc.gx0;
+  p.gy0 = h->desc.gy0;
+  p.gw = h->desc.gw;
+  p.bc = h->desc.bc;
+  p.status = h->d_status;
+  return p;
+}
+
+int launch(dgc_handle h, const dgk::RhsParams& p, cudaStream_t s) {
+  cudaError_t e = h->prec == DGC_F64 ? dgk::rhs_dispatch<double>(h->N, h->desc.physics, p, h->sm_count, s, nullptr)
+                                     : dgk::rhs_dispatch<float>(h->N, h->desc.physics, p, h->sm_count, s, nullptr);
+  if (e != cudaSuccess) return cuda_fail(e, "rhs kernel launch");
+  ++h->launches;
+  return DGC_OK;
+}
+
+int check_time_dependent(dgc_handle h) {
+  if (h->desc.physics == DGC_LAPLACE) return fail(DGC_ERR_UNSUPPORTED, "laplace handle has no time-dependent operator");
+  return DGC_OK;
+}
+
+}  // namespace
+
+extern "C" int dgc_rhs(dgc_handle h, const void* q, double t, void* out, void* stream) {
+  if (!h || !q || !out) return fail(DGC_ERR_ARG, "null argument");
+  if (int rc = check_time_dependent(h)) return rc;
+  if (q == out) return fail(DGC_ERR_ARG, "q and out must not alias");
+  if (!aligned16(q) || !aligned16(out)) return fail(DGC_ERR_ARG, "state buffers must be 16-byte aligned");
+  dgk::RhsParams p = base_params(h);
+  p.q_in = q;
+  p.out = out;
+  p.t = t;
+  p.mode = dgk::MODE_RHS;
+  return launch(h, p, static_cast<cudaStream_t>(stream));
+}
+
+extern "C" int dgc_rk4_step(dgc_handle h, void* q, double t, double dt, void* const* work, void* stream) {
+  if (!h || !q || !work || !work[0] || !work[1] || !work[2]) return fail(DGC_ERR_ARG, "null argument");
+  if (int rc = check_time_dependent(h)) return rc;
+  void* ya = work[0];
+  void* yb = work[1];
+  void* acc = work[2];
+  if (q == ya || q == yb || q == acc || ya == yb || ya == acc || yb == acc)
+    return fail(DGC_ERR_ARG, "q and the three work buffers must be distinct");
+  for (const void* b : {(const void*)q, (const void*)ya, (const void*)yb, (const void*)acc})
+    if (!aligned16(b)) return fail(DGC_ERR_ARG, "state buffers must be 16-byte aligned");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  dgk::RhsParams p = base_params(h);
+  p.mode = dgk::MODE_RK4;
+  p.aux = acc;
+  p.q0 = q;
+  const void* in[4] = {q, ya, yb, ya};
+  void* outb[4] = {ya, yb, ya, nullptr};
+  const double co[4] = {0.5 * dt, 0.5 * dt, dt, dt / 6.0};
+  const double wa[4] = {1.0, 2.0, 2.0, 0.0};
+  const double ts[4] = {t, t + 0.5 * dt, t + 0.5 * dt, t + dt};
+  for (int st = 0; st < 4; ++st) {
+    p.stage = st;
+    p.q_in = in[st];
+    p.out = outb[st];
+    p.ca = co[st];
+    p.cb = wa[st];
+    p.t = ts[st];
+    if (int rc = launch(h, p, s)) return rc;
+  }
+  return DGC_OK;
+}
+
+namespace {
+
+int lserk4_launches(dgc_handle h, void* q_in, void* q_out, void* res, double t, double dt, bool dev_time,
+                    cudaStream_t s) {
+  dgk::RhsParams p = base_params(h);
+  p.mode = dgk::MODE_LSERK;
+  p.aux = res;
+  p.dt = dt;
+  p.t_dev = dev_time ? h->d_time : nullptr;
+  void* bufs[2] = {q_in, q_out};
+  for (int st = 0; st < 5; ++st) {
+    p.q_in = bufs[st & 1];
+    p.out = bufs[(st + 1) & 1];
+    p.ca = kRkA[st];
+    p.cb = kRkB[st];
+    p.t = dev_time ? kRkC[st] * dt : t + kRkC[st] * dt;
+    if (int rc = launch(h, p, s)) return rc;
+  }
+  if (dev_time) {
+    k_clock<<<1, 1, 0, s>>>(h->d_time, dt);
+    CK(cudaGetLastError());
+    ++h->launches;
+  }
+  return DGC_OK;
+}
+
+int check_lserk_buffers(dgc_handle h, const void* a, const void* b, const void* r) {
+  if (!h || !a || !b || !r) return fail(DGC_ERR_ARG, "null argument");
+  if (a == b || a == r || b == r) return fail(DGC_ERR_ARG, "state, scratch and residual buffers must be distinct");
+  if (!aligned16(a) || !aligned16(b) || !aligned16(r)) return fail(DGC_ERR_ARG, "state buffers must be 16-byte aligned");
+  return check_time_dependent(h);
+}
+
+}  // namespace
+
+extern "C" int dgc_lserk4_stage(dgc_handle h, int stage, const void* q_in, void* q_out, void* res, double t,
+                                double dt, void* stream) {
+  if (int rc = check_lserk_buffers(h, q_in, q_out, res)) return rc;
+  if (stage < 0 || stage > 4) return fail(DGC_ERR_ARG, "LSERK4 stage %d outside [0, 4]", stage);
+  dgk::RhsParams p = base_params(h);
+  p.mode = dgk::MODE_LSERK;
+  p.aux = res;
+  p.dt = dt;
+  p.q_in = q_in;
+  p.out = q_out;
+  p.ca = kRkA[stage];
+  p.cb = kRkB[stage];
+  p.t = t + kRkC[stage] * dt;
+  return launch(h, p, static_cast<cudaStream_t>(stream));
+}
+
+extern "C" int dgc_lserk4_step(dgc_handle h, void* q_in, void* q_out, void* res, double t, double dt, void* stream) {
+  if (int rc = check_lserk_buffers(h, q_in, q_out, res)) return rc;
+  // 5 stages alternate q_in -> q_out -> q_in ...; the odd count ends in q_out
+  return lserk4_launches(h, q_in, q_out, res, t, dt, false, static_cast<cudaStream_t>(stream));
+}
+
+extern "C" int dgc_lserk4_run(dgc_handle h, void* qa, void* qb, void* res, double t0, double dt, int nsteps,
+                              int use_graph, void** final_state, void* stream) {
+  if (int rc = check_lserk_buffers(h, qa, qb, res)) return rc;
+  if (nsteps < 0) return fail(DGC_ERR_ARG, "negative step count");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // simulation time lives in device memory so that captured launches stay valid
+  CK(cudaMemcpyAsync(h->d_time, &t0, sizeof(double), cudaMemcpyHostToDevice, s));
+  int done = 0;
+  void* cur = qa;
+  void* other = qb;
+  if (use_graph && nsteps >= 2) {
+    const int gsteps = nsteps >= 20 ? 20 : 2;
+    const bool reuse = h->graph_exec && h->graph_key[0] == qa && h->graph_key[1] == qb && h->graph_key[2] == res &&
+                       h->graph_dt == dt && h->graph_steps == gsteps;
+    if (!reuse) {
+      if (h->graph_exec) {
+        cudaGraphExecDestroy(h->graph_exec);
+        h->graph_exec = nullptr;
+      }
+      cudaStream_t cs;
+      CK(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+      cudaGraph_t g = nullptr;
+      cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+      int rc = DGC_OK;
+      if (e == cudaSuccess) {
+        void* a = qa;
+        void* b = qb;
+        for (int i = 0; i < gsteps && rc == DGC_OK; ++i) {
+          rc = lserk4_launches(h, a, b, res, 0.0, dt, true, cs);
+          std::swap(a, b);
+        }
+        e = cudaStreamEndCapture(cs, &g);
+      }
+      cudaStreamDestroy(cs);
+      if (rc != DGC_OK) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+      }
+      if (e != cudaSuccess) return cuda_fail(e, "capture LSERK4 graph");
+      e = cudaGraphInstantiate(&h->graph_exec, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) return cuda_fail(e, "instantiate LSERK4 graph");
+      h->graph_key[0] = qa;
+      h->graph_key[1] = qb;
+      h->graph_key[2] = res;
+      h->graph_dt = dt;
+      h->graph_steps = gsteps;
+      h->launches -= (int64_t)gsteps * 6;  // captured, not executed
+    }
+    // gsteps is even, so every replay starts and ends with the state in qa
+    while (nsteps - done >= gsteps) {
+      CK(cudaGraphLaunch(h->graph_exec, s));
+      h->launches += (int64_t)gsteps * 6;
+      done += gsteps;
+    }
+  }
+  for (; done < nsteps; ++done) {
+    if (int rc = lserk4_launches(h, cur, other, res, 0.0, dt, true, s)) return rc;
+    std::swap(cur, other);
+  }
+  if (final_state) *final_state = cur;
+  return DGC_OK;
+}
+
+extern "C" int dgc_check_device_status(dgc_handle h, int* code) {
+  if (!h) return fail(DGC_ERR_ARG, "null handle");
+  int v = 0;
+  CK(cudaMemcpy(&v, h->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+  if (code) *code = v;
+  if (v != 0) {
+    CK(cudaMemset(h->d_status, 0, sizeof(int)));
+    return fail(DGC_ERR_DEVICE, "device-side error code %d (bounded wait expired)", v);
+  }
+  return DGC_OK;
+}
+
+extern "C" int64_t dgc_launch_count(dgc_handle h) { return h ? h->launches : -1; }
+
+// ---------------------------------------------------------------- host-only queries
+extern "C" int dgc_ref_nodes(int order, double* r, double* s) {
+  if (!r || !s) return fail(DGC_ERR_ARG, "null argument");
+  if (order < 1 || order > dgc::kMaxOrder) return fail(DGC_ERR_ARG, "order %d outside [1, %d]", order, dgc::kMaxOrder);
+  std::vector<double> rr, ss;
+  dgc::warp_blend_nodes(order, rr, ss);
+  std::memcpy(r, rr.data(), rr.size() * sizeof(double));
+  std::memcpy(s, ss.data(), ss.size() * sizeof(double));
+  return DGC_OK;
+}
+
+extern "C" int dgc_ref_operator(int order, int which, double* out) {
+  if (!out) return fail(DGC_ERR_ARG, "null argument");
+  dgc::RefElement re;
+  std::string err;
+  if (!dgc::build_ref_element(order, re, err)) return fail(DGC_ERR_ARG, "%s", err.c_str());
+  const std::vector<double>* src = nullptr;
+  switch (which) {
+    case DGC_OP_DR_WEAK: src = &re.Drw; break;
+    case DGC_OP_DS_WEAK: src = &re.Dsw; break;
+    case DGC_OP_LIFT: src = &re.Lw; break;
+    case DGC_OP_DR_STRONG: src = &re.Drs; break;
+    case DGC_OP_DS_STRONG: src = &re.Dss; break;
+    case DGC_OP_MASS: src = &re.M; break;
+    case DGC_OP_V: src = &re.V; break;
+    default: return fail(DGC_ERR_ARG, "unknown operator %d", which);
+  }
+  std::memcpy(out, src->data(), src->size() * sizeof(double));
+  return DGC_OK;
+}
+
+extern "C" int dgc_host_mesh(int nv, const double* vxy, int K, const int32_t* cells, int order, double* geom,
+                             int32_t* nbr, int* num_bfaces) {
+  dgc::RefElement re;
+  dgc::MeshData m;
+  std::string err;
+  if (!dgc::build_ref_element(order, re, err)) return fail(DGC_ERR_ARG, "%s", err.c_str());
+  if (!dgc::build_mesh(vxy, nv, cells, K, re, m, err)) return fail(DGC_ERR_MESH, "%s", err.c_str());
+  if (geom) std::memcpy(geom, m.geom.data(), m.geom.size() * sizeof(double));
+  if (nbr) std::memcpy(nbr, m.nbr.data(), m.nbr.size() * sizeof(int32_t));
+  if (num_bfaces) *num_bfaces = m.num_bfaces;
+  return DGC_OK;
+}

@@ -1,0 +1,93 @@
+// common.cuh -- shared device helpers: compile-time element sizes, bulk copies
+// (cp.async.bulk) into shared memory with mbarrier completion, and bounded waits.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace dgk {
+
+template <int N>
+struct Order {
+  static constexpr int Np = (N + 1) * (N + 2) / 2;
+  static constexpr int Nfp = N + 1;
+  static constexpr int NpP = (Np + 3) / 4 * 4;  // padded to 16-byte vectors of FP32
+  static constexpr int Nface = 3 * Nfp;
+};
+
+// face-node index, counter-clockwise (see setup.hpp: face_node)
+template <int N>
+__host__ __device__ constexpr int fmask(int f, int d) {
+  return f == 0 ? d
+                : (f == 1 ? d * (N + 1) - d * (d - 1) / 2 + N - d
+                          : (N - d) * (N + 1) - (N - d) * (N - d - 1) / 2);
+}
+
+// error codes written to the per-handle device status word
+enum : int {
+  kErrNone = 0,
+  kErrBarrierTimeout = 1,  // an mbarrier wait gave up
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void fence_barrier_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+
+// 1D bulk copy global -> shared, completion signalled on the mbarrier.
+// dst, src 16-byte aligned; bytes a multiple of 16.
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Wait for phase `parity` of the barrier to complete.  Gives up after about
+// one second, records kErrBarrierTimeout in *status and returns false.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* status) {
+  const uint32_t a = smem_u32(bar);
+  uint64_t t0 = 0;
+  for (uint32_t it = 0;; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if (it == 64) t0 = globaltimer_ns();
+    if (it > 64 && (it & 255) == 0 && globaltimer_ns() - t0 > 1000000000ull) {
+      if (status) atomicCAS(status, kErrNone, kErrBarrierTimeout);
+      return false;
+    }
+  }
+}
+
+template <typename R>
+struct Vec16;
+template <>
+struct Vec16<float> { using T = float4; static constexpr int n = 4; };
+template <>
+struct Vec16<double> { using T = double2; static constexpr int n = 2; };
+
+}  // namespace dgk

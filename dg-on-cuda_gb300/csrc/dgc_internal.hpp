@@ -1,0 +1,52 @@
+// dgc_internal.hpp -- the handle behind the C ABI (include/dgc_gb300.h).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "dgc_gb300.h"
+#include "rhs_launch.cuh"
+#include "setup.hpp"
+
+namespace dgc {
+struct IpdgState;
+}
+
+// the handle behind the opaque C type
+struct dgc_handle_s {
+  dgc_problem_desc desc{};
+  dgc::RefElement re;
+  dgc::MeshData mesh;
+  int K = 0, N = 0, Np = 0, NpP = 0, Nfp = 0, Nf = 1, prec = DGC_F64;
+  int device = 0, sm_count = 0;
+  // device data owned by the handle
+  double* d_geom = nullptr;   // [K][16] FP64
+  int32_t* d_nbr = nullptr;   // [K][4]
+  double* d_bxy = nullptr;    // boundary face node coordinates
+  double* d_tau = nullptr;    // [K][4] laplace penalty per face
+  void* d_mats64[2] = {nullptr, nullptr};  // weak, strong (transposed, padded)
+  void* d_mats32[2] = {nullptr, nullptr};
+  int* d_status = nullptr;    // device-side error word
+  double* d_time = nullptr;   // simulation time for graph-replayed steps
+  dgk::LaunchInfo rhs_info;
+  int64_t launches = 0;       // kernels launched through this handle
+  // cached CUDA graph of LSERK4 steps
+  cudaGraphExec_t graph_exec = nullptr;
+  void* graph_key[3] = {nullptr, nullptr, nullptr};
+  double graph_dt = 0.0;
+  int graph_steps = 0;
+  dgc::IpdgState* ipdg = nullptr;
+};
+
+namespace dgc {
+
+int set_error(int code, const char* msg);
+int upload_operators(dgc_handle_s* h, int form);
+int device_init(dgc_handle_s* h);
+void device_free(dgc_handle_s* h);
+int ipdg_init(dgc_handle_s* h);
+void ipdg_free(dgc_handle_s* h);
+void ipdg_operators_changed(dgc_handle_s* h);
+
+}  // namespace dgc

@@ -1,0 +1,53 @@
+// rhs_launch.cuh -- host-side launch of the fused RHS kernel for one
+// (precision, order, physics) instantiation.  Persistent grid: as many CTAs as
+// fit on the GPU at once (occupancy x SM count), capped by the tile count.
+#pragma once
+
+#include <mutex>
+
+#include "dg_rhs.cuh"
+
+namespace dgk {
+
+struct LaunchInfo {
+  int threads = 0, tile = 0, smem = 0, blocks_per_sm = 0;
+};
+
+template <typename R, int N, int P>
+cudaError_t rhs_configure(LaunchInfo* info) {
+  using C = RhsConfig<R, N, P>;
+  static std::once_flag once;
+  static cudaError_t st = cudaSuccess;
+  static int bps = 0;
+  std::call_once(once, [] {
+    st = cudaFuncSetAttribute(dg_rhs_kernel<R, N, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::kSmem);
+    if (st == cudaSuccess)
+      st = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, dg_rhs_kernel<R, N, P>, C::kThreads, C::kSmem);
+  });
+  if (info) {
+    info->threads = C::kThreads;
+    info->tile = C::TE;
+    info->smem = C::kSmem;
+    info->blocks_per_sm = bps;
+  }
+  return st;
+}
+
+template <typename R, int N, int P>
+cudaError_t rhs_launch(const RhsParams& p, int sm_count, cudaStream_t s) {
+  using C = RhsConfig<R, N, P>;
+  LaunchInfo li;
+  cudaError_t e = rhs_configure<R, N, P>(&li);
+  if (e != cudaSuccess) return e;
+  const int ntiles = (p.K + C::TE - 1) / C::TE;
+  int grid = sm_count * (li.blocks_per_sm > 0 ? li.blocks_per_sm : 1);
+  if (grid > ntiles) grid = ntiles;
+  dg_rhs_kernel<R, N, P><<<grid, C::kThreads, C::kSmem, s>>>(p);
+  return cudaGetLastError();
+}
+
+// dispatch over order (1..8) and physics; defined in rhs_f64.cu / rhs_f32.cu
+template <typename R>
+cudaError_t rhs_dispatch(int N, int P, const RhsParams& p, int sm_count, cudaStream_t s, LaunchInfo* info);
+
+}  // namespace dgk

@@ -1,0 +1,252 @@
+"""Python binding of the GB300 nodal-DG library (lib/libdgc_gb300.so).
+
+A thin ctypes layer over the C ABI in include/dgc_gb300.h.  PyTorch is used
+only to own device memory and streams (tensors are passed by data pointer);
+all arithmetic runs in the library's CUDA kernels.  There is no CPU fallback:
+if the shared library is missing or cannot be loaded, every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+import numpy as np
+
+from . import meshes  # noqa: F401
+
+PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(PKG, "lib", "libdgc_gb300.so")
+
+ADVECTION, MAXWELL_TM, MAXWELL_TE, LAPLACE = 0, 1, 2, 3
+F64, F32 = 0, 1
+BC_SINSIN, BC_GAUSS, BC_ZERO = 0, 1, 2
+TAU_ONE, TAU_SCALED = 0, 1
+LAYOUT_NATIVE, LAYOUT_REF_CPU, LAYOUT_REF_GPU = 0, 1, 2
+OP_DR_WEAK, OP_DS_WEAK, OP_LIFT, OP_DR_STRONG, OP_DS_STRONG, OP_MASS, OP_V = range(7)
+PHYSICS = {"advection": ADVECTION, "maxwell_tm": MAXWELL_TM, "maxwell_te": MAXWELL_TE, "laplace": LAPLACE}
+
+
+class DgcError(RuntimeError):
+    pass
+
+
+class ProblemDesc(C.Structure):
+    _fields_ = [("physics", C.c_int), ("order", C.c_int), ("precision", C.c_int),
+                ("ax", C.c_double), ("ay", C.c_double), ("bc", C.c_int),
+                ("gx0", C.c_double), ("gy0", C.c_double), ("gw", C.c_double),
+                ("tau", C.c_int), ("dirichlet", C.c_int)]
+
+
+class Info(C.Structure):
+    _fields_ = [("num_cells", C.c_int64), ("order", C.c_int), ("np", C.c_int), ("np_padded", C.c_int),
+                ("nfp", C.c_int), ("num_fields", C.c_int), ("precision", C.c_int),
+                ("state_len", C.c_int64), ("scalar_bytes", C.c_int64), ("num_boundary_faces", C.c_int),
+                ("min_edge", C.c_double), ("min_altitude", C.c_double),
+                ("rhs_tile", C.c_int), ("rhs_threads", C.c_int), ("rhs_smem", C.c_int),
+                ("rhs_blocks_per_sm", C.c_int), ("sm_count", C.c_int)]
+
+
+_lock = threading.Lock()
+_lib = None
+_vp = C.c_void_p
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+
+
+def lib():
+    """Load the CUDA library (raises if it was not built)."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH):
+                raise DgcError(f"{LIB_PATH} not built: run __graft_entry__.build() "
+                               "or python dg-on-cuda_gb300/dgc_gb300/build.py")
+            L = C.CDLL(LIB_PATH)
+            L.dgc_last_error.restype = C.c_char_p
+            L.dgc_create.argtypes = [C.c_int, _dp, C.c_int, _ip, C.POINTER(ProblemDesc), C.POINTER(_vp)]
+            L.dgc_destroy.argtypes = [_vp]
+            L.dgc_get_info.argtypes = [_vp, C.POINTER(Info)]
+            L.dgc_node_coordinates.argtypes = [_vp, _dp, _dp]
+            L.dgc_get_operator.argtypes = [_vp, C.c_int, _dp]
+            L.dgc_set_operators.argtypes = [_vp, C.c_int, _dp, _dp, _dp]
+            L.dgc_to_native.argtypes = [_vp, C.c_int, _vp, _vp, _vp]
+            L.dgc_from_native.argtypes = [_vp, C.c_int, _vp, _vp, _vp]
+            L.dgc_rhs.argtypes = [_vp, _vp, C.c_double, _vp, _vp]
+            L.dgc_axpy.argtypes = [_vp, C.c_double, _vp, _vp, _vp, _vp]
+            L.dgc_rk4_step.argtypes = [_vp, _vp, C.c_double, C.c_double, C.POINTER(_vp), _vp]
+            L.dgc_lserk4_step.argtypes = [_vp, _vp, _vp, _vp, C.c_double, C.c_double, _vp]
+            L.dgc_lserk4_stage.argtypes = [_vp, C.c_int, _vp, _vp, _vp, C.c_double, C.c_double, _vp]
+            L.dgc_lserk4_run.argtypes = [_vp, _vp, _vp, _vp, C.c_double, C.c_double, C.c_int, C.c_int,
+                                         C.POINTER(_vp), _vp]
+            L.dgc_check_device_status.argtypes = [_vp, C.POINTER(C.c_int)]
+            L.dgc_launch_count.restype = C.c_int64
+            L.dgc_launch_count.argtypes = [_vp]
+            L.dgc_ref_nodes.argtypes = [C.c_int, _dp, _dp]
+            L.dgc_ref_operator.argtypes = [C.c_int, C.c_int, _dp]
+            L.dgc_host_mesh.argtypes = [C.c_int, _dp, C.c_int, _ip, C.c_int, _dp, _ip, C.POINTER(C.c_int)]
+            _lib = L
+    return _lib
+
+
+def _check(rc: int) -> None:
+    if rc != 0:
+        raise DgcError(f"dgc error {rc}: {lib().dgc_last_error().decode()}")
+
+
+def _stream(stream=None) -> int:
+    if stream is not None:
+        return int(stream)
+    import torch
+    return int(torch.cuda.current_stream().cuda_stream)
+
+
+def _ptr(t) -> int:
+    return int(t.data_ptr())
+
+
+def ref_nodes(order: int):
+    n = (order + 1) * (order + 2) // 2
+    r = np.zeros(n)
+    s = np.zeros(n)
+    _check(lib().dgc_ref_nodes(order, r, s))
+    return r, s
+
+
+def ref_operator(order: int, which: int) -> np.ndarray:
+    n, nfp = (order + 1) * (order + 2) // 2, order + 1
+    shape = (n, 3 * nfp) if which == OP_LIFT else (n, n)
+    out = np.zeros(shape[0] * shape[1])
+    _check(lib().dgc_ref_operator(order, which, out))
+    return out.reshape(shape)
+
+
+def host_mesh(mesh, order: int):
+    """Validated topology and geometry computed on the host (no GPU)."""
+    xy = np.ascontiguousarray(mesh.xy, dtype=np.float64).reshape(-1)
+    cells = np.ascontiguousarray(mesh.cells, dtype=np.int32).reshape(-1)
+    K = cells.size // 3
+    geom = np.zeros(K * 16)
+    nbr = np.zeros(K * 4, np.int32)
+    nb = C.c_int(0)
+    _check(lib().dgc_host_mesh(xy.size // 2, xy, K, cells, order, geom, nbr, C.byref(nb)))
+    return geom.reshape(K, 16), nbr.reshape(K, 4), nb.value
+
+
+class Discretization:
+    """Mesh + order + physics on the current CUDA device (the handle of the C ABI)."""
+
+    def __init__(self, mesh, physics, order: int, precision: int = F64, ax: float = 1.0, ay: float = 1.0,
+                 bc: int = BC_SINSIN, gx0: float = -0.3, gy0: float = 0.0, gw: float = 0.02,
+                 tau: int = TAU_SCALED, dirichlet: bool = True):
+        if isinstance(physics, str):
+            physics = PHYSICS[physics]
+        xy = np.ascontiguousarray(mesh.xy, dtype=np.float64).reshape(-1)
+        cells = np.ascontiguousarray(mesh.cells, dtype=np.int32).reshape(-1)
+        self.desc = ProblemDesc(physics, order, precision, ax, ay, bc, gx0, gy0, gw, tau, int(dirichlet))
+        h = _vp()
+        _check(lib().dgc_create(xy.size // 2, xy, cells.size // 3, cells, C.byref(self.desc), C.byref(h)))
+        self._h = h
+        info = Info()
+        _check(lib().dgc_get_info(self._h, C.byref(info)))
+        self.info = info
+        self.K, self.N, self.Np, self.NpP = info.num_cells, info.order, info.np, info.np_padded
+        self.Nfp, self.Nf = info.nfp, info.num_fields
+        self.state_len = info.state_len
+        self.precision = precision
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                lib().dgc_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    # ---------------------------------------------------------------- host-side info
+    @property
+    def torch_dtype(self):
+        import torch
+        return torch.float64 if self.precision == F64 else torch.float32
+
+    def node_xy(self):
+        x = np.zeros(self.K * self.Np)
+        y = np.zeros(self.K * self.Np)
+        _check(lib().dgc_node_coordinates(self._h, x, y))
+        return x.reshape(self.K, self.Np), y.reshape(self.K, self.Np)
+
+    def operator(self, which: int) -> np.ndarray:
+        shape = {OP_LIFT: (self.Np, 3 * self.Nfp)}.get(which, (self.Np, self.Np))
+        out = np.zeros(shape[0] * shape[1])
+        _check(lib().dgc_get_operator(self._h, which, out))
+        return out.reshape(shape)
+
+    def set_operators(self, form: int, Dr, Ds, L) -> None:
+        f = lambda a: np.ascontiguousarray(a, dtype=np.float64).reshape(-1)  # noqa: E731
+        _check(lib().dgc_set_operators(self._h, form, f(Dr), f(Ds), f(L)))
+
+    def launch_count(self) -> int:
+        return int(lib().dgc_launch_count(self._h))
+
+    def check(self) -> None:
+        code = C.c_int(0)
+        _check(lib().dgc_check_device_status(self._h, C.byref(code)))
+
+    # ---------------------------------------------------------------- device state
+    def empty_state(self, zero: bool = True):
+        import torch
+        f = torch.zeros if zero else torch.empty
+        return f(self.state_len, dtype=self.torch_dtype, device="cuda")
+
+    def to_native(self, src, layout: int = LAYOUT_REF_CPU, out=None, stream=None):
+        out = self.empty_state() if out is None else out
+        _check(lib().dgc_to_native(self._h, layout, _ptr(src), _ptr(out), _stream(stream)))
+        return out
+
+    def from_native(self, q, layout: int = LAYOUT_REF_CPU, out=None, stream=None):
+        import torch
+        if out is None:
+            out = torch.empty(self.Nf * self.K * self.Np, dtype=self.torch_dtype, device="cuda")
+        _check(lib().dgc_from_native(self._h, layout, _ptr(q), _ptr(out), _stream(stream)))
+        return out
+
+    def upload(self, q_ref_cpu: np.ndarray, stream=None):
+        """Host array in the reference CPU layout [field][cell][node] -> native device state."""
+        import torch
+        src = torch.from_numpy(np.ascontiguousarray(q_ref_cpu).reshape(-1)).to(self.torch_dtype).cuda()
+        return self.to_native(src, LAYOUT_REF_CPU, stream=stream)
+
+    def download(self, q, stream=None) -> np.ndarray:
+        """Native device state -> host float64 array in the reference CPU layout."""
+        return self.from_native(q, LAYOUT_REF_CPU, stream=stream).double().cpu().numpy()
+
+    # ---------------------------------------------------------------- operators
+    def rhs(self, q, t: float, out=None, stream=None):
+        out = self.empty_state() if out is None else out
+        _check(lib().dgc_rhs(self._h, _ptr(q), t, _ptr(out), _stream(stream)))
+        return out
+
+    def axpy(self, a: float, x, y, out, stream=None):
+        _check(lib().dgc_axpy(self._h, a, _ptr(x), _ptr(y), _ptr(out), _stream(stream)))
+        return out
+
+    def rk4_step(self, q, t: float, dt: float, work, stream=None):
+        arr = (_vp * 3)(*[_ptr(w) for w in work])
+        _check(lib().dgc_rk4_step(self._h, _ptr(q), t, dt, arr, _stream(stream)))
+        return q
+
+    def lserk4_step(self, q_in, q_out, res, t: float, dt: float, stream=None):
+        _check(lib().dgc_lserk4_step(self._h, _ptr(q_in), _ptr(q_out), _ptr(res), t, dt, _stream(stream)))
+        return q_out
+
+    def lserk4_stage(self, stage: int, q_in, q_out, res, t: float, dt: float, stream=None):
+        _check(lib().dgc_lserk4_stage(self._h, stage, _ptr(q_in), _ptr(q_out), _ptr(res), t, dt,
+                                      _stream(stream)))
+        return q_out
+
+    def lserk4_run(self, qa, qb, res, t0: float, dt: float, nsteps: int, graph: bool = True, stream=None):
+        fin = _vp()
+        _check(lib().dgc_lserk4_run(self._h, _ptr(qa), _ptr(qb), _ptr(res), t0, dt, nsteps, int(graph),
+                                    C.byref(fin), _stream(stream)))
+        return qa if fin.value == _ptr(qa) else qb

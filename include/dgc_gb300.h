@@ -1,0 +1,194 @@
+/*
+ * dgc_gb300.h -- C ABI of the GB300 (sm_103a) nodal-DG hot path.
+ *
+ * A drop-in for the GPU path of hsongxa/dg-on-cuda on 2D triangle meshes:
+ * the device discretisation and operators (src/d_simple_discretization_2d.cuh,
+ * examples/*\/d_*_2d.cuh), their launchers (src/device_SemiDiscOp_wrapper.cuh,
+ * src/kernel_adapter.cuh), the time integrator (src/explicit_runge_kutta.h,
+ * src/k_axpy.cuh) and the laplace_2d IPDG operator (src/laplace_2d.h).
+ *
+ * Conventions
+ *  - Every function returns DGC_OK (0) or a negative dgc_status; no C++
+ *    exception crosses this boundary.  dgc_last_error() gives a message for the
+ *    calling thread's last failure.
+ *  - State vectors are caller-owned device buffers in the native layout
+ *    q[cell][field][NpP] (NpP = Np rounded up to a multiple of 4), 16-byte
+ *    aligned, in the handle's precision (double for DGC_F64, float for DGC_F32).
+ *    dgc_info.state_len gives the element count.  Padding entries are carried
+ *    along and never used.  dgc_to_native / dgc_from_native convert from / to
+ *    the reference's layouts.
+ *  - `stream` is a cudaStream_t (NULL = legacy default stream).  All calls are
+ *    asynchronous on that stream unless stated otherwise.
+ *  - Geometry, connectivity and operator matrices are owned by the handle.
+ */
+#ifndef DGC_GB300_H
+#define DGC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct dgc_handle_s* dgc_handle;
+
+typedef enum dgc_status {
+  DGC_OK = 0,
+  DGC_ERR_ARG = -1,          /* invalid argument (null / misaligned pointer, bad enum, aliasing) */
+  DGC_ERR_MESH = -2,         /* mesh rejected (out-of-range index, clockwise or degenerate cell, non-conforming) */
+  DGC_ERR_CUDA = -3,         /* a CUDA runtime call failed */
+  DGC_ERR_UNSUPPORTED = -4,  /* operation not defined for this handle (physics / precision) */
+  DGC_ERR_DEVICE = -5,       /* a kernel reported a device-side error (bounded wait expired) */
+  DGC_ERR_NOT_CONVERGED = -6 /* iterative solver stopped before reaching its tolerance */
+} dgc_status;
+
+typedef enum dgc_physics {
+  DGC_ADVECTION = 0,   /* u_t + a.grad u = 0, upwind flux (examples/advection_2d/advection_2d.h:156-258) */
+  DGC_MAXWELL_TM = 1,  /* (Hx, Hy, Ez), PEC walls (examples/maxwell_2d/maxwell_2d.h:178-311) */
+  DGC_MAXWELL_TE = 2,  /* (Ex, Ey, Hz), PEC walls: E+ = -E-, Hz+ = Hz- */
+  DGC_LAPLACE = 3      /* strong-form LDG/IPDG laplace_2d (src/laplace_2d.h:130-251) */
+} dgc_physics;
+
+typedef enum dgc_precision { DGC_F64 = 0, DGC_F32 = 1 } dgc_precision;
+
+/* advection inflow values: the exact translated solution */
+typedef enum dgc_bc {
+  DGC_BC_SINSIN = 0, /* sin(pi(x+1-ax t)) sin(pi(y+1-ay t)) (advection_2d.h:152,191) */
+  DGC_BC_GAUSS = 1,  /* exp(-((x-ax t-x0)^2 + (y-ay t-y0)^2)/w) */
+  DGC_BC_ZERO = 2
+} dgc_bc;
+
+/* laplace penalty: 1 (reference, laplace_2d.h:244) or (N+1)^2/h_f per face */
+typedef enum dgc_tau { DGC_TAU_ONE = 0, DGC_TAU_SCALED = 1 } dgc_tau;
+
+typedef enum dgc_layout {
+  DGC_LAYOUT_NATIVE = 0,
+  DGC_LAYOUT_REF_CPU = 1, /* q[field][cell][node] (USE_CPU_ONLY, advection_2d.h:117-119) */
+  DGC_LAYOUT_REF_GPU = 2  /* q[field][node][cell] (GPU build, advection_2d.h:120-123) */
+} dgc_layout;
+
+typedef enum dgc_operator {
+  DGC_OP_DR_WEAK = 0, DGC_OP_DS_WEAK = 1, DGC_OP_LIFT = 2,
+  DGC_OP_DR_STRONG = 3, DGC_OP_DS_STRONG = 4, DGC_OP_MASS = 5, DGC_OP_V = 6
+} dgc_operator;
+
+typedef struct dgc_problem_desc {
+  int physics;        /* dgc_physics */
+  int order;          /* N in [1, 8] */
+  int precision;      /* dgc_precision */
+  double ax, ay;      /* advection velocity */
+  int bc;             /* dgc_bc (advection) */
+  double gx0, gy0, gw;/* gaussian inflow data */
+  int tau;            /* dgc_tau (laplace) */
+  int dirichlet;      /* laplace: 1 = all boundary faces Dirichlet, 0 = all Neumann */
+} dgc_problem_desc;
+
+typedef struct dgc_info {
+  int64_t num_cells;       /* K */
+  int order, np, np_padded, nfp, num_fields;
+  int precision;
+  int64_t state_len;       /* K * num_fields * np_padded */
+  int64_t scalar_bytes;    /* 8 or 4 */
+  int num_boundary_faces;
+  double min_edge, min_altitude;
+  int rhs_tile, rhs_threads, rhs_smem, rhs_blocks_per_sm, sm_count;
+} dgc_info;
+
+/* Replaces create_simple_discretization_2d_on_device + the examples'
+ * create_device_object (src/d_simple_discretization_2d.cuh:89-131,
+ * examples/advection_2d/k_advection_2d.cu:45-100): builds the mesh topology,
+ * geometry and operator matrices from vertex coordinates (x, y interleaved, as
+ * simple_triangular_mesh_2d::fill_vertices takes them) and counter-clockwise
+ * triangles (fill_connectivity), and uploads them to the current device. */
+int dgc_create(int num_vertices, const double* vertex_xy, int num_cells, const int32_t* cells,
+               const dgc_problem_desc* desc, dgc_handle* out);
+
+/* Replaces destroy_simple_discretization_2d_on_device / destroy_device_object
+ * (src/d_simple_discretization_2d.cuh:133-152). */
+int dgc_destroy(dgc_handle h);
+
+const char* dgc_last_error(void);
+int dgc_get_info(dgc_handle h, dgc_info* out);
+
+/* Physical coordinates of the nodes, host arrays [cell][node] (replaces the
+ * position output of initialize_dofs, advection_2d.h:107-130). */
+int dgc_node_coordinates(dgc_handle h, double* x, double* y);
+
+/* Host copy of an operator matrix (row-major, FP64): Dr / Ds (Np x Np),
+ * LIFT (Np x 3 Nfp), mass, Vandermonde (replaces reading m_Dr/m_Ds/m_L). */
+int dgc_get_operator(dgc_handle h, int which, double* out);
+
+/* Replace the operator matrices by caller-supplied FP64 ones (e.g. the
+ * reference's own m_Dr, m_Ds, m_L, which k_advection_2d.cu:60-62 copies to
+ * __constant__ memory).  form 0 = weak (advection/Maxwell), 1 = strong. */
+int dgc_set_operators(dgc_handle h, int form, const double* Dr, const double* Ds, const double* L);
+
+/* Layout conversion between the native layout and the reference's CPU or
+ * GPU layout; both buffers on the device, in the handle's precision. */
+int dgc_to_native(dgc_handle h, int src_layout, const void* src, void* dst, void* stream);
+int dgc_from_native(dgc_handle h, int dst_layout, const void* src, void* dst, void* stream);
+
+/* One evaluation of the semi-discrete operator: out = L_h(q, t).  Replaces
+ * device_SemiDiscOp_wrapper<Op>::operator()(in, size, t, out)
+ * (src/device_SemiDiscOp_wrapper.cuh:52-57).  q and out must not alias. */
+int dgc_rhs(dgc_handle h, const void* q, double t, void* out, void* stream);
+
+/* out = a x + y over the state vector.  Replaces k_axpy_auto / axpy_n
+ * (src/k_axpy.cuh:47-55, src/axpy.h:112-122). */
+int dgc_axpy(dgc_handle h, double a, const void* x, const void* y, void* out, void* stream);
+
+/* One classical RK4 step in place on q, fused into 4 launches (replaces
+ * dgc::rk4 with its 4 operator calls and 8 axpy launches,
+ * src/explicit_runge_kutta.h:33-51).  work: 3 state vectors of scratch. */
+int dgc_rk4_step(dgc_handle h, void* q, double t, double dt, void* const* work, void* stream);
+
+/* One low-storage RK4 step (Carpenter-Kennedy, 5 stages, each one fused
+ * launch).  Reads q_in, writes the new state to q_out; q_in is used as
+ * scratch and its contents are destroyed; res is the LSERK residual register
+ * (zero it before the first step).  No reference counterpart (the reference
+ * integrates with classical RK4 only). */
+int dgc_lserk4_step(dgc_handle h, void* q_in, void* q_out, void* res, double t, double dt, void* stream);
+
+/* One LSERK4 stage (stage in 0..4) as a single fused launch:
+ * res = a_s res + dt L_h(q_in, t + c_s dt);  q_out = q_in + b_s res.
+ * dgc_lserk4_step is these five stages with q_in / q_out alternating. */
+int dgc_lserk4_stage(dgc_handle h, int stage, const void* q_in, void* q_out, void* res, double t, double dt,
+                     void* stream);
+
+/* nsteps LSERK4 steps starting from qa at time t0; buffers ping-pong between
+ * qa and qb; *final_state receives the buffer holding the result.  With
+ * use_graph != 0 the launches are replayed from a captured CUDA graph. */
+int dgc_lserk4_run(dgc_handle h, void* qa, void* qb, void* res, double t0, double dt, int nsteps,
+                   int use_graph, void** final_state, void* stream);
+
+/* Synchronise the handle's device status word: DGC_OK, or DGC_ERR_DEVICE if a
+ * kernel recorded an error since the last call (the word is then cleared). */
+int dgc_check_device_status(dgc_handle h, int* code);
+
+/* Number of kernels this handle has launched (captured graph replays count
+ * each kernel they contain). */
+int64_t dgc_launch_count(dgc_handle h);
+
+/* ---- host-only set-up queries (no GPU needed) ---------------------------- */
+
+/* Reference-element nodes of order N (alpha_optimized_nodes_triangle::
+ * node_positions, src/alpha_optimized_nodes_triangle.h:104-141). */
+int dgc_ref_nodes(int order, double* r, double* s);
+
+/* An operator matrix of order N, row-major FP64 (the m_Dr / m_Ds / m_L built
+ * in examples/advection_2d/advection_2d.h:78-101 and src/laplace_2d.h:88-112). */
+int dgc_ref_operator(int order, int which, double* out);
+
+/* Mesh validation, topology and geometry on the host: geom [K][16] doubles
+ * (rx, ry, sx, sy, J, faceJ[3], nx[3], ny[3], pad), nbr [K][4] int32
+ * ((cell << 2 | face) of the twin face, or -(1 + b) for boundary face b, in
+ * the order of simple_discretization_2d::fill_cell_interfaces,
+ * src/simple_discretization_2d.h:136-162).  Any output may be NULL. */
+int dgc_host_mesh(int num_vertices, const double* vertex_xy, int num_cells, const int32_t* cells, int order,
+                  double* geom, int32_t* nbr, int* num_boundary_faces);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
