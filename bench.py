@@ -194,6 +194,78 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def measure_e2e(D32, bufs, res, flush, stream, t, dt, steps, ws, dofs, barrier):
+    """Per step through the C ABI with pinned host buffers: H2D of the state,
+    one LSERK4 step (dgc_lserk4_step), D2H of the new state."""
+    import torch
+    h_state = torch.empty(D32.state_len, dtype=torch.float32, pin_memory=True)
+    h_state.copy_(bufs[0].cpu())
+    h_out = torch.empty_like(h_state)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    barrier()
+    for it in range(steps):
+        flush.fill_(float(it))
+        evs[it][0].record(stream)
+        bufs[0].copy_(h_state, non_blocking=True)
+        D32.lserk4_step(bufs[0], bufs[1], res, t, dt)
+        h_out.copy_(bufs[1], non_blocking=True)
+        evs[it][1].record(stream)
+    barrier()
+    ms = float(np.mean([a.elapsed_time(b) for a, b in evs]))
+    if ws > 1:
+        import torch.distributed as tdist
+        tt = torch.tensor([ms], device="cuda")
+        tdist.all_reduce(tt, op=tdist.ReduceOp.MAX)
+        ms = float(tt.item())
+    nbytes = D32.state_len * 4
+    return {"value": ws * dofs * 5 / (ms * 1e-3) / 1e9, "unit": UNIT, "h2d_bytes_per_step": nbytes,
+            "d2h_bytes_per_step": nbytes, "ms_per_step": ms,
+            "path": "dgc_lserk4_step via ctypes, pinned host state in and out every step"}
+
+
+def measure_fp64(dg, m, q_init, dt, flush, stream, steps, dofs):
+    import torch
+    D64 = dg.Discretization(m, "maxwell_te", ORDER, dg.F64)
+    a, b, r = D64.upload(q_init), D64.empty_state(), D64.empty_state()
+    for _ in range(3):
+        D64.lserk4_step(a, b, r, 0.0, dt)
+        a, b = b, a
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for it in range(steps):
+        flush.fill_(float(it))
+        evs[it][0].record(stream)
+        D64.lserk4_step(a, b, r, 0.0, dt)
+        evs[it][1].record(stream)
+        a, b = b, a
+    torch.cuda.synchronize()
+    ms = float(np.mean([x.elapsed_time(y) for x, y in evs]))
+    D64.check()
+    return D64, {"value": dofs * 5 / (ms * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": ms, "steps": steps}
+
+
+def measure_accuracy(dg, D32, D64, q_init, x, y, dt):
+    """Both precisions from the same initial data to T = 1 (graph-replayed
+    LSERK4); relative L2 errors against the exact cavity mode and each other."""
+    import torch
+    nsteps = int(np.ceil(1.0 / dt))
+    dtT = 1.0 / nsteps
+    t0 = time.perf_counter()
+    f32 = D32.lserk4_run(D32.upload(q_init), D32.empty_state(), D32.empty_state(), 0.0, dtT, nsteps, graph=True)
+    torch.cuda.synchronize()
+    t32 = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    f64 = D64.lserk4_run(D64.upload(q_init), D64.empty_state(), D64.empty_state(), 0.0, dtT, nsteps, graph=True)
+    torch.cuda.synchronize()
+    t64 = time.perf_counter() - t0
+    ex = te_exact(x, y, 1.0).reshape(-1)
+    u32, u64 = D32.download(f32), D64.download(f64)
+    nrm = np.linalg.norm(ex)
+    return {"T": 1.0, "steps": nsteps, "rel_l2_fp32_vs_exact": float(np.linalg.norm(u32 - ex) / nrm),
+            "rel_l2_fp64_vs_exact": float(np.linalg.norm(u64 - ex) / nrm),
+            "rel_l2_fp32_vs_fp64": float(np.linalg.norm(u32 - u64) / np.linalg.norm(u64)),
+            "fp32_run_s": t32, "fp64_run_s": t64}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -202,9 +274,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 plain-path timing")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end (host buffer) timing")
     args = ap.parse_args()
-    if args.warmup < 3:
-        args.warmup = 3
+    args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return run_reference(args)
 
@@ -232,7 +305,6 @@ def main():
     dt = 0.5 * D32.info.min_edge / (ORDER + 1) ** 2
     dofs = 3 * Np * K
     stream = torch.cuda.current_stream()
-
     qa = D32.upload(q_init)
     qb, res = D32.empty_state(), D32.empty_state()
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
@@ -264,10 +336,10 @@ def main():
     barrier()
     wall = time.perf_counter() - wall0
     launches = D32.launch_count() - launches0
+    clocks = sampler.stop()
     step_ms = np.array([events[i][0].elapsed_time(events[i][5]) for i in range(args.steps)])
     stage_ms = np.array([[events[i][s].elapsed_time(events[i][s + 1]) for s in range(5)]
                          for i in range(args.steps)])
-    clocks = sampler.stop()
     D32.check()
     my_ms = float(step_ms.mean())
     if ws > 1:
@@ -277,99 +349,41 @@ def main():
         my_ms = float(tt.item())
     value = ws * dofs * 5 / (my_ms * 1e-3) / 1e9
 
-    # ---- end to end through the C ABI with host buffers (pinned), per step:
-    # H2D of the state, one LSERK4 step (dgc_lserk4_step), D2H of the new state
-    h_state = torch.empty(D32.state_len, dtype=torch.float32, pin_memory=True)
-    h_state.copy_(bufs[0].cpu())
-    h_out = torch.empty_like(h_state)
-    ev_e2e = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-              for _ in range(args.steps)]
-    barrier()
-    for it in range(args.steps):
-        flush.fill_(float(it))
-        ev_e2e[it][0].record(stream)
-        bufs[0].copy_(h_state, non_blocking=True)
-        D32.lserk4_step(bufs[0], bufs[1], res, t, dt)
-        h_out.copy_(bufs[1], non_blocking=True)
-        ev_e2e[it][1].record(stream)
-    barrier()
-    e2e_ms = float(np.mean([a.elapsed_time(b) for a, b in ev_e2e]))
-    if ws > 1:
-        import torch.distributed as tdist
-        tt = torch.tensor([e2e_ms], device="cuda")
-        tdist.all_reduce(tt, op=tdist.ReduceOp.MAX)
-        e2e_ms = float(tt.item())
-    nbytes_state = D32.state_len * 4
-    e2e = {"value": ws * dofs * 5 / (e2e_ms * 1e-3) / 1e9, "unit": UNIT,
-           "h2d_bytes_per_step": nbytes_state, "d2h_bytes_per_step": nbytes_state,
-           "ms_per_step": e2e_ms, "path": "dgc_lserk4_step via ctypes, pinned host state in/out"}
-
-    # ---- roofline of the dominant kernel (the fused RHS + LSERK4 stage)
-    s = 4
-    alg_bytes_elem = 4 * 3 * Np * s + 14 * 8 + 3 * 4
+    # roofline of the dominant kernel (the fused RHS + LSERK4 stage): compulsory
+    # bytes per element = read q, read res, write res, write q (3 fields x Np x 4 B
+    # each) + 14 FP64 geometric factors + 3 int32 neighbour indices
+    alg_bytes_elem = 4 * 3 * Np * 4 + 14 * 8 + 3 * 4
     alg_bytes = alg_bytes_elem * K
     launch_ms = float(stage_ms.mean())
     achieved = alg_bytes / (launch_ms * 1e-3) / 1e9
     peak, peak_kind = measured_peak()
-    traffic = read_traffic()
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                "frac": achieved / peak, "traffic": read_traffic(), "peak_source": peak_kind,
                 "kernel": "dgk::dg_rhs_kernel<float,6,PHYS_TE> (LSERK4 stage)",
-                "alg_bytes_per_launch": alg_bytes, "launch_ms": launch_ms,
-                "stage_ms": [float(v) for v in stage_ms.mean(axis=0)]}
+                "alg_bytes_per_launch": alg_bytes, "alg_bytes_per_element": alg_bytes_elem,
+                "launch_ms": launch_ms, "stage_ms": [float(v) for v in stage_ms.mean(axis=0)]}
 
-    # ---- FP64 plain path on the same workload
-    D64 = dg.Discretization(m, "maxwell_te", ORDER, dg.F64)
-    a64 = D64.upload(q_init)
-    b64, r64 = D64.empty_state(), D64.empty_state()
-    for _ in range(3):
-        D64.lserk4_step(a64, b64, r64, 0.0, dt)
-        a64, b64 = b64, a64
-    n64 = max(3, min(args.steps, 10))
-    ev64 = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n64)]
-    for it in range(n64):
-        flush.fill_(float(it))
-        ev64[it][0].record(stream)
-        D64.lserk4_step(a64, b64, r64, 0.0, dt)
-        ev64[it][1].record(stream)
-        a64, b64 = b64, a64
-    torch.cuda.synchronize()
-    ms64 = float(np.mean([a.elapsed_time(b) for a, b in ev64]))
-    fp64 = {"value": dofs * 5 / (ms64 * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": ms64}
-
-    # ---- accuracy at T = 1 (both precisions, same initial data), rank 0 only
+    e2e = None if args.no_e2e else measure_e2e(D32, bufs, res, flush, stream, t, dt, args.steps, ws, dofs, barrier)
+    D64, fp64 = (None, None) if args.no_fp64 else measure_fp64(dg, m, q_init, dt, flush, stream,
+                                                                max(3, min(args.steps, 10)), dofs)
     accuracy = None
-    if rank == 0 and not args.no_accuracy:
-        nsteps = int(np.ceil(1.0 / dt))
-        dtT = 1.0 / nsteps
-        res32 = D32.empty_state()
-        f32 = D32.lserk4_run(D32.upload(q_init), D32.empty_state(), res32, 0.0, dtT, nsteps, graph=True)
-        r64b = D64.empty_state()
-        t0 = time.perf_counter()
-        f64 = D64.lserk4_run(D64.upload(q_init), D64.empty_state(), r64b, 0.0, dtT, nsteps, graph=True)
-        torch.cuda.synchronize()
-        ex = te_exact(x, y, 1.0).reshape(-1)
-        u32, u64 = D32.download(f32), D64.download(f64)
-        nrm = np.linalg.norm(ex)
-        accuracy = {"T": 1.0, "steps": nsteps, "rel_l2_fp32_vs_exact": float(np.linalg.norm(u32 - ex) / nrm),
-                    "rel_l2_fp64_vs_exact": float(np.linalg.norm(u64 - ex) / nrm),
-                    "rel_l2_fp32_vs_fp64": float(np.linalg.norm(u32 - u64) / np.linalg.norm(u64)),
-                    "fp64_run_s": time.perf_counter() - t0}
-
+    if rank == 0 and D64 is not None and not args.no_accuracy:
+        accuracy = measure_accuracy(dg, D32, D64, q_init, x, y, dt)
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         csteps = 10
         cg, csec = oracle_sample(csteps, 1)
         cpu = {"value": cg, "unit": UNIT, "cores": 1, "kind": "port",
-               "sample": f"{csteps} full LSERK4 steps (serial C port of the reference CPU operator, FP64, "
-                         f"{csec:.2f} s/step), host {cpu_model()}"}
+               "sample": f"{csteps} full LSERK4 steps of the workload (serial C port of the reference CPU "
+                         f"operator, FP64, {csec:.2f} s/step), host {cpu_model()}"}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": my_ms, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config_dict(ws),
                 "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu,
-                "clocks": clocks, "fp64_plain": fp64, "speedup_mixed_vs_fp64": value / ws / fp64["value"],
+                "clocks": clocks, "fp64_plain": fp64,
+                "speedup_mixed_vs_fp64": (value / ws / fp64["value"]) if fp64 else None,
                 "accuracy": accuracy, "wall_s_timed_region": wall}
         print(json.dumps(line))
     if ws > 1:
