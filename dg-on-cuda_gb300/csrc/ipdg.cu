@@ -1,20 +1,567 @@
-// ipdg.cu -- matrix-free laplace_2d (IPDG) apply and preconditioned CG.
+// ipdg.cu -- host side of the matrix-free laplace_2d operator and its solvers:
+// block-Jacobi set-up on the GPU, the device-driven PCG loop (scalars stay in
+// device memory; three-iteration chunks replayed from a CUDA graph), and mixed
+// precision iterative refinement (FP32 inner PCG, FP64 residuals).
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
 #include "dgc_internal.hpp"
+#include "ipdg.cuh"
+
+namespace dgk {
+
+enum IpdgKernel : int { IK_GRAD_PLAIN, IK_GRAD_PCG, IK_DIV_LAPLACE, IK_DIV_SPD, IK_DIV_SPD_DOT, IK_DIV_RESID,
+                        IK_UPDATE, IK_START };
+
+template <typename R, int N>
+const void* ipdg_fn(int kind) {
+  switch (kind) {
+    case IK_GRAD_PLAIN: return (const void*)ipdg_grad_kernel<R, N, GRAD_PLAIN>;
+    case IK_GRAD_PCG: return (const void*)ipdg_grad_kernel<R, N, GRAD_PCG>;
+    case IK_DIV_LAPLACE: return (const void*)ipdg_div_kernel<R, N, DIV_LAPLACE>;
+    case IK_DIV_SPD: return (const void*)ipdg_div_kernel<R, N, DIV_SPD>;
+    case IK_DIV_SPD_DOT: return (const void*)ipdg_div_kernel<R, N, DIV_SPD_DOT>;
+    case IK_DIV_RESID: return (const void*)ipdg_div_kernel<R, N, DIV_RESID>;
+    case IK_UPDATE: return (const void*)pcg_update_kernel<R, N>;
+    case IK_START: return (const void*)pcg_start_kernel<R, N>;
+    default: return nullptr;
+  }
+}
+
+template <typename R, int N>
+cudaError_t ipdg_launch_n(int kind, const IpdgParams& p, int sm, cudaStream_t s) {
+  using C = IpdgConfig<R, N>;
+  static std::once_flag once[8];
+  static int bps[8];
+  static cudaError_t st[8];
+  const void* fn = ipdg_fn<R, N>(kind);
+  if (!fn) return cudaErrorInvalidValue;
+  const bool dyn = kind <= IK_DIV_RESID;
+  const int smem = dyn ? (int)C::kSmem : 0;
+  std::call_once(once[kind], [&] {
+    st[kind] = cudaSuccess;
+    if (dyn) st[kind] = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (st[kind] == cudaSuccess) st[kind] = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps[kind], fn, 256, smem);
+  });
+  if (st[kind] != cudaSuccess) return st[kind];
+  const int ntiles = (p.K + C::TE - 1) / C::TE;
+  int grid = sm * (bps[kind] > 0 ? bps[kind] : 1);
+  if (grid > ntiles) grid = ntiles;
+  void* args[] = {const_cast<IpdgParams*>(&p)};
+  return cudaLaunchKernel(fn, dim3(grid), dim3(256), args, smem, s);
+}
+
+template <typename R>
+cudaError_t ipdg_launch(int N, int kind, const IpdgParams& p, int sm, cudaStream_t s) {
+  switch (N) {
+    case 1: return ipdg_launch_n<R, 1>(kind, p, sm, s);
+    case 2: return ipdg_launch_n<R, 2>(kind, p, sm, s);
+    case 3: return ipdg_launch_n<R, 3>(kind, p, sm, s);
+    case 4: return ipdg_launch_n<R, 4>(kind, p, sm, s);
+    case 5: return ipdg_launch_n<R, 5>(kind, p, sm, s);
+    case 6: return ipdg_launch_n<R, 6>(kind, p, sm, s);
+    case 7: return ipdg_launch_n<R, 7>(kind, p, sm, s);
+    case 8: return ipdg_launch_n<R, 8>(kind, p, sm, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template <int N>
+cudaError_t diag_blocks_n(int K, int dirichlet, const double* geom, const int4* nbr, const double* tau,
+                          const double* Dr, const double* Ds, const double* L, const double* M, double* blocks,
+                          float* blocks32, int bstr, int* status, cudaStream_t s) {
+  using O = Order<N>;
+  const int64_t n = (int64_t)K * O::Np;
+  ipdg_diag_blocks_kernel<N><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(K, dirichlet, geom, nbr, tau, Dr, Ds, L,
+                                                                         M, blocks, bstr);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  block_invert_kernel<N><<<K, 128, 0, s>>>(K, blocks, blocks32, bstr, status);
+  return cudaGetLastError();
+}
+
+cudaError_t diag_blocks(int N, int K, int dirichlet, const double* geom, const int4* nbr, const double* tau,
+                        const double* Dr, const double* Ds, const double* L, const double* M, double* blocks,
+                        float* blocks32, int bstr, int* status, cudaStream_t s) {
+#define DGK_DB(n) \
+  case n: return diag_blocks_n<n>(K, dirichlet, geom, nbr, tau, Dr, Ds, L, M, blocks, blocks32, bstr, status, s);
+  switch (N) {
+    DGK_DB(1) DGK_DB(2) DGK_DB(3) DGK_DB(4) DGK_DB(5) DGK_DB(6) DGK_DB(7) DGK_DB(8)
+    default: return cudaErrorInvalidValue;
+  }
+#undef DGK_DB
+}
+
+// ---------------------------------------------------------------- vector kernels
+__global__ void k_r64_to_r32(size_t n, const double* __restrict__ r, double scale, float* __restrict__ out) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    out[i] = (float)(r[i] * scale);
+}
+__global__ void k_x_update(size_t n, double* __restrict__ x, const float* __restrict__ d, double scale) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    x[i] += scale * (double)d[i];
+}
+template <typename R>
+__global__ void k_dot(size_t n, const R* __restrict__ a, const R* __restrict__ b, double* out) {
+  __shared__ double red[16];
+  double s = 0.0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    s += (double)a[i] * (double)b[i];
+  s = block_sum(s, red);
+  if (threadIdx.x == 0) atomicAdd(out, s);
+}
+__global__ void k_add(size_t n, double* __restrict__ x, const double* __restrict__ d) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    x[i] += d[i];
+}
+// out = J_k M f_k (mass-weighted right-hand side), one thread per node
+__global__ void k_mass(int K, int Np, int NpP, const double* __restrict__ geom, const double* __restrict__ M,
+                       const double* __restrict__ f, double* __restrict__ out) {
+  const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (g >= (int64_t)K * Np) return;
+  const int k = (int)(g / Np), i = (int)(g % Np);
+  double s = 0.0;
+  for (int j = 0; j < Np; ++j) s += M[i * Np + j] * f[(size_t)k * NpP + j];
+  out[(size_t)k * NpP + i] = geom[(size_t)k * 16 + 4] * s;
+}
+// start of a CG solve: relative tolerance against the initial residual
+__global__ void k_cg_start(CgScalars* cg, double tol2, int maxit) {
+  cg->bb = cg->rr[0];
+  cg->tol2 = tol2;
+  cg->maxit = maxit;
+  if (cg->rr[0] == 0.0) cg->done = 1;
+}
+// convergence bookkeeping, one thread: done when rr <= tol2 * bb or iters >= maxit
+__global__ void k_cg_check(CgScalars* cg, int slot) {
+  if (cg->done) return;
+  cg->iters += 1;
+  if (cg->rr[slot] <= cg->tol2 * cg->bb) cg->done = 1;
+  else if (cg->iters >= cg->maxit) cg->done = 2;
+}
+
+}  // namespace dgk
 
 namespace dgc {
 
-struct IpdgState {};
+struct IpdgState {
+  int bstr = 0;
+  bool ready = false;          // preconditioner built
+  double* binv64 = nullptr;
+  float* binv32 = nullptr;
+  void* mass64 = nullptr;      // padded M in FP64 / FP32
+  void* mass32 = nullptr;
+  double* dense64 = nullptr;   // row-major Dr | Ds | L | M (FP64) for the block set-up
+  // workspace: FP64 and FP32 vector sets
+  double* w64[10] = {};
+  float* w32[10] = {};
+  dgk::CgScalars* cg = nullptr;   // [2]: fp64 solve, fp32 inner solve
+  double* dots = nullptr;         // scratch dot products
+  dgk::CgScalars* h_cg = nullptr; // pinned host mirror
+  double* h_dots = nullptr;
+  // graphs of 3-iteration chunks per precision
+  cudaGraphExec_t chunk[2] = {nullptr, nullptr};
+  const void* chunk_key[2] = {nullptr, nullptr};
+};
 
-int ipdg_init(dgc_handle_s* h) {
-  (void)h;
+namespace {
+
+int cuda_err(cudaError_t e, const char* what) {
+  std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+  return set_error(DGC_ERR_CUDA, m.c_str());
+}
+#define CKI(call)                                    \
+  do {                                               \
+    cudaError_t e_ = (call);                         \
+    if (e_ != cudaSuccess) return cuda_err(e_, #call); \
+  } while (0)
+
+size_t nvec(const dgc_handle_s* h) { return (size_t)h->K * h->NpP; }
+
+template <typename R>
+dgk::IpdgParams base(const dgc_handle_s* h) {
+  dgk::IpdgParams p{};
+  p.K = h->K;
+  p.dirichlet = h->desc.dirichlet;
+  p.geom = h->d_geom;
+  p.nbr = reinterpret_cast<const int4*>(h->d_nbr);
+  p.tau = h->d_tau;
+  p.mats = sizeof(R) == 8 ? h->d_mats64[1] : h->d_mats32[1];
+  p.mass = sizeof(R) == 8 ? h->ipdg->mass64 : h->ipdg->mass32;
+  p.binv = sizeof(R) == 8 ? (const void*)h->ipdg->binv64 : (const void*)h->ipdg->binv32;
+  p.status = h->d_status;
+  return p;
+}
+
+template <typename R>
+int launch(dgc_handle_s* h, int kind, const dgk::IpdgParams& p, cudaStream_t s) {
+  cudaError_t e = dgk::ipdg_launch<R>(h->N, kind, p, h->sm_count, s);
+  if (e != cudaSuccess) return cuda_err(e, "ipdg kernel launch");
+  ++h->launches;
   return DGC_OK;
 }
 
+int grid_for(const dgc_handle_s* h, size_t n) {
+  return (int)std::min<size_t>((n + 255) / 256, (size_t)h->sm_count * 8);
+}
+
+template <typename R>
+R* wv(dgc_handle_s* h, int i) {
+  if constexpr (sizeof(R) == 8) return h->ipdg->w64[i];
+  else return h->ipdg->w32[i];
+}
+
+// workspace slots
+// (search directions rotate through W_P .. W_P + 2 by iteration slot, so that
+// a grad pass never overwrites the direction its neighbours are still reading)
+enum { W_X = 0, W_R = 1, W_Z = 2, W_P = 3, W_AP = 6, W_QX = 7, W_QY = 8, W_T = 9, W_COUNT = 10 };
+
+}  // namespace
+
+int ipdg_build_preconditioner(dgc_handle_s* h, cudaStream_t s) {
+  IpdgState* st = h->ipdg;
+  if (st->ready) return DGC_OK;
+  if (!h->desc.dirichlet) return set_error(DGC_ERR_UNSUPPORTED, "block-Jacobi CG needs Dirichlet boundaries (SPD form)");
+  cudaError_t e = dgk::diag_blocks(h->N, h->K, 1, h->d_geom, reinterpret_cast<const int4*>(h->d_nbr), h->d_tau,
+                                   st->dense64, st->dense64 + (size_t)h->Np * h->Np,
+                                   st->dense64 + (size_t)2 * h->Np * h->Np,
+                                   st->dense64 + (size_t)2 * h->Np * h->Np + (size_t)h->Np * 3 * h->Nfp,
+                                   st->binv64, st->binv32, st->bstr, h->d_status, s);
+  if (e != cudaSuccess) return cuda_err(e, "block-Jacobi set-up");
+  h->launches += 2;
+  st->ready = true;
+  return DGC_OK;
+}
+
+int upload_ipdg_matrices(dgc_handle_s* h) {
+  IpdgState* st = h->ipdg;
+  const int Np = h->Np, NF = 3 * h->Nfp;
+  std::vector<double> m64((size_t)st->bstr, 0.0);
+  std::vector<float> m32((size_t)st->bstr, 0.0f);
+  for (int i = 0; i < Np * Np; ++i) {
+    m64[i] = h->re.M[i];
+    m32[i] = (float)h->re.M[i];
+  }
+  CKI(cudaMemcpy(st->mass64, m64.data(), m64.size() * 8, cudaMemcpyHostToDevice));
+  CKI(cudaMemcpy(st->mass32, m32.data(), m32.size() * 4, cudaMemcpyHostToDevice));
+  std::vector<double> dense;
+  dense.insert(dense.end(), h->re.Drs.begin(), h->re.Drs.end());
+  dense.insert(dense.end(), h->re.Dss.begin(), h->re.Dss.end());
+  dense.insert(dense.end(), h->re.Ls.begin(), h->re.Ls.end());
+  dense.insert(dense.end(), h->re.M.begin(), h->re.M.end());
+  (void)NF;
+  CKI(cudaMemcpy(st->dense64, dense.data(), dense.size() * 8, cudaMemcpyHostToDevice));
+  st->ready = false;
+  return DGC_OK;
+}
+
+int ipdg_init(dgc_handle_s* h) {
+  if (h->desc.physics != DGC_LAPLACE) return DGC_OK;
+  if (h->desc.tau != DGC_TAU_ONE && h->desc.tau != DGC_TAU_SCALED)
+    return set_error(DGC_ERR_ARG, "unknown tau mode");
+  auto* st = new IpdgState();
+  h->ipdg = st;
+  const int Np = h->Np, NF = 3 * h->Nfp;
+  st->bstr = (Np * Np + 3) / 4 * 4;
+  if (h->desc.tau == DGC_TAU_ONE) {
+    std::vector<double> ones((size_t)4 * h->K, 1.0);
+    CKI(cudaMemcpy(h->d_tau, ones.data(), ones.size() * 8, cudaMemcpyHostToDevice));
+  }
+  CKI(cudaMalloc(&st->mass64, (size_t)st->bstr * 8));
+  CKI(cudaMalloc(&st->mass32, (size_t)st->bstr * 4));
+  CKI(cudaMalloc(&st->dense64, ((size_t)3 * Np * Np + (size_t)Np * NF) * 8));
+  CKI(cudaMalloc(&st->binv64, (size_t)h->K * st->bstr * 8));
+  CKI(cudaMalloc(&st->binv32, (size_t)h->K * st->bstr * 4));
+  CKI(cudaMemset(st->binv64, 0, (size_t)h->K * st->bstr * 8));
+  CKI(cudaMemset(st->binv32, 0, (size_t)h->K * st->bstr * 4));
+  const size_t n = nvec(h);
+  for (int i = 0; i < W_COUNT; ++i) {
+    CKI(cudaMalloc(&st->w64[i], n * 8));
+    CKI(cudaMalloc(&st->w32[i], n * 4));
+    CKI(cudaMemset(st->w64[i], 0, n * 8));
+    CKI(cudaMemset(st->w32[i], 0, n * 4));
+  }
+  CKI(cudaMalloc(&st->cg, 2 * sizeof(dgk::CgScalars)));
+  CKI(cudaMemset(st->cg, 0, 2 * sizeof(dgk::CgScalars)));
+  CKI(cudaMalloc(&st->dots, 64));
+  CKI(cudaMallocHost(&st->h_cg, 2 * sizeof(dgk::CgScalars)));
+  CKI(cudaMallocHost(&st->h_dots, 64));
+  return upload_ipdg_matrices(h);
+}
+
 void ipdg_free(dgc_handle_s* h) {
-  delete h->ipdg;
+  IpdgState* st = h->ipdg;
+  if (!st) return;
+  for (int i = 0; i < 2; ++i)
+    if (st->chunk[i]) cudaGraphExecDestroy(st->chunk[i]);
+  cudaFree(st->binv64);
+  cudaFree(st->binv32);
+  cudaFree(st->mass64);
+  cudaFree(st->mass32);
+  cudaFree(st->dense64);
+  for (int i = 0; i < W_COUNT; ++i) {
+    cudaFree(st->w64[i]);
+    cudaFree(st->w32[i]);
+  }
+  cudaFree(st->cg);
+  cudaFree(st->dots);
+  cudaFreeHost(st->h_cg);
+  cudaFreeHost(st->h_dots);
+  delete st;
   h->ipdg = nullptr;
 }
 
-void ipdg_operators_changed(dgc_handle_s* h) { (void)h; }
+void ipdg_operators_changed(dgc_handle_s* h) {
+  if (h->ipdg) upload_ipdg_matrices(h);
+}
+
+namespace {
+
+int check_laplace(dgc_handle_s* h) {
+  if (!h) return set_error(DGC_ERR_ARG, "null handle");
+  if (h->desc.physics != DGC_LAPLACE || !h->ipdg)
+    return set_error(DGC_ERR_UNSUPPORTED, "operation needs a DGC_LAPLACE handle");
+  return DGC_OK;
+}
+
+// grad + div of u into out, with the given div mode (and b for residuals)
+template <typename R>
+int apply(dgc_handle_s* h, int div_kind, const R* u, R* out, const R* b, double* dot, cudaStream_t s) {
+  dgk::IpdgParams p = base<R>(h);
+  p.u = u;
+  p.qx = wv<R>(h, W_QX);
+  p.qy = wv<R>(h, W_QY);
+  if (int rc = launch<R>(h, dgk::IK_GRAD_PLAIN, p, s)) return rc;
+  p.du_src = u;
+  p.out = out;
+  p.b = b;
+  p.dot_out = dot;
+  return launch<R>(h, div_kind, p, s);
+}
+
+// one CG iteration (three launches) for slot i mod 3
+template <typename R>
+int cg_iteration(dgc_handle_s* h, int cgi, int slot, int first, cudaStream_t s) {
+  dgk::IpdgParams p = base<R>(h);
+  p.cg = h->ipdg->cg + cgi;
+  p.slot = slot;
+  p.first = first;
+  p.u = wv<R>(h, W_Z);
+  p.p = wv<R>(h, W_P + slot);
+  p.p_old = wv<R>(h, W_P + (slot + 2) % 3);
+  p.qx = wv<R>(h, W_QX);
+  p.qy = wv<R>(h, W_QY);
+  if (int rc = launch<R>(h, dgk::IK_GRAD_PCG, p, s)) return rc;
+  p.du_src = wv<R>(h, W_P + slot);
+  p.out = wv<R>(h, W_AP);
+  if (int rc = launch<R>(h, dgk::IK_DIV_SPD_DOT, p, s)) return rc;
+  p.x = wv<R>(h, W_X);
+  p.r = wv<R>(h, W_R);
+  p.z = wv<R>(h, W_Z);
+  p.Ap = wv<R>(h, W_AP);
+  if (int rc = launch<R>(h, dgk::IK_UPDATE, p, s)) return rc;
+  dgk::k_cg_check<<<1, 1, 0, s>>>(h->ipdg->cg + cgi, (slot + 1) % 3);
+  CKI(cudaGetLastError());
+  ++h->launches;
+  return DGC_OK;
+}
+
+// PCG on S x = r0 with x = 0 initially (x, r in workspace slots W_X, W_R);
+// stops at ||r|| <= rtol ||r0|| or maxit.  Returns iterations via *iters.
+template <typename R>
+int pcg_core(dgc_handle_s* h, double rtol, int maxit, bool use_graph, int* iters, int* converged, cudaStream_t s) {
+  IpdgState* st = h->ipdg;
+  const int cgi = sizeof(R) == 8 ? 0 : 1;
+  dgk::CgScalars init{};
+  CKI(cudaMemcpyAsync(st->cg + cgi, &init, sizeof init, cudaMemcpyHostToDevice, s));
+  dgk::IpdgParams p = base<R>(h);
+  p.cg = st->cg + cgi;
+  p.r = wv<R>(h, W_R);
+  p.z = wv<R>(h, W_Z);
+  CKI(cudaMemsetAsync(wv<R>(h, W_X), 0, nvec(h) * sizeof(R), s));
+  for (int i = 0; i < 3; ++i) CKI(cudaMemsetAsync(wv<R>(h, W_P + i), 0, nvec(h) * sizeof(R), s));
+  if (int rc = launch<R>(h, dgk::IK_START, p, s)) return rc;
+  // bb = rr[0], tol2 = rtol^2 (device side, one thread)
+  dgk::k_cg_start<<<1, 1, 0, s>>>(st->cg + cgi, rtol * rtol, maxit);
+  CKI(cudaGetLastError());
+  if (int rc = cg_iteration<R>(h, cgi, 0, 1, s)) return rc;
+  const void* key = wv<R>(h, W_X);
+  if (use_graph && (!st->chunk[cgi] || st->chunk_key[cgi] != key)) {
+    if (st->chunk[cgi]) cudaGraphExecDestroy(st->chunk[cgi]);
+    st->chunk[cgi] = nullptr;
+    cudaStream_t cs;
+    CKI(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    int rc = DGC_OK;
+    const int64_t l0 = h->launches;
+    if (e == cudaSuccess) {
+      for (int i = 1; i <= 3 && rc == DGC_OK; ++i) rc = cg_iteration<R>(h, cgi, i % 3, 0, cs);
+      e = cudaStreamEndCapture(cs, &g);
+    }
+    h->launches = l0;
+    cudaStreamDestroy(cs);
+    if (rc != DGC_OK) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    if (e != cudaSuccess) return cuda_err(e, "capture CG chunk");
+    e = cudaGraphInstantiate(&st->chunk[cgi], g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_err(e, "instantiate CG chunk");
+    st->chunk_key[cgi] = key;
+  }
+  int done_it = 1;
+  const int chunks_per_check = 4;
+  while (true) {
+    for (int c = 0; c < chunks_per_check; ++c) {
+      if (use_graph) {
+        CKI(cudaGraphLaunch(st->chunk[cgi], s));
+        h->launches += 12;
+      } else {
+        for (int i = 1; i <= 3; ++i)
+          if (int rc = cg_iteration<R>(h, cgi, i % 3, 0, s)) return rc;
+      }
+      done_it += 3;
+    }
+    CKI(cudaMemcpyAsync(st->h_cg + cgi, st->cg + cgi, sizeof(dgk::CgScalars), cudaMemcpyDeviceToHost, s));
+    CKI(cudaStreamSynchronize(s));
+    if (st->h_cg[cgi].done) break;
+    if (done_it > maxit + 12) break;
+  }
+  *iters = st->h_cg[cgi].iters;
+  *converged = st->h_cg[cgi].done == 1;
+  return DGC_OK;
+}
+
+template <typename R>
+int true_residual(dgc_handle_s* h, const double* b64, const double* x64, double* r64, double* rr, cudaStream_t s) {
+  IpdgState* st = h->ipdg;
+  CKI(cudaMemsetAsync(st->dots, 0, 8, s));
+  if (int rc = apply<double>(h, dgk::IK_DIV_RESID, x64, r64, b64, st->dots, s)) return rc;
+  CKI(cudaMemcpyAsync(st->h_dots, st->dots, 8, cudaMemcpyDeviceToHost, s));
+  CKI(cudaStreamSynchronize(s));
+  *rr = st->h_dots[0];
+  return DGC_OK;
+}
+
+}  // namespace
 
 }  // namespace dgc
+
+using namespace dgc;
+
+extern "C" int dgc_laplace_apply(dgc_handle h, const void* u, void* out, void* stream) {
+  if (int rc = check_laplace(h)) return rc;
+  if (!u || !out || u == out) return set_error(DGC_ERR_ARG, "u and out must be distinct, non-null buffers");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  return h->prec == DGC_F64
+             ? apply<double>(h, dgk::IK_DIV_LAPLACE, (const double*)u, (double*)out, nullptr, nullptr, s)
+             : apply<float>(h, dgk::IK_DIV_LAPLACE, (const float*)u, (float*)out, nullptr, nullptr, s);
+}
+
+extern "C" int dgc_laplace_spd_apply(dgc_handle h, const void* u, void* out, void* stream) {
+  if (int rc = check_laplace(h)) return rc;
+  if (!u || !out || u == out) return set_error(DGC_ERR_ARG, "u and out must be distinct, non-null buffers");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  return h->prec == DGC_F64 ? apply<double>(h, dgk::IK_DIV_SPD, (const double*)u, (double*)out, nullptr, nullptr, s)
+                            : apply<float>(h, dgk::IK_DIV_SPD, (const float*)u, (float*)out, nullptr, nullptr, s);
+}
+
+extern "C" int dgc_pcg_solve(dgc_handle h, const double* b, double* x, const dgc_solve_opts* opts,
+                             dgc_solve_stats* stats, void* stream) {
+  if (int rc = check_laplace(h)) return rc;
+  if (!b || !x || !opts || b == x) return set_error(DGC_ERR_ARG, "b and x must be distinct, non-null buffers");
+  if (!(opts->rtol > 0.0) || opts->maxit <= 0) return set_error(DGC_ERR_ARG, "rtol must be > 0 and maxit > 0");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  IpdgState* st = h->ipdg;
+  if (int rc = ipdg_build_preconditioner(h, s)) return rc;
+  const auto t0 = std::chrono::steady_clock::now();
+  const size_t n = nvec(h);
+  dgc_solve_stats S{};
+  // ||b||^2
+  CKI(cudaMemsetAsync(st->dots, 0, 8, s));
+  dgk::k_dot<double><<<grid_for(h, n), 256, 0, s>>>(n, b, b, st->dots);
+  CKI(cudaGetLastError());
+  CKI(cudaMemcpyAsync(st->h_dots, st->dots, 8, cudaMemcpyDeviceToHost, s));
+  CKI(cudaStreamSynchronize(s));
+  const double bb = st->h_dots[0];
+  const double tol2 = opts->rtol * opts->rtol * bb;
+  double* r64 = st->w64[W_T];
+  double rr = 0.0;
+  // r = b - S x (x is the caller's initial guess)
+  if (int rc = true_residual<double>(h, b, x, r64, &rr, s)) return rc;
+  const bool graph = opts->use_graph != 0;
+  if (opts->mode == DGC_SOLVE_FP64_PCG) {
+    if (rr > tol2) {
+      // solve S d = r in FP64, then x += d
+      CKI(cudaMemcpyAsync(st->w64[W_R], r64, n * 8, cudaMemcpyDeviceToDevice, s));
+      int it = 0, conv = 0;
+      // aim a little below the target: CG tracks the recursive residual
+      const double rel = 0.5 * std::sqrt(tol2 / rr);
+      if (int rc = pcg_core<double>(h, rel, opts->maxit, graph, &it, &conv, s)) return rc;
+      S.inner_iterations = it;
+      S.iterations = it;
+      S.outer_iterations = 1;
+      dgk::k_add<<<grid_for(h, n), 256, 0, s>>>(n, x, st->w64[W_X]);
+      CKI(cudaGetLastError());
+      if (int rc = true_residual<double>(h, b, x, r64, &rr, s)) return rc;
+    }
+  } else if (opts->mode == DGC_SOLVE_MIXED_IR) {
+    const double inner = opts->inner_rtol > 0.0 ? opts->inner_rtol : 1e-4;
+    int outer = 0;
+    while (rr > tol2 && outer < opts->max_outer) {
+      const double nr = std::sqrt(rr);
+      dgk::k_r64_to_r32<<<grid_for(h, n), 256, 0, s>>>(n, r64, 1.0 / nr, st->w32[W_R]);
+      CKI(cudaGetLastError());
+      int it = 0, conv = 0;
+      const int budget = opts->maxit - S.inner_iterations;
+      if (budget <= 0) break;
+      if (int rc = pcg_core<float>(h, inner, budget, graph, &it, &conv, s)) return rc;
+      S.inner_iterations += it;
+      dgk::k_x_update<<<grid_for(h, n), 256, 0, s>>>(n, x, st->w32[W_X], nr);
+      CKI(cudaGetLastError());
+      ++outer;
+      if (int rc = true_residual<double>(h, b, x, r64, &rr, s)) return rc;
+    }
+    S.outer_iterations = outer;
+    S.iterations = S.inner_iterations;
+  } else {
+    return set_error(DGC_ERR_ARG, "unknown solve mode");
+  }
+  CKI(cudaStreamSynchronize(s));
+  S.final_relres = bb > 0.0 ? std::sqrt(rr / bb) : 0.0;
+  S.converged = rr <= tol2 ? 1 : 0;
+  S.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  if (stats) *stats = S;
+  if (!S.converged) return set_error(DGC_ERR_NOT_CONVERGED, "PCG did not reach the requested tolerance");
+  return DGC_OK;
+}
+
+extern "C" int dgc_mass_apply(dgc_handle h, const double* f, double* out, void* stream) {
+  if (int rc = check_laplace(h)) return rc;
+  if (!f || !out || f == out) return set_error(DGC_ERR_ARG, "f and out must be distinct, non-null buffers");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int64_t n = (int64_t)h->K * h->Np;
+  CKI(cudaMemsetAsync(out, 0, nvec(h) * 8, s));
+  dgk::k_mass<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(h->K, h->Np, h->NpP, h->d_geom, (const double*)h->ipdg->mass64,
+                                                      f, out);
+  CKI(cudaGetLastError());
+  ++h->launches;
+  return DGC_OK;
+}
+
+extern "C" int dgc_block_jacobi(dgc_handle h, double* blocks, void* stream) {
+  if (int rc = check_laplace(h)) return rc;
+  if (!blocks) return set_error(DGC_ERR_ARG, "null argument");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (int rc = ipdg_build_preconditioner(h, s)) return rc;
+  const int Np = h->Np, bs = h->ipdg->bstr;
+  CKI(cudaMemcpy2DAsync(blocks, (size_t)Np * Np * 8, h->ipdg->binv64, (size_t)bs * 8, (size_t)Np * Np * 8, h->K,
+                        cudaMemcpyDeviceToDevice, s));
+  return DGC_OK;
+}

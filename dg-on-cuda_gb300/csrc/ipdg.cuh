@@ -33,9 +33,10 @@ struct CgScalars {
   double pAp;
   double bb;        // ||b||^2 (of the system being solved)
   double tol2;      // stop when rr <= tol2 * bb
-  int done;         // set once converged; later kernels become no-ops
+  int done;         // set once converged (1) or out of iterations (2); later kernels become no-ops
   int iters;        // completed iterations
-  int pad[2];
+  int maxit;        // iteration budget of this solve
+  int pad;
 };
 
 struct IpdgParams {
@@ -48,7 +49,8 @@ struct IpdgParams {
   const void* mass;     // M (Np x Np, R), symmetric
   // grad pass
   const void* u;        // input u (GRAD_PLAIN) or z (GRAD_PCG)
-  void* p;              // GRAD_PCG: p (read p_old, write p)
+  void* p;              // GRAD_PCG: new search direction p (written); update: p (read)
+  const void* p_old;    // GRAD_PCG: previous search direction (a different buffer)
   void* qx;
   void* qy;
   // div pass
@@ -188,6 +190,7 @@ __global__ void __launch_bounds__(256) ipdg_grad_kernel(const IpdgParams p) {
   if (!t.init(p.mats, nullptr, p.status)) return;
   const R* u_in = static_cast<const R*>(p.u);
   R* pv = static_cast<R*>(p.p);
+  const R* pold = static_cast<const R*>(p.p_old);
   R beta = (R)0;
   if (MODE == GRAD_PCG && !p.first) {
     const int s = p.slot, sp = (s + 2) % 3;
@@ -198,7 +201,7 @@ __global__ void __launch_bounds__(256) ipdg_grad_kernel(const IpdgParams p) {
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const int k0 = tile * TE, ne = min(TE, p.K - k0);
     // A = u (or z), B = p_old
-    if (!t.load(k0, ne, u_in, MODE == GRAD_PCG ? pv : nullptr, nullptr, nullptr, p.geom, p.nbr, nullptr, p.status))
+    if (!t.load(k0, ne, u_in, MODE == GRAD_PCG ? pold : nullptr, nullptr, nullptr, p.geom, p.nbr, nullptr, p.status))
       return;
     R* sU = t.A();
     if (MODE == GRAD_PCG) {
@@ -222,7 +225,7 @@ __global__ void __launch_bounds__(256) ipdg_grad_kernel(const IpdgParams p) {
         R up;
         if (kn >= k0 && kn < k0 + ne) up = sU[(kn - k0) * NpP + nd2];
         else if (MODE == GRAD_PCG)
-          up = __ldg(u_in + (size_t)kn * NpP + nd2) + beta * pv[(size_t)kn * NpP + nd2];
+          up = __ldg(u_in + (size_t)kn * NpP + nd2) + beta * __ldg(pold + (size_t)kn * NpP + nd2);
         else up = __ldg(u_in + (size_t)kn * NpP + nd2);
         du = um - up;
       } else {

@@ -47,6 +47,22 @@ class Info(C.Structure):
                 ("rhs_blocks_per_sm", C.c_int), ("sm_count", C.c_int)]
 
 
+class SolveOpts(C.Structure):
+    _fields_ = [("mode", C.c_int), ("rtol", C.c_double), ("maxit", C.c_int), ("inner_rtol", C.c_double),
+                ("max_outer", C.c_int), ("use_graph", C.c_int)]
+
+
+class SolveStats(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("outer_iterations", C.c_int), ("inner_iterations", C.c_int),
+                ("converged", C.c_int), ("final_relres", C.c_double), ("seconds", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+SOLVE_FP64_PCG, SOLVE_MIXED_IR = 0, 1
+ERR_NOT_CONVERGED = -6
+
 _lock = threading.Lock()
 _lib = None
 _vp = C.c_void_p
@@ -82,6 +98,11 @@ def lib():
             L.dgc_check_device_status.argtypes = [_vp, C.POINTER(C.c_int)]
             L.dgc_launch_count.restype = C.c_int64
             L.dgc_launch_count.argtypes = [_vp]
+            L.dgc_laplace_apply.argtypes = [_vp, _vp, _vp, _vp]
+            L.dgc_laplace_spd_apply.argtypes = [_vp, _vp, _vp, _vp]
+            L.dgc_mass_apply.argtypes = [_vp, _vp, _vp, _vp]
+            L.dgc_pcg_solve.argtypes = [_vp, _vp, _vp, C.POINTER(SolveOpts), C.POINTER(SolveStats), _vp]
+            L.dgc_block_jacobi.argtypes = [_vp, _vp, _vp]
             L.dgc_ref_nodes.argtypes = [C.c_int, _dp, _dp]
             L.dgc_ref_operator.argtypes = [C.c_int, C.c_int, _dp]
             L.dgc_host_mesh.argtypes = [C.c_int, _dp, C.c_int, _ip, C.c_int, _dp, _ip, C.POINTER(C.c_int)]
@@ -250,3 +271,38 @@ class Discretization:
         _check(lib().dgc_lserk4_run(self._h, _ptr(qa), _ptr(qb), _ptr(res), t0, dt, nsteps, int(graph),
                                     C.byref(fin), _stream(stream)))
         return qa if fin.value == _ptr(qa) else qb
+
+    # ---------------------------------------------------------------- laplace_2d
+    def laplace(self, u, out=None, stream=None):
+        out = self.empty_state() if out is None else out
+        _check(lib().dgc_laplace_apply(self._h, _ptr(u), _ptr(out), _stream(stream)))
+        return out
+
+    def spd(self, u, out=None, stream=None):
+        out = self.empty_state() if out is None else out
+        _check(lib().dgc_laplace_spd_apply(self._h, _ptr(u), _ptr(out), _stream(stream)))
+        return out
+
+    def mass(self, f, out=None, stream=None):
+        import torch
+        out = torch.zeros(self.state_len, dtype=torch.float64, device="cuda") if out is None else out
+        _check(lib().dgc_mass_apply(self._h, _ptr(f), _ptr(out), _stream(stream)))
+        return out
+
+    def block_jacobi(self, stream=None):
+        import torch
+        out = torch.zeros(self.K * self.Np * self.Np, dtype=torch.float64, device="cuda")
+        _check(lib().dgc_block_jacobi(self._h, _ptr(out), _stream(stream)))
+        return out.view(self.K, self.Np, self.Np)
+
+    def pcg(self, b, x=None, mode: int = SOLVE_FP64_PCG, rtol: float = 1e-10, maxit: int = 20000,
+            inner_rtol: float = 1e-4, max_outer: int = 20, graph: bool = True, stream=None, check: bool = True):
+        """Solve S x = b (FP64 device vectors, native layout).  Returns (x, stats dict)."""
+        import torch
+        x = torch.zeros(self.state_len, dtype=torch.float64, device="cuda") if x is None else x
+        opts = SolveOpts(mode, rtol, maxit, inner_rtol, max_outer, int(graph))
+        st = SolveStats()
+        rc = lib().dgc_pcg_solve(self._h, _ptr(b), _ptr(x), C.byref(opts), C.byref(st), _stream(stream))
+        if rc != 0 and not (rc == ERR_NOT_CONVERGED and not check):
+            _check(rc)
+        return x, st.as_dict()

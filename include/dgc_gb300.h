@@ -162,6 +162,58 @@ int dgc_lserk4_stage(dgc_handle h, int stage, const void* q_in, void* q_out, voi
 int dgc_lserk4_run(dgc_handle h, void* qa, void* qb, void* res, double t0, double dt, int nsteps,
                    int use_graph, void** final_state, void* stream);
 
+/* ---- laplace_2d (DGC_LAPLACE handles; scalar field, native layout) -------- */
+
+/* out = A u, the discrete Laplacian with homogeneous boundary data (all faces
+ * Dirichlet or all Neumann per desc->dirichlet).  Replaces
+ * laplace_2d::operator() / apply_homogeneous (src/laplace_2d.h:121-251) and the
+ * two-phase device operator launched through kernel_adapter::execute_phase
+ * (src/kernel_adapter.cuh:77-82, examples/poisson_2d/d_poisson_2d.cuh:55-172).
+ * u and out in the handle's precision. */
+int dgc_laplace_apply(dgc_handle h, const void* u, void* out, void* stream);
+
+/* out = S u = -blockdiag(J_k M) A u: the mass-weighted form, symmetric
+ * positive definite for Dirichlet problems. */
+int dgc_laplace_spd_apply(dgc_handle h, const void* u, void* out, void* stream);
+
+/* out = blockdiag(J_k M) f (FP64): turns nodal values of f into the right-hand
+ * side of S u = M_J f for -laplace(u) = f. */
+int dgc_mass_apply(dgc_handle h, const double* f, double* out, void* stream);
+
+typedef enum dgc_solve_mode {
+  DGC_SOLVE_FP64_PCG = 0, /* block-Jacobi PCG in FP64 */
+  DGC_SOLVE_MIXED_IR = 1  /* FP32 block-Jacobi PCG inside FP64 iterative refinement */
+} dgc_solve_mode;
+
+typedef struct dgc_solve_opts {
+  int mode;           /* dgc_solve_mode */
+  double rtol;        /* stop at ||b - S x||_2 <= rtol ||b||_2 (true FP64 residual) */
+  int maxit;          /* total CG iteration budget */
+  double inner_rtol;  /* mixed: relative tolerance of each FP32 inner solve (default 1e-4) */
+  int max_outer;      /* mixed: refinement steps */
+  int use_graph;      /* replay 3-iteration chunks from a CUDA graph */
+} dgc_solve_opts;
+
+typedef struct dgc_solve_stats {
+  int iterations;       /* CG iterations (FP64 or FP32 inner, summed) */
+  int outer_iterations; /* refinement steps (mixed) */
+  int inner_iterations;
+  int converged;
+  double final_relres;  /* ||b - S x|| / ||b||, computed in FP64 */
+  double seconds;       /* host wall time of the call (synchronises the stream) */
+} dgc_solve_stats;
+
+/* Solve S x = b with block-Jacobi preconditioned CG (b, x FP64 device
+ * vectors, native layout; x holds the initial guess).  No reference
+ * counterpart: the reference assembles the matrix column by column and calls
+ * cuSOLVER-Sp QR (examples/poisson_2d/main.cpp:130-223).  Returns
+ * DGC_ERR_NOT_CONVERGED (with stats filled) if the tolerance is not met. */
+int dgc_pcg_solve(dgc_handle h, const double* b, double* x, const dgc_solve_opts* opts, dgc_solve_stats* stats,
+                  void* stream);
+
+/* The block-Jacobi inverse blocks S_kk^-1 (FP64, K x Np x Np, device). */
+int dgc_block_jacobi(dgc_handle h, double* blocks, void* stream);
+
 /* Synchronise the handle's device status word: DGC_OK, or DGC_ERR_DEVICE if a
  * kernel recorded an error since the last call (the word is then cleared). */
 int dgc_check_device_status(dgc_handle h, int* code);

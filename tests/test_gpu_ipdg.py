@@ -1,0 +1,137 @@
+"""GPU parity of the matrix-free laplace_2d (IPDG) operator and the
+block-Jacobi PCG solvers, through the C ABI.
+
+FP64 applies: the reference's own laplace_2d outputs (tests/golden/, tau = 1,
+homogeneous Dirichlet) and the oracle (scaled tau, Neumann) at 1e-12 relative.
+FP32 applies: the oracle at 2e-5.  Solvers: both methods reach the requested
+true FP64 residual and agree with the oracle's FP64 PCG solution.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, oracle
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+import dgc_gb300 as dg  # noqa: E402
+from dgc_gb300 import meshes  # noqa: E402
+
+
+def relerr(a, b):
+    a, b = np.ravel(a), np.ravel(b)
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    from dgc_gb300 import build
+    build.build()
+
+
+def golden_mesh(d):
+    return meshes.Mesh(xy=d["mesh_xy"].reshape(-1, 2), cells=d["mesh_cells"].reshape(-1, 3))
+
+
+@pytest.mark.parametrize("case", [f"{m}_N{n}" for m in ("jit4", "coarse") for n in range(1, 7)] +
+                         ["cells4_N1", "cells4_N2", "cells4_N3"])
+def test_laplace_matches_reference(case):
+    d = np.load(os.path.join(GOLDEN, f"ref_{case}.npz"))
+    N = int(case.split("_N")[1])
+    D = dg.Discretization(golden_mesh(d), "laplace", N, dg.F64, tau=dg.TAU_ONE, dirichlet=True)
+    out = D.download(D.laplace(D.upload(d["lap_u"])))
+    assert relerr(out, d["lap_out"]) < 1e-12
+
+
+@pytest.mark.parametrize("N", range(1, 9))
+@pytest.mark.parametrize("dirichlet", (True, False))
+def test_laplace_scaled_tau_matches_oracle(N, dirichlet):
+    m = meshes.jittered_square(5, 40 + N)
+    o = oracle.Oracle(m.xy, m.cells, N)
+    rng = np.random.default_rng(N)
+    u = rng.standard_normal(o.K * o.Np)
+    D = dg.Discretization(m, "laplace", N, dg.F64, tau=dg.TAU_SCALED, dirichlet=dirichlet)
+    assert relerr(D.download(D.laplace(D.upload(u))), o.laplace(u, dirichlet, 1)) < 1e-12
+    D32 = dg.Discretization(m, "laplace", N, dg.F32, tau=dg.TAU_SCALED, dirichlet=dirichlet)
+    assert relerr(D32.download(D32.laplace(D32.upload(u))), o.laplace(u, dirichlet, 1)) < 2e-5
+
+
+@pytest.mark.parametrize("N", (1, 2, 4, 6))
+def test_spd_form_and_block_jacobi(N):
+    m = meshes.jittered_square(4, 7 + N)
+    o = oracle.Oracle(m.xy, m.cells, N)
+    D = dg.Discretization(m, "laplace", N, dg.F64, tau=dg.TAU_SCALED)
+    u = np.random.default_rng(3).standard_normal(o.K * o.Np)
+    assert relerr(D.download(D.spd(D.upload(u))), o.spd(u, 1)) < 1e-12
+    binv = D.block_jacobi().cpu().numpy()
+    blocks = o.spd_blocks(1)
+    ref = np.linalg.inv(blocks)
+    assert relerr(binv, ref) < 1e-10
+    # symmetric positive definite blocks
+    assert np.allclose(blocks, blocks.transpose(0, 2, 1), atol=1e-10 * np.abs(blocks).max())
+    assert (np.linalg.eigvalsh(0.5 * (blocks + blocks.transpose(0, 2, 1))) > 0).all()
+
+
+def poisson_rhs(D, x, y):
+    """b = M_J f for -laplace(u) = f, u = sin(pi x) sin(pi y)."""
+    f = 2 * np.pi ** 2 * np.sin(np.pi * x) * np.sin(np.pi * y)
+    fn = D.upload(f.reshape(-1))
+    return D.mass(fn), np.sin(np.pi * x) * np.sin(np.pi * y)
+
+
+@pytest.mark.parametrize("N", (2, 4))
+def test_pcg_fp64_and_mixed_match_oracle(N):
+    m = meshes.jittered_square(8, 100 + N)
+    o = oracle.Oracle(m.xy, m.cells, N)
+    D = dg.Discretization(m, "laplace", N, dg.F64, tau=dg.TAU_SCALED)
+    x, y = D.node_xy()
+    b, uex = poisson_rhs(D, x, y)
+    b_ref = o.mass(2 * np.pi ** 2 * np.sin(np.pi * x) * np.sin(np.pi * y))
+    assert relerr(D.download(b), b_ref) < 1e-13
+    x64, st64 = D.pcg(b, mode=dg.SOLVE_FP64_PCG, rtol=1e-10)
+    xmx, stmx = D.pcg(b, mode=dg.SOLVE_MIXED_IR, rtol=1e-10, inner_rtol=1e-4)
+    assert st64["converged"] and st64["final_relres"] <= 1e-10
+    assert stmx["converged"] and stmx["final_relres"] <= 1e-10 and stmx["outer_iterations"] >= 2
+    xo, it, rel = o.pcg(b_ref, rtol=1e-12, tau_mode=1)
+    assert it > 0 and rel <= 1e-12
+    u64, umx = D.download(x64), D.download(xmx)
+    assert relerr(u64, xo) < 1e-8
+    assert relerr(umx, xo) < 1e-8
+    # the discrete solution approximates sin(pi x) sin(pi y)
+    assert relerr(u64, uex) < (0.02 if N == 2 else 2e-4)
+
+
+def test_pcg_graph_and_plain_agree():
+    m = meshes.jittered_square(10, 3)
+    D = dg.Discretization(m, "laplace", 3, dg.F64, tau=dg.TAU_SCALED)
+    x, y = D.node_xy()
+    b, _ = poisson_rhs(D, x, y)
+    xa, sa = D.pcg(b, rtol=1e-9, graph=True)
+    xb, sb = D.pcg(b, rtol=1e-9, graph=False)
+    # dot products are reduced with atomics, so runs agree to rounding only
+    assert abs(sa["iterations"] - sb["iterations"]) <= 1
+    assert relerr(xa.cpu().numpy(), xb.cpu().numpy()) < 1e-8
+
+
+def test_pcg_reports_non_convergence():
+    m = meshes.jittered_square(10, 3)
+    D = dg.Discretization(m, "laplace", 3, dg.F64)
+    x, y = D.node_xy()
+    b, _ = poisson_rhs(D, x, y)
+    _, st = D.pcg(b, rtol=1e-12, maxit=5, check=False)
+    assert not st["converged"] and st["iterations"] <= 5
+    with pytest.raises(dg.DgcError, match="tolerance"):
+        D.pcg(b, rtol=1e-12, maxit=5)
+
+
+def test_laplace_handle_rejects_time_stepping():
+    m = meshes.jittered_square(3, 3)
+    D = dg.Discretization(m, "laplace", 2, dg.F64)
+    q = D.empty_state()
+    with pytest.raises(dg.DgcError, match="laplace"):
+        D.rhs(q, 0.0)
+    A = dg.Discretization(m, "advection", 2, dg.F64)
+    with pytest.raises(dg.DgcError, match="LAPLACE"):
+        A.laplace(A.empty_state())
