@@ -299,6 +299,7 @@ def main():
 
     m = meshes.jittered_square(NSIDE, SEED)
     D32 = dg.Discretization(m, "maxwell_te", ORDER, dg.F32)
+    tuned, tune_ms = D32.autotune(reps=10)
     K, Np = D32.K, D32.Np
     x, y = D32.node_xy()
     q_init = te_initial(x, y)
@@ -361,7 +362,10 @@ def main():
                 "frac": achieved / peak, "traffic": read_traffic(), "peak_source": peak_kind,
                 "kernel": "dgk::dg_rhs_kernel<float,6,PHYS_TE> (LSERK4 stage)",
                 "alg_bytes_per_launch": alg_bytes, "alg_bytes_per_element": alg_bytes_elem,
-                "launch_ms": launch_ms, "stage_ms": [float(v) for v in stage_ms.mean(axis=0)]}
+                "launch_ms": launch_ms, "stage_ms": [float(v) for v in stage_ms.mean(axis=0)],
+                "tile": {"variant": tuned, "elements_per_tile": D32.info.rhs_tile,
+                         "threads": D32.info.rhs_threads, "smem_bytes": D32.info.rhs_smem,
+                         "ctas_per_sm": D32.info.rhs_blocks_per_sm, "autotune_ms": tune_ms}}
 
     e2e = None if args.no_e2e else measure_e2e(D32, bufs, res, flush, stream, t, dt, args.steps, ws, dofs, barrier)
     D64, fp64 = (None, None) if args.no_fp64 else measure_fp64(dg, m, q_init, dt, flush, stream,

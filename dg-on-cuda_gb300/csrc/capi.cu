@@ -1,7 +1,9 @@
 // capi.cu -- C ABI of the GB300 nodal-DG hot path (declared in include/dgc_gb300.h).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdarg>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -188,8 +190,10 @@ int device_init(dgc_handle_s* h) {
   if (h->desc.physics != DGC_LAPLACE) {
     dgk::LaunchInfo li;
     cudaError_t e = h->prec == DGC_F64
-                        ? dgk::rhs_dispatch<double>(h->N, h->desc.physics, dgk::RhsParams{}, h->sm_count, 0, &li)
-                        : dgk::rhs_dispatch<float>(h->N, h->desc.physics, dgk::RhsParams{}, h->sm_count, 0, &li);
+                        ? dgk::rhs_dispatch<double>(h->N, h->desc.physics, h->rhs_variant, dgk::RhsParams{},
+                                                    h->sm_count, 0, &li)
+                        : dgk::rhs_dispatch<float>(h->N, h->desc.physics, h->rhs_variant, dgk::RhsParams{},
+                                                   h->sm_count, 0, &li);
     if (e != cudaSuccess) return cuda_fail(e, "configure rhs kernel");
     h->rhs_info = li;
   }
@@ -350,8 +354,10 @@ dgk::RhsParams base_params(dgc_handle h) {
 }
 
 int launch(dgc_handle h, const dgk::RhsParams& p, cudaStream_t s) {
-  cudaError_t e = h->prec == DGC_F64 ? dgk::rhs_dispatch<double>(h->N, h->desc.physics, p, h->sm_count, s, nullptr)
-                                     : dgk::rhs_dispatch<float>(h->N, h->desc.physics, p, h->sm_count, s, nullptr);
+  cudaError_t e =
+      h->prec == DGC_F64
+          ? dgk::rhs_dispatch<double>(h->N, h->desc.physics, h->rhs_variant, p, h->sm_count, s, nullptr)
+          : dgk::rhs_dispatch<float>(h->N, h->desc.physics, h->rhs_variant, p, h->sm_count, s, nullptr);
   if (e != cudaSuccess) return cuda_fail(e, "rhs kernel launch");
   ++h->launches;
   return DGC_OK;
@@ -586,4 +592,134 @@ extern "C" int dgc_host_mesh(int nv, const double* vxy, int K, const int32_t* ce
   if (nbr) std::memcpy(nbr, m.nbr.data(), m.nbr.size() * sizeof(int32_t));
   if (num_bfaces) *num_bfaces = m.num_bfaces;
   return DGC_OK;
+}
+
+// ---------------------------------------------------------------- autotuning
+namespace {
+
+int refresh_rhs_info(dgc_handle h) {
+  dgk::LaunchInfo li;
+  cudaError_t e = h->prec == DGC_F64 ? dgk::rhs_dispatch<double>(h->N, h->desc.physics, h->rhs_variant,
+                                                                 dgk::RhsParams{}, h->sm_count, 0, &li)
+                                     : dgk::rhs_dispatch<float>(h->N, h->desc.physics, h->rhs_variant,
+                                                                dgk::RhsParams{}, h->sm_count, 0, &li);
+  if (e != cudaSuccess) return cuda_fail(e, "configure rhs kernel");
+  h->rhs_info = li;
+  return DGC_OK;
+}
+
+std::string tune_key(dgc_handle h) {
+  cudaDeviceProp prop{};
+  cudaGetDeviceProperties(&prop, h->device);
+  int kb = 0;
+  while ((1 << (kb + 1)) <= h->K) ++kb;  // K bucket: floor(log2 K)
+  char buf[256];
+  std::snprintf(buf, sizeof buf, "%s|sm%d|phys%d|prec%d|N%d|K2^%d", prop.name, prop.multiProcessorCount,
+                h->desc.physics, h->prec, h->N, kb);
+  for (char* c = buf; *c; ++c)
+    if (*c == ' ') *c = '_';
+  return buf;
+}
+
+int cache_lookup(const std::string& key) {
+  const char* path = std::getenv("DGC_TUNE_CACHE");
+  if (!path || !*path) return -1;
+  FILE* f = std::fopen(path, "r");
+  if (!f) return -1;
+  char k[300];
+  int v, found = -1;
+  while (std::fscanf(f, "%299s %d", k, &v) == 2)
+    if (key == k) found = v;  // last entry wins
+  std::fclose(f);
+  return found;
+}
+
+void cache_store(const std::string& key, int v) {
+  const char* path = std::getenv("DGC_TUNE_CACHE");
+  if (!path || !*path) return;
+  FILE* f = std::fopen(path, "a");
+  if (!f) return;
+  std::fprintf(f, "%s %d\n", key.c_str(), v);
+  std::fclose(f);
+}
+
+}  // namespace
+
+extern "C" int dgc_num_variants(dgc_handle h) {
+  if (!h) return fail(DGC_ERR_ARG, "null handle");
+  if (h->desc.physics == DGC_LAPLACE) return 1;
+  return dgk::rhs_num_variants(h->prec == DGC_F32, h->N);
+}
+
+extern "C" int dgc_set_variant(dgc_handle h, int v) {
+  if (!h) return fail(DGC_ERR_ARG, "null handle");
+  const int nv = dgc_num_variants(h);
+  if (v < 0 || v >= nv) return fail(DGC_ERR_ARG, "variant %d outside [0, %d)", v, nv);
+  h->rhs_variant = v;
+  return h->desc.physics == DGC_LAPLACE ? DGC_OK : refresh_rhs_info(h);
+}
+
+extern "C" int dgc_autotune(dgc_handle h, int reps, double* times_ms, int* chosen, void* stream) {
+  if (!h) return fail(DGC_ERR_ARG, "null handle");
+  if (int rc = check_time_dependent(h)) return rc;
+  const int nv = dgc_num_variants(h);
+  const std::string key = tune_key(h);
+  if (!times_ms) {
+    const int v = cache_lookup(key);
+    if (v >= 0 && v < nv) {
+      if (chosen) *chosen = v;
+      return dgc_set_variant(h, v);
+    }
+  }
+  if (reps <= 0) reps = 10;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const size_t bytes = (size_t)h->K * h->Nf * h->NpP * (h->prec == DGC_F64 ? 8 : 4);
+  void *qa = nullptr, *qb = nullptr, *res = nullptr;
+  CK(cudaMalloc(&qa, bytes));
+  CK(cudaMalloc(&qb, bytes));
+  CK(cudaMalloc(&res, bytes));
+  CK(cudaMemsetAsync(qa, 0, bytes, s));
+  CK(cudaMemsetAsync(qb, 0, bytes, s));
+  CK(cudaMemsetAsync(res, 0, bytes, s));
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  const int keep = h->rhs_variant;
+  const int64_t l0 = h->launches;
+  int best = 0;
+  double best_ms = 1e300;
+  int rc = DGC_OK;
+  for (int v = 0; v < nv && rc == DGC_OK; ++v) {
+    h->rhs_variant = v;
+    std::vector<float> ms;
+    for (int r = 0; r < reps + 2 && rc == DGC_OK; ++r) {
+      cudaEventRecord(e0, s);
+      rc = dgc_lserk4_stage(h, r % 5, (r & 1) ? qb : qa, (r & 1) ? qa : qb, res, 0.0, 1e-6, s);
+      cudaEventRecord(e1, s);
+      cudaEventSynchronize(e1);
+      float t = 0.0f;
+      cudaEventElapsedTime(&t, e0, e1);
+      if (r >= 2) ms.push_back(t);
+    }
+    std::sort(ms.begin(), ms.end());
+    const double med = ms.empty() ? 1e300 : ms[ms.size() / 2];
+    if (times_ms) times_ms[v] = med;
+    if (med < best_ms) {
+      best_ms = med;
+      best = v;
+    }
+  }
+  h->launches = l0;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(qa);
+  cudaFree(qb);
+  cudaFree(res);
+  if (rc != DGC_OK) {
+    h->rhs_variant = keep;
+    return rc;
+  }
+  cache_store(key, best);
+  if (chosen) *chosen = best;
+  return dgc_set_variant(h, best);
 }

@@ -30,6 +30,7 @@ struct dgc_handle_s {
   int* d_status = nullptr;    // device-side error word
   double* d_time = nullptr;   // simulation time for graph-replayed steps
   dgk::LaunchInfo rhs_info;
+  int rhs_variant = 0;        // tile-shape variant of the fused RHS kernel (dgc_autotune)
   int64_t launches = 0;       // kernels launched through this handle
   // cached CUDA graph of LSERK4 steps
   cudaGraphExec_t graph_exec = nullptr;

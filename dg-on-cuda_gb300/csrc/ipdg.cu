@@ -496,43 +496,41 @@ extern "C" int dgc_pcg_solve(dgc_handle h, const double* b, double* x, const dgc
   // r = b - S x (x is the caller's initial guess)
   if (int rc = true_residual<double>(h, b, x, r64, &rr, s)) return rc;
   const bool graph = opts->use_graph != 0;
-  if (opts->mode == DGC_SOLVE_FP64_PCG) {
-    if (rr > tol2) {
-      // solve S d = r in FP64, then x += d
+  if (opts->mode != DGC_SOLVE_FP64_PCG && opts->mode != DGC_SOLVE_MIXED_IR)
+    return set_error(DGC_ERR_ARG, "unknown solve mode");
+  // Refinement loop on the true FP64 residual.  FP64 mode: each pass solves
+  // S d = r in FP64 to a little below the remaining target (a second pass
+  // mops up the drift between CG's recursive and true residuals).  Mixed
+  // mode: each pass solves the normalised residual system in FP32 to
+  // inner_rtol and adds the correction in FP64.
+  const bool fp64 = opts->mode == DGC_SOLVE_FP64_PCG;
+  const double inner = opts->inner_rtol > 0.0 ? opts->inner_rtol : 1e-4;
+  const int max_outer = opts->max_outer > 0 ? opts->max_outer : (fp64 ? 4 : 20);
+  int outer = 0;
+  while (rr > tol2 && outer < max_outer) {
+    const int budget = opts->maxit - S.inner_iterations;
+    if (budget <= 0) break;
+    const double nr = std::sqrt(rr);
+    int it = 0, conv = 0;
+    if (fp64) {
       CKI(cudaMemcpyAsync(st->w64[W_R], r64, n * 8, cudaMemcpyDeviceToDevice, s));
-      int it = 0, conv = 0;
-      // aim a little below the target: CG tracks the recursive residual
-      const double rel = 0.5 * std::sqrt(tol2 / rr);
-      if (int rc = pcg_core<double>(h, rel, opts->maxit, graph, &it, &conv, s)) return rc;
-      S.inner_iterations = it;
-      S.iterations = it;
-      S.outer_iterations = 1;
+      const double rel = std::max(0.5 * std::sqrt(tol2 / rr), 1e-15);
+      if (int rc = pcg_core<double>(h, rel, budget, graph, &it, &conv, s)) return rc;
       dgk::k_add<<<grid_for(h, n), 256, 0, s>>>(n, x, st->w64[W_X]);
-      CKI(cudaGetLastError());
-      if (int rc = true_residual<double>(h, b, x, r64, &rr, s)) return rc;
-    }
-  } else if (opts->mode == DGC_SOLVE_MIXED_IR) {
-    const double inner = opts->inner_rtol > 0.0 ? opts->inner_rtol : 1e-4;
-    int outer = 0;
-    while (rr > tol2 && outer < opts->max_outer) {
-      const double nr = std::sqrt(rr);
+    } else {
       dgk::k_r64_to_r32<<<grid_for(h, n), 256, 0, s>>>(n, r64, 1.0 / nr, st->w32[W_R]);
       CKI(cudaGetLastError());
-      int it = 0, conv = 0;
-      const int budget = opts->maxit - S.inner_iterations;
-      if (budget <= 0) break;
       if (int rc = pcg_core<float>(h, inner, budget, graph, &it, &conv, s)) return rc;
-      S.inner_iterations += it;
       dgk::k_x_update<<<grid_for(h, n), 256, 0, s>>>(n, x, st->w32[W_X], nr);
-      CKI(cudaGetLastError());
-      ++outer;
-      if (int rc = true_residual<double>(h, b, x, r64, &rr, s)) return rc;
     }
-    S.outer_iterations = outer;
-    S.iterations = S.inner_iterations;
-  } else {
-    return set_error(DGC_ERR_ARG, "unknown solve mode");
+    CKI(cudaGetLastError());
+    h->launches += 2;
+    S.inner_iterations += it;
+    ++outer;
+    if (int rc = true_residual<double>(h, b, x, r64, &rr, s)) return rc;
   }
+  S.outer_iterations = outer;
+  S.iterations = S.inner_iterations;
   CKI(cudaStreamSynchronize(s));
   S.final_relres = bb > 0.0 ? std::sqrt(rr / bb) : 0.0;
   S.converged = rr <= tol2 ? 1 : 0;

@@ -23,7 +23,8 @@ static cudaError_t by_phys(int P, const RhsParams& p, int sm, cudaStream_t s, La
 }
 
 template <>
-cudaError_t rhs_dispatch<double>(int N, int P, const RhsParams& p, int sm, cudaStream_t s, LaunchInfo* info) {
+cudaError_t rhs_dispatch<double>(int N, int P, int v, const RhsParams& p, int sm, cudaStream_t s, LaunchInfo* info) {
+  (void)v;
   switch (N) {
     case 1: return by_phys<1>(P, p, sm, s, info);
     case 2: return by_phys<2>(P, p, sm, s, info);

@@ -48,6 +48,59 @@ cudaError_t rhs_launch(const RhsParams& p, int sm_count, cudaStream_t s) {
 
 // dispatch over order (1..8) and physics; defined in rhs_f64.cu / rhs_f32.cu
 template <typename R>
-cudaError_t rhs_dispatch(int N, int P, const RhsParams& p, int sm_count, cudaStream_t s, LaunchInfo* info);
+cudaError_t rhs_dispatch(int N, int P, int variant, const RhsParams& p, int sm_count, cudaStream_t s,
+                         LaunchInfo* info);
+// number of tile-shape variants compiled for (precision, order)
+int rhs_num_variants(int prec_f32, int N);
+
+}  // namespace dgk
+
+#include "dg_rhs_v2.cuh"
+
+namespace dgk {
+
+template <int N, int P, int G, int EPT>
+cudaError_t rhs_v2_shape(const RhsParams* p, int sm_count, cudaStream_t s, LaunchInfo* info) {
+  using C = V2Config<N, P, G, EPT>;
+  static std::once_flag once;
+  static cudaError_t st = cudaSuccess;
+  static int bps = 0;
+  std::call_once(once, [] {
+    st = cudaFuncSetAttribute(dg_rhs_v2_kernel<N, P, G, EPT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              C::kSmem);
+    if (st == cudaSuccess)
+      st = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, dg_rhs_v2_kernel<N, P, G, EPT>, C::kThreads,
+                                                         C::kSmem);
+  });
+  if (st != cudaSuccess) return st;
+  if (info) {
+    info->threads = C::kThreads;
+    info->tile = C::TE;
+    info->smem = C::kSmem;
+    info->blocks_per_sm = bps;
+    return cudaSuccess;
+  }
+  const int ntiles = (p->K + C::TE - 1) / C::TE;
+  int grid = sm_count * (bps > 0 ? bps : 1);
+  if (grid > ntiles) grid = ntiles;
+  dg_rhs_v2_kernel<N, P, G, EPT><<<grid, C::kThreads, C::kSmem, s>>>(*p);
+  return cudaGetLastError();
+}
+
+// launch (p != nullptr) or describe (info != nullptr) tile-shape variant v
+template <int N, int P>
+cudaError_t rhs_v2(int v, const RhsParams* p, int sm, cudaStream_t s, LaunchInfo* info) {
+  using S = V2Shapes<N>;
+  switch (v) {
+    case 0: return rhs_v2_shape<N, P, S::G[0], S::EPT[0]>(p, sm, s, info);
+    case 1: return rhs_v2_shape<N, P, S::G[1], S::EPT[1]>(p, sm, s, info);
+    case 2: return rhs_v2_shape<N, P, S::G[2], S::EPT[2]>(p, sm, s, info);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+// per-order entry points, defined in rhs_f32_n<N>.cu
+template <int N>
+cudaError_t rhs_v2_order(int P, int v, const RhsParams* p, int sm, cudaStream_t s, LaunchInfo* info);
 
 }  // namespace dgk

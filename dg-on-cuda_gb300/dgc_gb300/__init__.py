@@ -103,6 +103,9 @@ def lib():
             L.dgc_mass_apply.argtypes = [_vp, _vp, _vp, _vp]
             L.dgc_pcg_solve.argtypes = [_vp, _vp, _vp, C.POINTER(SolveOpts), C.POINTER(SolveStats), _vp]
             L.dgc_block_jacobi.argtypes = [_vp, _vp, _vp]
+            L.dgc_num_variants.argtypes = [_vp]
+            L.dgc_set_variant.argtypes = [_vp, C.c_int]
+            L.dgc_autotune.argtypes = [_vp, C.c_int, C.c_void_p, C.POINTER(C.c_int), _vp]
             L.dgc_ref_nodes.argtypes = [C.c_int, _dp, _dp]
             L.dgc_ref_operator.argtypes = [C.c_int, C.c_int, _dp]
             L.dgc_host_mesh.argtypes = [C.c_int, _dp, C.c_int, _ip, C.c_int, _dp, _ip, C.POINTER(C.c_int)]
@@ -209,6 +212,30 @@ class Discretization:
 
     def launch_count(self) -> int:
         return int(lib().dgc_launch_count(self._h))
+
+    def num_variants(self) -> int:
+        n = lib().dgc_num_variants(self._h)
+        if n < 0:
+            _check(n)
+        return n
+
+    def set_variant(self, v: int) -> None:
+        _check(lib().dgc_set_variant(self._h, v))
+        info = Info()
+        _check(lib().dgc_get_info(self._h, C.byref(info)))
+        self.info = info
+
+    def autotune(self, reps: int = 10, measure: bool = True, stream=None):
+        """Time the tile-shape variants and keep the fastest; returns (chosen, times_ms or None)."""
+        n = self.num_variants()
+        times = (C.c_double * n)() if measure else None
+        chosen = C.c_int(-1)
+        _check(lib().dgc_autotune(self._h, reps, C.cast(times, C.c_void_p) if measure else None,
+                                  C.byref(chosen), _stream(stream)))
+        info = Info()
+        _check(lib().dgc_get_info(self._h, C.byref(info)))
+        self.info = info
+        return chosen.value, (list(times) if measure else None)
 
     def check(self) -> None:
         code = C.c_int(0)

@@ -222,6 +222,25 @@ int dgc_check_device_status(dgc_handle h, int* code);
  * each kernel they contain). */
 int64_t dgc_launch_count(dgc_handle h);
 
+/* ---- tile-shape autotuning of the fused RHS kernel (no reference
+ * counterpart: the reference takes grid and block sizes from argv,
+ * examples/advection_2d/main.cpp:71-79) --------------------------------- */
+
+/* Number of compiled tile-shape variants for this handle (>= 1). */
+int dgc_num_variants(dgc_handle h);
+
+/* Select variant v (0 <= v < dgc_num_variants). */
+int dgc_set_variant(dgc_handle h, int v);
+
+/* Time every variant with `reps` LSERK4-stage launches on this handle's mesh
+ * (scratch buffers are allocated and freed inside) and select the fastest.
+ * times_ms (optional, dgc_num_variants entries) receives the median time per
+ * launch.  When times_ms is NULL and the file named by the environment
+ * variable DGC_TUNE_CACHE holds a choice for this (GPU, physics, precision,
+ * order, log2 K) key, that choice is applied without timing; new choices are
+ * appended to that file.  Synchronises the stream. */
+int dgc_autotune(dgc_handle h, int reps, double* times_ms, int* chosen, void* stream);
+
 /* ---- host-only set-up queries (no GPU needed) ---------------------------- */
 
 /* Reference-element nodes of order N (alpha_optimized_nodes_triangle::
