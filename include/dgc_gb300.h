@@ -143,6 +143,18 @@ int dgc_axpy(dgc_handle h, double a, const void* x, const void* y, void* out, vo
  * src/explicit_runge_kutta.h:33-51).  work: 3 state vectors of scratch. */
 int dgc_rk4_step(dgc_handle h, void* q, double t, double dt, void* const* work, void* stream);
 
+/* dgc_rk4_step without caller work buffers, for callers that cannot allocate
+ * device memory (code running under global-mode stream capture, real-time
+ * loops that must not touch the allocator, plugins whose device memory is
+ * owned by the host application).  No counterpart in the reference.  The
+ * three work vectors live in a 6 MiB file-scope device array that every GPU
+ * loading the library holds until exit; the state vector may be at most
+ * 2 MiB (larger handles get DGC_ERR_ARG).  The first call on each device
+ * looks up the array's device address (cudaGetSymbolAddress) with that device
+ * current, so make it before any stream capture.  All calls share the array:
+ * calls whose GPU work overlaps race on it. */
+int dgc_rk4_step_static(dgc_handle h, void* q, double t, double dt, void* stream);
+
 /* One low-storage RK4 step (Carpenter-Kennedy, 5 stages, each one fused
  * launch).  Reads q_in, writes the new state to q_out; q_in is used as
  * scratch and its contents are destroyed; res is the LSERK residual register
