@@ -114,6 +114,29 @@ int upload_operators(dgc_handle_s* h, int form) {
   if (!h->d_mats32[form]) CK(cudaMalloc(&h->d_mats32[form], m32.size() * sizeof(float)));
   CK(cudaMemcpy(h->d_mats64[form], m64.data(), m64.size() * sizeof(double), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(h->d_mats32[form], m32.data(), m32.size() * sizeof(float), cudaMemcpyHostToDevice));
+  if (form == 0 && re.N <= 6) {
+    // tensor-core operand: row n = output node, K = [Dr(n,:) | Ds(n,:) | LIFT(n,:)],
+    // K-major core matrices (8 rows x 4 floats), hi / lo TF32 split
+    const int Np = re.Np, NF = 3 * re.Nfp;
+    const int KP = (2 * Np + NF + 7) / 8 * 8, NC = Np <= 16 ? 16 : 32, SBO4 = KP / 4 * 32;
+    std::vector<float> tc((size_t)2 * NC * KP, 0.0f);
+    for (int n = 0; n < Np; ++n)
+      for (int k = 0; k < 2 * Np + NF; ++k) {
+        const double x = k < Np ? Dr[(size_t)n * Np + k]
+                                : (k < 2 * Np ? Ds[(size_t)n * Np + k - Np] : L[(size_t)n * NF + k - 2 * Np]);
+        const float xf = (float)x;
+        uint32_t bits;
+        std::memcpy(&bits, &xf, 4);
+        bits &= 0xFFFFE000u;
+        float hi;
+        std::memcpy(&hi, &bits, 4);
+        const size_t o = (size_t)(n >> 3) * SBO4 + (k >> 2) * 32 + (n & 7) * 4 + (k & 3);
+        tc[o] = hi;
+        tc[(size_t)NC * KP + o] = xf - hi;
+      }
+    if (!h->d_tc_b) CK(cudaMalloc(&h->d_tc_b, tc.size() * sizeof(float)));
+    CK(cudaMemcpy(h->d_tc_b, tc.data(), tc.size() * sizeof(float), cudaMemcpyHostToDevice));
+  }
   return DGC_OK;
 }
 
@@ -212,6 +235,7 @@ void device_free(dgc_handle_s* h) {
     cudaFree(h->d_mats64[f]);
     cudaFree(h->d_mats32[f]);
   }
+  cudaFree(h->d_tc_b);
   ipdg_free(h);
 }
 
@@ -343,6 +367,7 @@ dgk::RhsParams base_params(dgc_handle h) {
   p.nbr = reinterpret_cast<const int4*>(h->d_nbr);
   p.bxy = h->d_bxy;
   p.mats = h->prec == DGC_F64 ? h->d_mats64[0] : h->d_mats32[0];
+  p.mats_tc = h->prec == DGC_F32 ? h->d_tc_b : nullptr;
   p.ax = h->desc.ax;
   p.ay = h->desc.ay;
   p.gx0 = h->desc.gx0;

@@ -45,6 +45,7 @@ struct RhsParams {
   const int4* nbr;    // [K]
   const double* bxy;  // boundary face nodes [nbf][Nfp][2]
   const void* mats;   // DrT | DsT | LT, each padded to 16 bytes
+  const void* mats_tc;// FP32 tensor-core operand [Dr | Ds | LIFT] (split TF32, core-matrix layout)
   double t, dt;       // time of the operator evaluation (offset when t_dev is set), step size
   const double* t_dev;// optional device-resident base time: operator time = *t_dev + t
   double ca, cb;      // LSERK: a_k, b_k | RK4: output coefficient, accumulator weight

@@ -1,0 +1,360 @@
+// dg_rhs_tc.cuh -- fused RHS + time-stage kernel with the element contractions
+// on the 5th-generation tensor cores (tcgen05, TMEM accumulators), FP32 via
+// split TF32 (3 products: hi*hi + hi*lo + lo*hi).
+//
+// Formulation.  Per-element geometric factors are constant on an element, so
+// they can scale the operator's inputs instead of its outputs:
+//   Dx q = Dr (rx q) + Ds (sx q),   Dy q = Dr (ry q) + Ds (sy q),
+// and the lifted surface term is LIFT (-faceJ/J f).  Every output field of an
+// element is therefore one product of the constant operator [Dr | Ds | LIFT]
+// (K = 2 Np + 3 Nfp, padded to 8) with a K-vector built from the element's
+// state, geometry and face fluxes:
+//   D^T (rows = element x field, cols = nodes) = A (rows x K) * B^T (K x nodes)
+// with A built in shared memory per tile and B = [Dr | Ds | LIFT] (one row per
+// output node) loaded once per CTA.  One tcgen05.mma kind::tf32 with M = 128,
+// N = 16 or 32, K = 8 per instruction; D lives in TMEM (32 columns).  Each of
+// the 128 threads then reads its own row (one element-field, all nodes) with
+// tcgen05.ld and applies the stage update with float4 global traffic.
+//
+// Operand layout: K-major, no swizzle ("canonical" core matrices of 8 rows x
+// 16 bytes): element (row, k) at byte (row/8)*SBO + (k/4)*128 + (row%8)*16 +
+// (k%4)*4 with LBO = 128, SBO = (K/4)*128.
+#pragma once
+
+#include "dg_rhs.cuh"
+
+namespace dgk {
+
+// ---------------------------------------------------------------- tcgen05 wrappers
+__device__ __forceinline__ void tmem_alloc32(uint32_t* dst) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 32;" ::"r"(smem_u32(dst)) : "memory");
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc32(uint32_t taddr) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 32;" ::"r"(taddr) : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tc_mma_tf32(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
+                                            uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(a_desc), "l"(b_desc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void tc_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+// 16 / 32 consecutive TMEM columns of the warp's 32 lanes (one row per thread)
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
+  tmem_ld16(taddr, v);
+  tmem_ld16(taddr + 16, v + 16);
+}
+
+// shared-memory matrix descriptor: K-major, no swizzle, descriptor version 1
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | ((uint64_t)1 << 46);
+}
+
+__device__ __forceinline__ float tf32_hi(float x) { return __uint_as_float(__float_as_uint(x) & 0xFFFFE000u); }
+
+template <int N, int P>
+struct TcConfig {
+  using O = Order<N>;
+  static constexpr int Np = O::Np, Nfp = O::Nfp, NpP = O::NpP, NFACE = O::Nface;
+  static constexpr int Nf = PhysTraits<P>::Nf;
+  static constexpr int kThreads = 128;
+  static constexpr int TE = 128 / Nf;                  // elements per tile (rows = TE * Nf <= 128)
+  static constexpr int ESTR = Nf * NpP;
+  static constexpr int KP = (2 * Np + NFACE + 7) / 8 * 8;  // contraction length
+  static constexpr int NC = Np <= 16 ? 16 : 32;        // MMA N (output nodes, padded)
+  static constexpr int SBO = (KP / 4) * 128;           // bytes between 8-row groups
+  static constexpr uint32_t kBBytes = NC * KP * 4;     // one split of B
+  static constexpr uint32_t kABytes = 128 * KP * 4;    // one split of A
+  static constexpr uint32_t kQ = TE * ESTR * 4, kG = TE * 16 * 8, kN = TE * 16;
+  static constexpr uint32_t kBuf = kQ + kG + kN;
+  static constexpr uint32_t oBar = 0;                  // 4 mbarriers + TMEM address
+  static constexpr uint32_t oB = 64;
+  static constexpr uint32_t oA = oB + 2 * kBBytes;
+  static constexpr uint32_t oBuf = oA + 2 * kABytes;
+  static constexpr uint32_t kSmem = oBuf + 2 * kBuf;
+  // instruction descriptor: D f32, A/B tf32, both K-major, N >> 3, M >> 4
+  static constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(NC >> 3) << 17) |
+                                     ((uint32_t)(128 >> 4) << 24);
+};
+
+template <int SBO>
+__device__ __forceinline__ uint32_t op_off(int row, int k) {  // float offset in an operand
+  return (uint32_t)((row >> 3) * (SBO / 4) + (k >> 2) * 32 + (row & 7) * 4 + (k & 3));
+}
+
+template <int N, int P>
+__global__ void __launch_bounds__(128) dg_rhs_tc_kernel(const RhsParams p) {
+  using C = TcConfig<N, P>;
+  constexpr int Np = C::Np, Nfp = C::Nfp, NpP = C::NpP, NFACE = C::NFACE, NF = C::Nf;
+  constexpr int TE = C::TE, ESTR = C::ESTR, KP = C::KP, NC = C::NC, SBO = C::SBO;
+
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + C::oBar);  // [0],[1] tiles, [2] operator, [3] MMA
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + C::oBar + 32);
+  float* Bhi = reinterpret_cast<float*>(smem + C::oB);
+  float* Ahi = reinterpret_cast<float*>(smem + C::oA);
+  float* Alo = Ahi + C::kABytes / 4;
+  auto bufQ = [&](int b) { return reinterpret_cast<float*>(smem + C::oBuf + b * C::kBuf); };
+  auto bufG = [&](int b) { return reinterpret_cast<double*>(smem + C::oBuf + b * C::kBuf + C::kQ); };
+  auto bufN = [&](int b) { return reinterpret_cast<int4*>(smem + C::oBuf + b * C::kBuf + C::kQ + C::kG); };
+
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int ntiles = (p.K + TE - 1) / TE;
+  const float* qin = static_cast<const float*>(p.q_in);
+  const double tnow = p.t_dev ? *p.t_dev + p.t : p.t;
+
+  if (tid == 0) {
+    for (int i = 0; i < 4; ++i) mbar_init(&bar[i], 1);
+    fence_barrier_init();
+  }
+  if (warp == 0) tmem_alloc32(tmem_slot);
+  // zero A (its padding columns and unused rows are never written again)
+  for (int x = tid; x < (int)(2 * C::kABytes / 4); x += 128) Ahi[x] = 0.0f;
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  auto issue = [&](int tile, int b) {
+    const int k0 = tile * TE, ne = min(TE, p.K - k0);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    const uint32_t bq = ne * ESTR * 4, bg = ne * 16 * 8, bn = ne * 16;
+    mbar_arrive_expect_tx(&bar[b], bq + bg + bn);
+    bulk_g2s(bufQ(b), qin + (size_t)k0 * ESTR, bq, &bar[b]);
+    bulk_g2s(bufG(b), p.geom + (size_t)k0 * 16, bg, &bar[b]);
+    bulk_g2s(bufN(b), p.nbr + k0, bn, &bar[b]);
+  };
+  if (tid == 0) {
+    mbar_arrive_expect_tx(&bar[2], 2 * C::kBBytes);
+    bulk_g2s(Bhi, p.mats, 2 * C::kBBytes, &bar[2]);
+    if ((int)blockIdx.x < ntiles) issue(blockIdx.x, 0);
+  }
+  bool ok = mbar_wait(&bar[2], 0, p.status);
+  ok = __syncthreads_and(ok);
+
+  const uint32_t aH = smem_u32(Ahi), aL = smem_u32(Alo), bH = smem_u32(Bhi), bL = bH + C::kBBytes;
+  uint32_t ph[2] = {0, 0}, phm = 0;
+  int it = 0;
+  for (int tile = blockIdx.x; ok && tile < ntiles; tile += gridDim.x, ++it) {
+    const int b = it & 1;
+    const int k0 = tile * TE, ne = min(TE, p.K - k0);
+    const int nxt = tile + gridDim.x;
+    if (tid == 0 && nxt < ntiles) issue(nxt, b ^ 1);
+    ok = __syncthreads_and(mbar_wait(&bar[b], ph[b], p.status));
+    if (!ok) break;
+    ph[b] ^= 1;
+    const float* sQ = bufQ(b);
+    const double* sG = bufG(b);
+    const int4* sN = bufN(b);
+
+    // ---- face fluxes -> lifted columns of A: gamma = -(faceJ / J) * flux
+    for (int x = tid; x < ne * NFACE; x += 128) {
+      const int e = x / NFACE, fm = x - e * NFACE, f = fm / Nfp, d = fm - f * Nfp;
+      const double* g = sG + e * 16;
+      const int nb = f == 0 ? sN[e].x : (f == 1 ? sN[e].y : sN[e].z);
+      const int nd = fmask<N>(f, d);
+      float a[NF], bb[NF];
+#pragma unroll
+      for (int c = 0; c < NF; ++c) a[c] = sQ[e * ESTR + c * NpP + nd];
+      if (nb >= 0) {
+        const int kn = nb >> 2, nd2 = fmask<N>(nb & 3, Nfp - 1 - d);
+        if (kn >= k0 && kn < k0 + ne) {
+#pragma unroll
+          for (int c = 0; c < NF; ++c) bb[c] = sQ[(kn - k0) * ESTR + c * NpP + nd2];
+        } else {
+          const float* qb = qin + (size_t)kn * ESTR + nd2;
+#pragma unroll
+          for (int c = 0; c < NF; ++c) bb[c] = __ldg(qb + c * NpP);
+        }
+      } else if (P == PHYS_ADV) {
+        const int bf = -1 - nb;
+        const double xx = p.bxy[((size_t)bf * Nfp + d) * 2], yy = p.bxy[((size_t)bf * Nfp + d) * 2 + 1];
+        bb[0] = (float)adv_exact(p, tnow, xx, yy);
+      } else if (P == PHYS_TM) {
+        bb[0] = a[0]; bb[1] = a[1]; bb[2] = -a[2];
+      } else {
+        bb[0] = -a[0]; bb[1] = -a[1]; bb[2] = a[2];
+      }
+      const float nx = (float)g[8 + f], ny = (float)g[11 + f];
+      const float sc = (float)(-g[5 + f] / g[4]);  // -faceJ / J
+      float fl[NF];
+      if (P == PHYS_ADV) {
+        const float an = (float)p.ax * nx + (float)p.ay * ny;
+        fl[0] = ((an >= 0.0f) ? a[0] : bb[0]) * an;
+      } else if (P == PHYS_TM) {
+        const float w = (a[2] + bb[2]) + ny * (a[0] - bb[0]) - nx * (a[1] - bb[1]);
+        fl[0] = 0.5f * ny * w;
+        fl[1] = -0.5f * nx * w;
+        fl[2] = 0.5f * (ny * (a[0] + bb[0]) - nx * (a[1] + bb[1]) + a[2] - bb[2]);
+      } else {
+        const float w = (a[2] + bb[2]) - ny * (a[0] - bb[0]) + nx * (a[1] - bb[1]);
+        fl[0] = -0.5f * ny * w;
+        fl[1] = 0.5f * nx * w;
+        fl[2] = 0.5f * (nx * (a[1] + bb[1]) - ny * (a[0] + bb[0]) + a[2] - bb[2]);
+      }
+#pragma unroll
+      for (int c = 0; c < NF; ++c) {
+        const float v = fl[c] * sc;
+        const uint32_t o = op_off<SBO>(e * NF + c, 2 * Np + fm);
+        const float h = tf32_hi(v);
+        Ahi[o] = h;
+        Alo[o] = v - h;
+      }
+    }
+    // ---- volume columns of A: row (e, f) holds (alpha_j, beta_j) = the
+    //      geometric combination of the input fields feeding output field f
+    const int row = tid, e = row / NF, fo = row - e * NF;
+    if (e < ne) {
+      const double* g = sG + e * 16;
+      const float rx = (float)g[0], ry = (float)g[1], sx = (float)g[2], sy = (float)g[3];
+      const float* qe = sQ + e * ESTR;
+      // per input node j: the (alpha, beta) pair of this row
+      auto ab = [&](int j, float& al, float& be) {
+        if (P == PHYS_ADV) {
+          const float u = qe[j];
+          al = ((float)p.ax * rx + (float)p.ay * ry) * u;
+          be = ((float)p.ax * sx + (float)p.ay * sy) * u;
+        } else if (P == PHYS_TM) {  // Hx' = Dy Ez, Hy' = -Dx Ez, Ez' = -Dx Hy + Dy Hx
+          const float hx = qe[j], hy = qe[NpP + j], ez = qe[2 * NpP + j];
+          if (fo == 0) { al = ry * ez; be = sy * ez; }
+          else if (fo == 1) { al = -rx * ez; be = -sx * ez; }
+          else { al = ry * hx - rx * hy; be = sy * hx - sx * hy; }
+        } else {                    // Ex' = -Dy Hz, Ey' = Dx Hz, Hz' = Dx Ey - Dy Ex
+          const float ex = qe[j], ey = qe[NpP + j], hz = qe[2 * NpP + j];
+          if (fo == 0) { al = -ry * hz; be = -sy * hz; }
+          else if (fo == 1) { al = rx * hz; be = sx * hz; }
+          else { al = rx * ey - ry * ex; be = sx * ey - sy * ex; }
+        }
+      };
+      // columns k < 2 Np in 4-wide chunks: k < Np -> alpha_k, else beta_{k - Np};
+      // a full chunk is one conflict-free 16-byte store per split (a quarter
+      // warp fills one 128-byte core-matrix row block)
+#pragma unroll 2
+      for (int c = 0; c < (2 * Np + 3) / 4; ++c) {
+        float v[4];
+#pragma unroll
+        for (int l = 0; l < 4; ++l) {
+          const int k = 4 * c + l;
+          float al = 0.f, be = 0.f;
+          if (k < 2 * Np) ab(k < Np ? k : k - Np, al, be);
+          v[l] = k < Np ? al : be;
+        }
+        const uint32_t o = op_off<SBO>(row, 4 * c);
+        if (4 * c + 3 < 2 * Np) {
+          const float4 h = make_float4(tf32_hi(v[0]), tf32_hi(v[1]), tf32_hi(v[2]), tf32_hi(v[3]));
+          *reinterpret_cast<float4*>(Ahi + o) = h;
+          *reinterpret_cast<float4*>(Alo + o) = make_float4(v[0] - h.x, v[1] - h.y, v[2] - h.z, v[3] - h.w);
+        } else {
+#pragma unroll
+          for (int l = 0; l < 4; ++l)
+            if (4 * c + l < 2 * Np) {
+              const float h = tf32_hi(v[l]);
+              Ahi[o + l] = h;
+              Alo[o + l] = v[l] - h;
+            }
+        }
+      }
+    }
+    // make the generic-proxy writes of A visible to the tensor core
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+      tc_fence_after();
+#pragma unroll 1
+      for (int s = 0; s < KP / 8; ++s) {
+        const uint64_t dAh = smem_desc(aH + s * 256, 128, SBO), dAl = smem_desc(aL + s * 256, 128, SBO);
+        const uint64_t dBh = smem_desc(bH + s * 256, 128, SBO), dBl = smem_desc(bL + s * 256, 128, SBO);
+        tc_mma_tf32(tmem, dAh, dBh, C::kIdesc, s > 0 ? 1u : 0u);
+        tc_mma_tf32(tmem, dAh, dBl, C::kIdesc, 1u);
+        tc_mma_tf32(tmem, dAl, dBh, C::kIdesc, 1u);
+      }
+      tc_commit(&bar[3]);
+    }
+    ok = __syncthreads_and(mbar_wait(&bar[3], phm, p.status));
+    phm ^= 1;
+    if (!ok) break;
+    tc_fence_after();
+    // ---- epilogue: thread row = (element, field), all nodes of that row
+    float rhs[NC];
+    if (NC == 32) tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16), rhs);
+    else tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16), rhs);
+    if (e < ne) {
+      const size_t base = (size_t)(k0 + e) * ESTR + (size_t)fo * NpP;
+      const float* qrow = sQ + e * ESTR + fo * NpP;
+      float* out = static_cast<float*>(p.out);
+      float* aux = static_cast<float*>(p.aux);
+      if (p.mode == MODE_RHS) {
+#pragma unroll
+        for (int j = 0; j < NpP; j += 4)
+          *reinterpret_cast<float4*>(out + base + j) =
+              make_float4(j < Np ? rhs[j] : 0.f, j + 1 < Np ? rhs[j + 1] : 0.f, j + 2 < Np ? rhs[j + 2] : 0.f,
+                          j + 3 < Np ? rhs[j + 3] : 0.f);
+      } else if (p.mode == MODE_LSERK) {
+        const float ca = (float)p.ca, cb = (float)p.cb, dt = (float)p.dt;
+        float4 rv[NpP / 4];
+#pragma unroll
+        for (int j = 0; j < NpP; j += 4) rv[j / 4] = *reinterpret_cast<const float4*>(aux + base + j);
+#pragma unroll
+        for (int j = 0; j < NpP; j += 4) {
+          const float4 qv = *reinterpret_cast<const float4*>(qrow + j);
+          float4 r = rv[j / 4];
+          r.x = ca * r.x + dt * (j < Np ? rhs[j] : 0.f);
+          r.y = ca * r.y + dt * (j + 1 < Np ? rhs[j + 1] : 0.f);
+          r.z = ca * r.z + dt * (j + 2 < Np ? rhs[j + 2] : 0.f);
+          r.w = ca * r.w + dt * (j + 3 < Np ? rhs[j + 3] : 0.f);
+          *reinterpret_cast<float4*>(aux + base + j) = r;
+          *reinterpret_cast<float4*>(out + base + j) =
+              make_float4(qv.x + cb * r.x, qv.y + cb * r.y, qv.z + cb * r.z, qv.w + cb * r.w);
+        }
+      } else {
+        float* q0 = static_cast<float*>(p.q0);
+        const float co = (float)p.ca, wa = (float)p.cb;
+        for (int j = 0; j < Np; ++j) {
+          const size_t o = base + j;
+          if (p.stage == 0) {
+            aux[o] = rhs[j];
+            out[o] = qrow[j] + co * rhs[j];
+          } else if (p.stage < 3) {
+            aux[o] = aux[o] + wa * rhs[j];
+            out[o] = q0[o] + co * rhs[j];
+          } else {
+            q0[o] = q0[o] + co * (aux[o] + rhs[j]);
+          }
+        }
+      }
+    }
+    tc_fence_before();
+    __syncthreads();
+  }
+  // ---- release TMEM on every exit path
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    tmem_dealloc32(tmem);
+  }
+}
+
+}  // namespace dgk

@@ -27,6 +27,7 @@ struct dgc_handle_s {
   double* d_tau = nullptr;    // [K][4] laplace penalty per face
   void* d_mats64[2] = {nullptr, nullptr};  // weak, strong (transposed, padded)
   void* d_mats32[2] = {nullptr, nullptr};
+  void* d_tc_b = nullptr;     // FP32 tensor-core operand [Dr | Ds | LIFT] (weak form, split TF32)
   int* d_status = nullptr;    // device-side error word
   double* d_time = nullptr;   // simulation time for graph-replayed steps
   dgk::LaunchInfo rhs_info;

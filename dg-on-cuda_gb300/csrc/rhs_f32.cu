@@ -4,8 +4,8 @@
 
 namespace dgk {
 
-// orders 1..6: register-blocked kernel (dg_rhs_v2.cuh, tile-shape variant v);
-// orders 7, 8: dg_rhs_kernel
+// orders 1..6: variant v of rhs_f32_variant (rhs_launch.cuh); orders 7, 8:
+// dg_rhs_kernel
 template <int N>
 static cudaError_t by_phys(int P, int v, const RhsParams& p, int sm, cudaStream_t s, LaunchInfo* info) {
   if constexpr (N <= 6) {
@@ -43,6 +43,6 @@ cudaError_t rhs_dispatch<float>(int N, int P, int v, const RhsParams& p, int sm,
   }
 }
 
-int rhs_num_variants(int prec_f32, int N) { return (prec_f32 && N <= 6) ? kV2Variants : 1; }
+int rhs_num_variants(int prec_f32, int N) { return (prec_f32 && N <= 6) ? kF32Variants : 1; }
 
 }  // namespace dgk

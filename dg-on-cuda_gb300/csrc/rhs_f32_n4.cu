@@ -1,4 +1,4 @@
-// rhs_f32_n4.cu -- FP32 register-blocked RHS kernels of order 4 (all physics and
+// rhs_f32_n4.cu -- FP32 RHS kernels (all variants) of order 4 (all physics and
 // tile-shape variants); one translation unit per order so they compile in parallel.
 #include "rhs_launch.cuh"
 
@@ -7,9 +7,9 @@ namespace dgk {
 template <>
 cudaError_t rhs_v2_order<4>(int P, int v, const RhsParams* p, int sm, cudaStream_t s, LaunchInfo* info) {
   switch (P) {
-    case PHYS_ADV: return rhs_v2<4, PHYS_ADV>(v, p, sm, s, info);
-    case PHYS_TM: return rhs_v2<4, PHYS_TM>(v, p, sm, s, info);
-    case PHYS_TE: return rhs_v2<4, PHYS_TE>(v, p, sm, s, info);
+    case PHYS_ADV: return rhs_f32_variant<4, PHYS_ADV>(v, p, sm, s, info);
+    case PHYS_TM: return rhs_f32_variant<4, PHYS_TM>(v, p, sm, s, info);
+    case PHYS_TE: return rhs_f32_variant<4, PHYS_TE>(v, p, sm, s, info);
     default: return cudaErrorInvalidValue;
   }
 }

@@ -55,6 +55,7 @@ int rhs_num_variants(int prec_f32, int N);
 
 }  // namespace dgk
 
+#include "dg_rhs_tc.cuh"
 #include "dg_rhs_v2.cuh"
 
 namespace dgk {
@@ -97,6 +98,46 @@ cudaError_t rhs_v2(int v, const RhsParams* p, int sm, cudaStream_t s, LaunchInfo
     case 2: return rhs_v2_shape<N, P, S::G[2], S::EPT[2]>(p, sm, s, info);
     default: return cudaErrorInvalidValue;
   }
+}
+
+template <int N, int P>
+cudaError_t rhs_tc(const RhsParams* p, int sm_count, cudaStream_t s, LaunchInfo* info) {
+  using C = TcConfig<N, P>;
+  static std::once_flag once;
+  static cudaError_t st = cudaSuccess;
+  static int bps = 0;
+  std::call_once(once, [] {
+    st = cudaFuncSetAttribute(dg_rhs_tc_kernel<N, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::kSmem);
+    if (st == cudaSuccess)
+      st = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, dg_rhs_tc_kernel<N, P>, C::kThreads, C::kSmem);
+  });
+  if (st != cudaSuccess) return st;
+  if (info) {
+    info->threads = C::kThreads;
+    info->tile = C::TE;
+    info->smem = C::kSmem;
+    info->blocks_per_sm = bps;
+    return cudaSuccess;
+  }
+  if (!p->mats_tc) return cudaErrorInvalidValue;
+  const int ntiles = (p->K + C::TE - 1) / C::TE;
+  int grid = sm_count * (bps > 0 ? bps : 1);
+  if (grid > ntiles) grid = ntiles;
+  dg_rhs_tc_kernel<N, P><<<grid, C::kThreads, C::kSmem, s>>>(*p);
+  return cudaGetLastError();
+}
+
+// FP32 variants at orders 1..6: 0 = one thread per element-node (dg_rhs_kernel),
+// 1..3 = register-blocked tile shapes (dg_rhs_v2_kernel), 4 = tensor cores
+// (dg_rhs_tc_kernel)
+constexpr int kF32Variants = 5;
+
+template <int N, int P>
+cudaError_t rhs_f32_variant(int v, const RhsParams* p, int sm, cudaStream_t s, LaunchInfo* info) {
+  if (v == 0) return info ? rhs_configure<float, N, P>(info) : rhs_launch<float, N, P>(*p, sm, s);
+  if (v >= 1 && v <= 3) return rhs_v2<N, P>(v - 1, p, sm, s, info);
+  if (v == 4) return rhs_tc<N, P>(p, sm, s, info);
+  return cudaErrorInvalidValue;
 }
 
 // per-order entry points, defined in rhs_f32_n<N>.cu
