@@ -12,9 +12,10 @@
 //   D^T (rows = element x field, cols = nodes) = A (rows x K) * B^T (K x nodes)
 // with A built in shared memory per tile and B = [Dr | Ds | LIFT] (one row per
 // output node) loaded once per CTA.  One tcgen05.mma kind::tf32 with M = 128,
-// N = 16 or 32, K = 8 per instruction; D lives in TMEM (32 columns).  Each of
-// the 128 threads then reads its own row (one element-field, all nodes) with
-// tcgen05.ld and applies the stage update with float4 global traffic.
+// N = 16 or 32, K = 8 per instruction; D lives in TMEM (32 columns).  The 256
+// threads then read their rows (one element-field, 16 nodes per thread) with
+// tcgen05.ld (two threads per row, 16 columns each) and applies the stage
+// update with float4 global traffic.
 //
 // Operand layout: K-major, no swizzle ("canonical" core matrices of 8 rows x
 // 16 bytes): element (row, k) at byte (row/8)*SBO + (k/4)*128 + (row%8)*16 +
@@ -79,7 +80,7 @@ struct TcConfig {
   using O = Order<N>;
   static constexpr int Np = O::Np, Nfp = O::Nfp, NpP = O::NpP, NFACE = O::Nface;
   static constexpr int Nf = PhysTraits<P>::Nf;
-  static constexpr int kThreads = 128;
+  static constexpr int kThreads = 256;  // two threads per A/D row (row = tid % 128)
   static constexpr int TE = 128 / Nf;                  // elements per tile (rows = TE * Nf <= 128)
   static constexpr int ESTR = Nf * NpP;
   static constexpr int KP = (2 * Np + NFACE + 7) / 8 * 8;  // contraction length
@@ -95,6 +96,7 @@ struct TcConfig {
   static constexpr uint32_t oBuf = oA + 2 * kABytes;
   static constexpr uint32_t kSmem = oBuf + 2 * kBuf;
   // instruction descriptor: D f32, A/B tf32, both K-major, N >> 3, M >> 4
+  static constexpr int kItems = (TE * NFACE + kThreads - 1) / kThreads;  // face nodes per thread
   static constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(NC >> 3) << 17) |
                                      ((uint32_t)(128 >> 4) << 24);
 };
@@ -105,7 +107,7 @@ __device__ __forceinline__ uint32_t op_off(int row, int k) {  // float offset in
 }
 
 template <int N, int P>
-__global__ void __launch_bounds__(128) dg_rhs_tc_kernel(const RhsParams p) {
+__global__ void __launch_bounds__(256) dg_rhs_tc_kernel(const RhsParams p) {
   using C = TcConfig<N, P>;
   constexpr int Np = C::Np, Nfp = C::Nfp, NpP = C::NpP, NFACE = C::NFACE, NF = C::Nf;
   constexpr int TE = C::TE, ESTR = C::ESTR, KP = C::KP, NC = C::NC, SBO = C::SBO;
@@ -131,7 +133,7 @@ __global__ void __launch_bounds__(128) dg_rhs_tc_kernel(const RhsParams p) {
   }
   if (warp == 0) tmem_alloc32(tmem_slot);
   // zero A (its padding columns and unused rows are never written again)
-  for (int x = tid; x < (int)(2 * C::kABytes / 4); x += 128) Ahi[x] = 0.0f;
+  for (int x = tid; x < (int)(2 * C::kABytes / 4); x += C::kThreads) Ahi[x] = 0.0f;
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
@@ -148,7 +150,7 @@ __global__ void __launch_bounds__(128) dg_rhs_tc_kernel(const RhsParams p) {
   };
   if (tid == 0) {
     mbar_arrive_expect_tx(&bar[2], 2 * C::kBBytes);
-    bulk_g2s(Bhi, p.mats, 2 * C::kBBytes, &bar[2]);
+    bulk_g2s(Bhi, p.mats_tc, 2 * C::kBBytes, &bar[2]);
     if ((int)blockIdx.x < ntiles) issue(blockIdx.x, 0);
   }
   bool ok = mbar_wait(&bar[2], 0, p.status);
@@ -169,63 +171,77 @@ __global__ void __launch_bounds__(128) dg_rhs_tc_kernel(const RhsParams p) {
     const double* sG = bufG(b);
     const int4* sN = bufN(b);
 
-    // ---- face fluxes -> lifted columns of A: gamma = -(faceJ / J) * flux
-    for (int x = tid; x < ne * NFACE; x += 128) {
-      const int e = x / NFACE, fm = x - e * NFACE, f = fm / Nfp, d = fm - f * Nfp;
-      const double* g = sG + e * 16;
-      const int nb = f == 0 ? sN[e].x : (f == 1 ? sN[e].y : sN[e].z);
-      const int nd = fmask<N>(f, d);
-      float a[NF], bb[NF];
+    // ---- face fluxes -> lifted columns of A: gamma = -(faceJ / J) * flux.
+    //      All gathers of a thread are issued before any flux is computed.
+    {
+      float av[C::kItems][NF], bv[C::kItems][NF];
 #pragma unroll
-      for (int c = 0; c < NF; ++c) a[c] = sQ[e * ESTR + c * NpP + nd];
-      if (nb >= 0) {
-        const int kn = nb >> 2, nd2 = fmask<N>(nb & 3, Nfp - 1 - d);
-        if (kn >= k0 && kn < k0 + ne) {
+      for (int it2 = 0; it2 < C::kItems; ++it2) {
+        const int x = tid + it2 * C::kThreads;
+        if (x >= ne * NFACE) continue;
+        const int e = x / NFACE, fm = x - e * NFACE, f = fm / Nfp, d = fm - f * Nfp;
+        const int nb = f == 0 ? sN[e].x : (f == 1 ? sN[e].y : sN[e].z);
+        const int nd = fmask<N>(f, d);
 #pragma unroll
-          for (int c = 0; c < NF; ++c) bb[c] = sQ[(kn - k0) * ESTR + c * NpP + nd2];
+        for (int c = 0; c < NF; ++c) av[it2][c] = sQ[e * ESTR + c * NpP + nd];
+        if (nb >= 0) {
+          const int kn = nb >> 2, nd2 = fmask<N>(nb & 3, Nfp - 1 - d);
+          if (kn >= k0 && kn < k0 + ne) {
+#pragma unroll
+            for (int c = 0; c < NF; ++c) bv[it2][c] = sQ[(kn - k0) * ESTR + c * NpP + nd2];
+          } else {
+            const float* qb = qin + (size_t)kn * ESTR + nd2;
+#pragma unroll
+            for (int c = 0; c < NF; ++c) bv[it2][c] = __ldg(qb + c * NpP);
+          }
+        } else if (P == PHYS_ADV) {
+          const int bf = -1 - nb;
+          const double xx = p.bxy[((size_t)bf * Nfp + d) * 2], yy = p.bxy[((size_t)bf * Nfp + d) * 2 + 1];
+          bv[it2][0] = (float)adv_exact(p, tnow, xx, yy);
+        } else if (P == PHYS_TM) {
+          bv[it2][0] = av[it2][0]; bv[it2][1] = av[it2][1]; bv[it2][2] = -av[it2][2];
         } else {
-          const float* qb = qin + (size_t)kn * ESTR + nd2;
-#pragma unroll
-          for (int c = 0; c < NF; ++c) bb[c] = __ldg(qb + c * NpP);
+          bv[it2][0] = -av[it2][0]; bv[it2][1] = -av[it2][1]; bv[it2][2] = av[it2][2];
         }
-      } else if (P == PHYS_ADV) {
-        const int bf = -1 - nb;
-        const double xx = p.bxy[((size_t)bf * Nfp + d) * 2], yy = p.bxy[((size_t)bf * Nfp + d) * 2 + 1];
-        bb[0] = (float)adv_exact(p, tnow, xx, yy);
-      } else if (P == PHYS_TM) {
-        bb[0] = a[0]; bb[1] = a[1]; bb[2] = -a[2];
-      } else {
-        bb[0] = -a[0]; bb[1] = -a[1]; bb[2] = a[2];
-      }
-      const float nx = (float)g[8 + f], ny = (float)g[11 + f];
-      const float sc = (float)(-g[5 + f] / g[4]);  // -faceJ / J
-      float fl[NF];
-      if (P == PHYS_ADV) {
-        const float an = (float)p.ax * nx + (float)p.ay * ny;
-        fl[0] = ((an >= 0.0f) ? a[0] : bb[0]) * an;
-      } else if (P == PHYS_TM) {
-        const float w = (a[2] + bb[2]) + ny * (a[0] - bb[0]) - nx * (a[1] - bb[1]);
-        fl[0] = 0.5f * ny * w;
-        fl[1] = -0.5f * nx * w;
-        fl[2] = 0.5f * (ny * (a[0] + bb[0]) - nx * (a[1] + bb[1]) + a[2] - bb[2]);
-      } else {
-        const float w = (a[2] + bb[2]) - ny * (a[0] - bb[0]) + nx * (a[1] - bb[1]);
-        fl[0] = -0.5f * ny * w;
-        fl[1] = 0.5f * nx * w;
-        fl[2] = 0.5f * (nx * (a[1] + bb[1]) - ny * (a[0] + bb[0]) + a[2] - bb[2]);
       }
 #pragma unroll
-      for (int c = 0; c < NF; ++c) {
-        const float v = fl[c] * sc;
-        const uint32_t o = op_off<SBO>(e * NF + c, 2 * Np + fm);
-        const float h = tf32_hi(v);
-        Ahi[o] = h;
-        Alo[o] = v - h;
+      for (int it2 = 0; it2 < C::kItems; ++it2) {
+        const int x = tid + it2 * C::kThreads;
+        if (x >= ne * NFACE) continue;
+        const int e = x / NFACE, fm = x - e * NFACE, f = fm / Nfp;
+        const double* g = sG + e * 16;
+        const float* a = av[it2];
+        const float* bb = bv[it2];
+        const float nx = (float)g[8 + f], ny = (float)g[11 + f];
+        const float sc = (float)(-g[5 + f] / g[4]);  // -faceJ / J
+        float fl[NF];
+        if (P == PHYS_ADV) {
+          const float an = (float)p.ax * nx + (float)p.ay * ny;
+          fl[0] = ((an >= 0.0f) ? a[0] : bb[0]) * an;
+        } else if (P == PHYS_TM) {
+          const float w = (a[2] + bb[2]) + ny * (a[0] - bb[0]) - nx * (a[1] - bb[1]);
+          fl[0] = 0.5f * ny * w;
+          fl[1] = -0.5f * nx * w;
+          fl[2] = 0.5f * (ny * (a[0] + bb[0]) - nx * (a[1] + bb[1]) + a[2] - bb[2]);
+        } else {
+          const float w = (a[2] + bb[2]) - ny * (a[0] - bb[0]) + nx * (a[1] - bb[1]);
+          fl[0] = -0.5f * ny * w;
+          fl[1] = 0.5f * nx * w;
+          fl[2] = 0.5f * (nx * (a[1] + bb[1]) - ny * (a[0] + bb[0]) + a[2] - bb[2]);
+        }
+#pragma unroll
+        for (int c = 0; c < NF; ++c) {
+          const float v = fl[c] * sc;
+          const uint32_t o = op_off<SBO>(e * NF + c, 2 * Np + fm);
+          const float h = tf32_hi(v);
+          Ahi[o] = h;
+          Alo[o] = v - h;
+        }
       }
     }
     // ---- volume columns of A: row (e, f) holds (alpha_j, beta_j) = the
     //      geometric combination of the input fields feeding output field f
-    const int row = tid, e = row / NF, fo = row - e * NF;
+    const int row = tid & 127, half = tid >> 7, e = row / NF, fo = row - e * NF;
     if (e < ne) {
       const double* g = sG + e * 16;
       const float rx = (float)g[0], ry = (float)g[1], sx = (float)g[2], sy = (float)g[3];
@@ -252,7 +268,7 @@ __global__ void __launch_bounds__(128) dg_rhs_tc_kernel(const RhsParams p) {
       // a full chunk is one conflict-free 16-byte store per split (a quarter
       // warp fills one 128-byte core-matrix row block)
 #pragma unroll 2
-      for (int c = 0; c < (2 * Np + 3) / 4; ++c) {
+      for (int c = half; c < (2 * Np + 3) / 4; c += 2) {
         float v[4];
 #pragma unroll
         for (int l = 0; l < 4; ++l) {
@@ -296,51 +312,59 @@ __global__ void __launch_bounds__(128) dg_rhs_tc_kernel(const RhsParams p) {
     phm ^= 1;
     if (!ok) break;
     tc_fence_after();
-    // ---- epilogue: thread row = (element, field), all nodes of that row
-    float rhs[NC];
-    if (NC == 32) tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16), rhs);
-    else tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16), rhs);
-    if (e < ne) {
-      const size_t base = (size_t)(k0 + e) * ESTR + (size_t)fo * NpP;
-      const float* qrow = sQ + e * ESTR + fo * NpP;
-      float* out = static_cast<float*>(p.out);
-      float* aux = static_cast<float*>(p.aux);
-      if (p.mode == MODE_RHS) {
+    // ---- epilogue: thread (row, half) = (element, field) and nodes
+    //      [16 half, 16 half + 16) of that row, read from its warp's TMEM lanes
+    const int j0 = 16 * half;
+    if (j0 < NC) {
+      float rhs[16];
+      tmem_ld16(tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)j0, rhs);
+      if (e < ne && j0 < NpP) {
+        const size_t base = (size_t)(k0 + e) * ESTR + (size_t)fo * NpP;
+        const float* qrow = sQ + e * ESTR + fo * NpP;
+        float* out = static_cast<float*>(p.out);
+        float* aux = static_cast<float*>(p.aux);
+        constexpr int J1 = NpP < 16 ? NpP : 16;  // nodes of this half (upper half: NpP - 16)
+        const int jn = (NpP - j0) < J1 ? (NpP - j0) : J1;
+        auto rv = [&](int j) { return (j0 + j) < Np ? rhs[j] : 0.0f; };
+        if (p.mode == MODE_RHS) {
 #pragma unroll
-        for (int j = 0; j < NpP; j += 4)
-          *reinterpret_cast<float4*>(out + base + j) =
-              make_float4(j < Np ? rhs[j] : 0.f, j + 1 < Np ? rhs[j + 1] : 0.f, j + 2 < Np ? rhs[j + 2] : 0.f,
-                          j + 3 < Np ? rhs[j + 3] : 0.f);
-      } else if (p.mode == MODE_LSERK) {
-        const float ca = (float)p.ca, cb = (float)p.cb, dt = (float)p.dt;
-        float4 rv[NpP / 4];
+          for (int j = 0; j < J1; j += 4)
+            if (j < jn)
+              *reinterpret_cast<float4*>(out + base + j0 + j) = make_float4(rv(j), rv(j + 1), rv(j + 2), rv(j + 3));
+        } else if (p.mode == MODE_LSERK) {
+          const float ca = (float)p.ca, cb = (float)p.cb, dt = (float)p.dt;
+          float4 r4[J1 / 4];
 #pragma unroll
-        for (int j = 0; j < NpP; j += 4) rv[j / 4] = *reinterpret_cast<const float4*>(aux + base + j);
+          for (int j = 0; j < J1; j += 4)
+            if (j < jn) r4[j / 4] = *reinterpret_cast<const float4*>(aux + base + j0 + j);
 #pragma unroll
-        for (int j = 0; j < NpP; j += 4) {
-          const float4 qv = *reinterpret_cast<const float4*>(qrow + j);
-          float4 r = rv[j / 4];
-          r.x = ca * r.x + dt * (j < Np ? rhs[j] : 0.f);
-          r.y = ca * r.y + dt * (j + 1 < Np ? rhs[j + 1] : 0.f);
-          r.z = ca * r.z + dt * (j + 2 < Np ? rhs[j + 2] : 0.f);
-          r.w = ca * r.w + dt * (j + 3 < Np ? rhs[j + 3] : 0.f);
-          *reinterpret_cast<float4*>(aux + base + j) = r;
-          *reinterpret_cast<float4*>(out + base + j) =
-              make_float4(qv.x + cb * r.x, qv.y + cb * r.y, qv.z + cb * r.z, qv.w + cb * r.w);
-        }
-      } else {
-        float* q0 = static_cast<float*>(p.q0);
-        const float co = (float)p.ca, wa = (float)p.cb;
-        for (int j = 0; j < Np; ++j) {
-          const size_t o = base + j;
-          if (p.stage == 0) {
-            aux[o] = rhs[j];
-            out[o] = qrow[j] + co * rhs[j];
-          } else if (p.stage < 3) {
-            aux[o] = aux[o] + wa * rhs[j];
-            out[o] = q0[o] + co * rhs[j];
-          } else {
-            q0[o] = q0[o] + co * (aux[o] + rhs[j]);
+          for (int j = 0; j < J1; j += 4)
+            if (j < jn) {
+              const float4 qv = *reinterpret_cast<const float4*>(qrow + j0 + j);
+              float4 r = r4[j / 4];
+              r.x = ca * r.x + dt * rv(j);
+              r.y = ca * r.y + dt * rv(j + 1);
+              r.z = ca * r.z + dt * rv(j + 2);
+              r.w = ca * r.w + dt * rv(j + 3);
+              *reinterpret_cast<float4*>(aux + base + j0 + j) = r;
+              *reinterpret_cast<float4*>(out + base + j0 + j) =
+                  make_float4(qv.x + cb * r.x, qv.y + cb * r.y, qv.z + cb * r.z, qv.w + cb * r.w);
+            }
+        } else {
+          float* q0 = static_cast<float*>(p.q0);
+          const float co = (float)p.ca, wa = (float)p.cb;
+          for (int j = 0; j < jn; ++j) {
+            if (j0 + j >= Np) break;
+            const size_t o = base + j0 + j;
+            if (p.stage == 0) {
+              aux[o] = rhs[j];
+              out[o] = qrow[j0 + j] + co * rhs[j];
+            } else if (p.stage < 3) {
+              aux[o] = aux[o] + wa * rhs[j];
+              out[o] = q0[o] + co * rhs[j];
+            } else {
+              q0[o] = q0[o] + co * (aux[o] + rhs[j]);
+            }
           }
         }
       }
