@@ -276,6 +276,7 @@ def main():
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 plain-path timing")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end (host buffer) timing")
+    ap.add_argument("--variant", type=int, default=-1, help="force an RHS kernel variant instead of autotuning")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -299,7 +300,11 @@ def main():
 
     m = meshes.jittered_square(NSIDE, SEED)
     D32 = dg.Discretization(m, "maxwell_te", ORDER, dg.F32)
-    tuned, tune_ms = D32.autotune(reps=10)
+    if args.variant >= 0:
+        D32.set_variant(args.variant)
+        tuned, tune_ms = args.variant, None
+    else:
+        tuned, tune_ms = D32.autotune(reps=10)
     K, Np = D32.K, D32.Np
     x, y = D32.node_xy()
     q_init = te_initial(x, y)

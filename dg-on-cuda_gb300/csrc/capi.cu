@@ -114,25 +114,34 @@ int upload_operators(dgc_handle_s* h, int form) {
   if (!h->d_mats32[form]) CK(cudaMalloc(&h->d_mats32[form], m32.size() * sizeof(float)));
   CK(cudaMemcpy(h->d_mats64[form], m64.data(), m64.size() * sizeof(double), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(h->d_mats32[form], m32.data(), m32.size() * sizeof(float), cudaMemcpyHostToDevice));
-  if (form == 0 && re.N <= 6) {
-    // tensor-core operand: row n = output node, K = [Dr(n,:) | Ds(n,:) | LIFT(n,:)],
-    // K-major core matrices (8 rows x 4 floats), hi / lo TF32 split
-    const int Np = re.Np, NF = 3 * re.Nfp;
-    const int KP = (2 * Np + NF + 7) / 8 * 8, NC = Np <= 16 ? 16 : 32, SBO4 = KP / 4 * 32;
+  if (form == 1 && re.N <= 6) {
+    // tensor-core operand (the FP32 tcgen05 kernel evaluates the strong form):
+    // row n = output node, K = [Dr(n,:) pad | Ds(n,:) pad | LIFT(n,:)] with the
+    // derivative blocks padded to NpP columns; K-major core matrices (8 rows x
+    // 4 floats); hi / lo TF32 split
+    const int Np = re.Np, NF = 3 * re.Nfp, NpP = dgc::padded_nodes(re.N);
+    const int KP = (2 * NpP + NF + 7) / 8 * 8, NC = Np <= 16 ? 16 : 32, SBO4 = KP / 4 * 32;
     std::vector<float> tc((size_t)2 * NC * KP, 0.0f);
     for (int n = 0; n < Np; ++n)
-      for (int k = 0; k < 2 * Np + NF; ++k) {
-        const double x = k < Np ? Dr[(size_t)n * Np + k]
-                                : (k < 2 * Np ? Ds[(size_t)n * Np + k - Np] : L[(size_t)n * NF + k - 2 * Np]);
-        const float xf = (float)x;
-        uint32_t bits;
-        std::memcpy(&bits, &xf, 4);
-        bits &= 0xFFFFE000u;
-        float hi;
-        std::memcpy(&hi, &bits, 4);
+      for (int k = 0; k < 2 * NpP + NF; ++k) {
+        double x = 0.0;
+        if (k < NpP) x = k < Np ? Dr[(size_t)n * Np + k] : 0.0;
+        else if (k < 2 * NpP) x = (k - NpP) < Np ? Ds[(size_t)n * Np + k - NpP] : 0.0;
+        else x = L[(size_t)n * NF + k - 2 * NpP];
+        // round to nearest TF32 (10 explicit mantissa bits, ties away from zero)
+        auto tf32 = [](float f) {
+          uint32_t b;
+          std::memcpy(&b, &f, 4);
+          b = (b + 0x1000u) & 0xFFFFE000u;
+          float r;
+          std::memcpy(&r, &b, 4);
+          return r;
+        };
+        const float hi = tf32((float)x);
+        const float lo = tf32((float)(x - (double)hi));
         const size_t o = (size_t)(n >> 3) * SBO4 + (k >> 2) * 32 + (n & 7) * 4 + (k & 3);
         tc[o] = hi;
-        tc[(size_t)NC * KP + o] = xf - hi;
+        tc[(size_t)NC * KP + o] = lo;
       }
     if (!h->d_tc_b) CK(cudaMalloc(&h->d_tc_b, tc.size() * sizeof(float)));
     CK(cudaMemcpy(h->d_tc_b, tc.data(), tc.size() * sizeof(float), cudaMemcpyHostToDevice));
