@@ -211,6 +211,17 @@ int device_init(dgc_handle_s* h) {
   if (!m.bxy.empty()) CK(cudaMemcpy(h->d_bxy, m.bxy.data(), m.bxy.size() * sizeof(double), cudaMemcpyHostToDevice));
   CK(cudaMalloc(&h->d_tau, m.tau.size() * sizeof(double)));
   CK(cudaMemcpy(h->d_tau, m.tau.data(), m.tau.size() * sizeof(double), cudaMemcpyHostToDevice));
+  {
+    const std::vector<double> g64 = kernel_geometry<double>(m.geom, h->K);
+    const std::vector<float> g32 = kernel_geometry<float>(m.geom, h->K);
+    const std::vector<float> t32(m.tau.begin(), m.tau.end());
+    CK(cudaMalloc(&h->d_kgeom64, g64.size() * sizeof(double)));
+    CK(cudaMemcpy(h->d_kgeom64, g64.data(), g64.size() * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMalloc(&h->d_kgeom32, g32.size() * sizeof(float)));
+    CK(cudaMemcpy(h->d_kgeom32, g32.data(), g32.size() * sizeof(float), cudaMemcpyHostToDevice));
+    CK(cudaMalloc(&h->d_tau32, t32.size() * sizeof(float)));
+    CK(cudaMemcpy(h->d_tau32, t32.data(), t32.size() * sizeof(float), cudaMemcpyHostToDevice));
+  }
   CK(cudaMalloc(&h->d_status, 64));
   CK(cudaMemset(h->d_status, 0, 64));
   CK(cudaMalloc(&h->d_time, 64));
@@ -238,6 +249,9 @@ void device_free(dgc_handle_s* h) {
   cudaFree(h->d_nbr);
   cudaFree(h->d_bxy);
   cudaFree(h->d_tau);
+  cudaFree(h->d_kgeom64);
+  cudaFree(h->d_kgeom32);
+  cudaFree(h->d_tau32);
   cudaFree(h->d_status);
   cudaFree(h->d_time);
   for (int f = 0; f < 2; ++f) {
@@ -372,7 +386,7 @@ namespace {
 dgk::RhsParams base_params(dgc_handle h) {
   dgk::RhsParams p{};
   p.K = h->K;
-  p.geom = h->d_geom;
+  p.geom = h->prec == DGC_F64 ? (const void*)h->d_kgeom64 : (const void*)h->d_kgeom32;
   p.nbr = reinterpret_cast<const int4*>(h->d_nbr);
   p.bxy = h->d_bxy;
   p.mats = h->prec == DGC_F64 ? h->d_mats64[0] : h->d_mats32[0];
@@ -572,12 +586,18 @@ extern "C" int dgc_lserk4_run(dgc_handle h, void* qa, void* qb, void* res, doubl
 
 extern "C" int dgc_check_device_status(dgc_handle h, int* code) {
   if (!h) return fail(DGC_ERR_ARG, "null handle");
-  int v = 0;
-  CK(cudaMemcpy(&v, h->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+  int w[16] = {};
+  CK(cudaMemcpy(w, h->d_status, sizeof w, cudaMemcpyDeviceToHost));
+  const int v = w[0];
   if (code) *code = v;
   if (v != 0) {
-    CK(cudaMemset(h->d_status, 0, sizeof(int)));
-    return fail(DGC_ERR_DEVICE, "device-side error code %d (bounded wait expired)", v);
+    unsigned long long rec[3];
+    std::memcpy(rec, w + 2, sizeof rec);
+    CK(cudaMemset(h->d_status, 0, 64));
+    if (v != 1) return fail(DGC_ERR_DEVICE, "device-side error code %d (singular diagonal block)", v);
+    return fail(DGC_ERR_DEVICE,
+                "device-side error code %d (bounded wait expired after %llu ns, %llu SM cycles, %llu polls)", v,
+                rec[0], rec[1], rec[2]);
   }
   return DGC_OK;
 }

@@ -63,10 +63,13 @@ __device__ __forceinline__ uint64_t globaltimer_ns() {
 }
 
 // Wait for phase `parity` of the barrier to complete.  Gives up after about
-// one second, records kErrBarrierTimeout in *status and returns false.
+// one second, records kErrBarrierTimeout in status[0] and returns false.  The
+// first wait to give up also records, in the 8-byte words at status + 2,
+// status + 4 and status + 6: the elapsed global-timer ns, the elapsed SM
+// cycles and the number of polls.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* status) {
   const uint32_t a = smem_u32(bar);
-  uint64_t t0 = 0;
+  uint64_t t0 = 0, c0 = 0;
   for (uint32_t it = 0;; ++it) {
     uint32_t done;
     asm volatile(
@@ -75,10 +78,21 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* s
         : "r"(a), "r"(parity)
         : "memory");
     if (done) return true;
-    if (it == 64) t0 = globaltimer_ns();
-    if (it > 64 && (it & 255) == 0 && globaltimer_ns() - t0 > 1000000000ull) {
-      if (status) atomicCAS(status, kErrNone, kErrBarrierTimeout);
-      return false;
+    if (it == 64) {
+      t0 = globaltimer_ns();
+      c0 = clock64();
+    }
+    if (it > 64 && (it & 255) == 0) {
+      const uint64_t dt = globaltimer_ns() - t0;
+      if (dt > 1000000000ull) {
+        if (status && atomicCAS(status, kErrNone, kErrBarrierTimeout) == kErrNone) {
+          unsigned long long* rec = reinterpret_cast<unsigned long long*>(status + 2);
+          rec[0] = dt;
+          rec[1] = (unsigned long long)(clock64() - c0);
+          rec[2] = it;
+        }
+        return false;
+      }
     }
   }
 }

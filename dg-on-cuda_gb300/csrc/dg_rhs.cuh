@@ -14,8 +14,9 @@
 // dgc::rk4 (src/explicit_runge_kutta.h:33-51, src/k_axpy.cuh:38-55).
 //
 // Layout (HBM): state q[k][field][NpP], NpP = Np padded to a multiple of 4, so
-// that every element is a contiguous, 16-byte aligned run.  Geometry is FP64,
-// 16 doubles per element; neighbours are one int4 per element.
+// that every element is a contiguous, 16-byte aligned run.  Geometry records
+// are 16 values per element in the kernel's type (rounded once on the host
+// from the FP64 set-up, -1/J precomputed); neighbours are one int4 per element.
 //
 // Execution: persistent CTAs loop over tiles of TE elements.  The operator
 // matrices (stored transposed) are copied into shared memory once per CTA and
@@ -41,7 +42,7 @@ struct RhsParams {
   void* out;          // RHS: rhs | LSERK: next state | RK4: next stage input
   void* aux;          // LSERK: residual | RK4: stage accumulator
   void* q0;           // RK4: base state (updated by the last stage)
-  const double* geom; // [K][16]
+  const void* geom;   // [K][16] kernel geometry records in the kernel type (slot 4 = -1/J)
   const int4* nbr;    // [K]
   const double* bxy;  // boundary face nodes [nbf][Nfp][2]
   const void* mats;   // DrT | DsT | LT, each padded to 16 bytes
@@ -76,7 +77,7 @@ struct RhsConfig {
   static constexpr uint32_t oMats = 16;
   static constexpr uint32_t oQ = oMats + MatLayout<R, N>::kBytes;
   static constexpr uint32_t oGeom = (oQ + TE * ESTR * sizeof(R) + 15) / 16 * 16;
-  static constexpr uint32_t oNbr = oGeom + TE * 16 * sizeof(double);
+  static constexpr uint32_t oNbr = oGeom + TE * 16 * sizeof(R);
   static constexpr uint32_t oFlux = oNbr + TE * 16;
   static constexpr uint32_t kSmem = (oFlux + TE * Nf * O::Nface * sizeof(R) + 15) / 16 * 16;
 };
@@ -108,7 +109,7 @@ __global__ void __launch_bounds__(256) dg_rhs_kernel(const RhsParams p) {
   R* sDsT = sDrT + kD;
   R* sLT = sDrT + 2 * kD;
   R* sQ = reinterpret_cast<R*>(smem + C::oQ);
-  double* sG = reinterpret_cast<double*>(smem + C::oGeom);
+  R* sG = reinterpret_cast<R*>(smem + C::oGeom);
   int4* sN = reinterpret_cast<int4*>(smem + C::oNbr);
   R* sF = reinterpret_cast<R*>(smem + C::oFlux);
 
@@ -116,6 +117,8 @@ __global__ void __launch_bounds__(256) dg_rhs_kernel(const RhsParams p) {
   const int ntiles = (p.K + TE - 1) / TE;
   const R* qin = static_cast<const R*>(p.q_in);
   const double tnow = p.t_dev ? *p.t_dev + p.t : p.t;
+  // scalar parameters converted once to the kernel type
+  const R cax = (R)p.ax, cay = (R)p.ay, cca = (R)p.ca, ccb = (R)p.cb, cdt = (R)p.dt;
 
   if (tid == 0) {
     mbar_init(bar, 1);
@@ -127,7 +130,12 @@ __global__ void __launch_bounds__(256) dg_rhs_kernel(const RhsParams p) {
     mbar_arrive_expect_tx(bar, MatLayout<R, N>::kBytes);
     bulk_g2s(sDrT, p.mats, MatLayout<R, N>::kBytes, bar);
   }
-  if (!mbar_wait(bar, phase, p.status)) return;
+  // All threads must have observed the matrix phase before thread 0 re-arms
+  // the same barrier for the first tile: otherwise a fast tile copy can
+  // complete the next phase before a slow warp polls this one, and that warp
+  // would then wait for a phase that never comes.  The AND also makes a
+  // timed-out wait exit the whole CTA.
+  if (!__syncthreads_and(mbar_wait(bar, phase, p.status))) return;
   phase ^= 1;
 
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
@@ -135,19 +143,19 @@ __global__ void __launch_bounds__(256) dg_rhs_kernel(const RhsParams p) {
     const int ne = min(TE, p.K - k0);
     if (tid == 0) {
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      const uint32_t bq = ne * ESTR * sizeof(R), bg = ne * 16 * sizeof(double), bn = ne * 16;
+      const uint32_t bq = ne * ESTR * sizeof(R), bg = ne * 16 * sizeof(R), bn = ne * 16;
       mbar_arrive_expect_tx(bar, bq + bg + bn);
       bulk_g2s(sQ, qin + (size_t)k0 * ESTR, bq, bar);
-      bulk_g2s(sG, p.geom + (size_t)k0 * 16, bg, bar);
+      bulk_g2s(sG, static_cast<const R*>(p.geom) + (size_t)k0 * 16, bg, bar);
       bulk_g2s(sN, p.nbr + k0, bn, bar);
     }
-    if (!mbar_wait(bar, phase, p.status)) return;
+    if (!__syncthreads_and(mbar_wait(bar, phase, p.status))) return;
     phase ^= 1;
 
     // ---- numerical fluxes on the tile's face nodes, scaled by faceJ
     for (int it = tid; it < ne * NFACE; it += blockDim.x) {
       const int e = it / NFACE, fm = it - e * NFACE, f = fm / Nfp, d = fm - f * Nfp;
-      const double* g = sG + e * 16;
+      const R* g = sG + e * 16;
       const int nb = f == 0 ? sN[e].x : (f == 1 ? sN[e].y : sN[e].z);
       const int nd = fmask<N>(f, d);
       const R* qa = sQ + e * ESTR;
@@ -177,7 +185,7 @@ __global__ void __launch_bounds__(256) dg_rhs_kernel(const RhsParams p) {
       }
       R* fo = sF + e * NF * NFACE + fm;
       if (P == PHYS_ADV) {
-        const R an = (R)p.ax * nx + (R)p.ay * ny;
+        const R an = cax * nx + cay * ny;
         fo[0] = ((an >= (R)0) ? a[0] : b[0]) * an * fJ;
       } else if (P == PHYS_TM) {
         const R d0 = a[0] - b[0], d1 = a[1] - b[1], s2 = a[2] + b[2];
@@ -219,13 +227,13 @@ __global__ void __launch_bounds__(256) dg_rhs_kernel(const RhsParams p) {
 #pragma unroll
         for (int c = 0; c < NF; ++c) lf[c] = fma(l, fe[c * NFACE + m], lf[c]);
       }
-      const double* g = sG + e * 16;
+      const R* g = sG + e * 16;
       const R rx = (R)g[0], ry = (R)g[1], sx = (R)g[2], sy = (R)g[3];
-      const R ilJ = (R)(-1.0 / g[4]);
+      const R ilJ = g[4];  // -1/J
       R rhs[NF];
       if (P == PHYS_ADV) {
         const R dx = rx * ur[0] + sx * us[0], dy = ry * ur[0] + sy * us[0];
-        rhs[0] = (R)p.ax * dx + (R)p.ay * dy + ilJ * lf[0];
+        rhs[0] = cax * dx + cay * dy + ilJ * lf[0];
       } else if (P == PHYS_TM) {  // Hx' = Dy Ez, Hy' = -Dx Ez, Ez' = -Dx Hy + Dy Hx
         rhs[0] = (ry * ur[2] + sy * us[2]) + ilJ * lf[0];
         rhs[1] = -(rx * ur[2] + sx * us[2]) + ilJ * lf[1];
@@ -242,17 +250,16 @@ __global__ void __launch_bounds__(256) dg_rhs_kernel(const RhsParams p) {
 #pragma unroll
         for (int c = 0; c < NF; ++c) out[base + c * NpP] = rhs[c];
       } else if (p.mode == MODE_LSERK) {
-        const R ca = (R)p.ca, cb = (R)p.cb, dt = (R)p.dt;
 #pragma unroll
         for (int c = 0; c < NF; ++c) {
           const size_t o = base + c * NpP;
-          const R r = ca * aux[o] + dt * rhs[c];
+          const R r = cca * aux[o] + cdt * rhs[c];
           aux[o] = r;
-          out[o] = qe[c * NpP + i] + cb * r;
+          out[o] = qe[c * NpP + i] + ccb * r;
         }
       } else {  // classical RK4 stage
         R* q0 = static_cast<R*>(p.q0);
-        const R co = (R)p.ca, wa = (R)p.cb;
+        const R co = cca, wa = ccb;
 #pragma unroll
         for (int c = 0; c < NF; ++c) {
           const size_t o = base + c * NpP;

@@ -106,7 +106,7 @@ struct TcConfig {
   static constexpr int SBO = (KP / 4) * 128;           // bytes between 8-row groups
   static constexpr uint32_t kBBytes = NC * KP * 4;     // one split of B
   static constexpr uint32_t kABytes = 128 * KP * 4;    // one split of A
-  static constexpr uint32_t kQ = TE * ESTR * 4, kG = TE * 16 * 8, kN = TE * 16;
+  static constexpr uint32_t kQ = TE * ESTR * 4, kG = TE * 16 * 4, kN = TE * 16;
   static constexpr uint32_t kBuf = kQ + kG + kN;
   static constexpr uint32_t oBar = 0;                  // 4 mbarriers + TMEM address
   static constexpr uint32_t oB = 64;
@@ -138,7 +138,7 @@ __global__ void __launch_bounds__(256) dg_rhs_tc_kernel(const RhsParams p) {
   float* Ahi = reinterpret_cast<float*>(smem + C::oA);
   float* Alo = Ahi + C::kABytes / 4;
   auto bufQ = [&](int b) { return reinterpret_cast<float*>(smem + C::oBuf + b * C::kBuf); };
-  auto bufG = [&](int b) { return reinterpret_cast<double*>(smem + C::oBuf + b * C::kBuf + C::kQ); };
+  auto bufG = [&](int b) { return reinterpret_cast<float*>(smem + C::oBuf + b * C::kBuf + C::kQ); };
   auto bufN = [&](int b) { return reinterpret_cast<int4*>(smem + C::oBuf + b * C::kBuf + C::kQ + C::kG); };
 
   const int tid = threadIdx.x, warp = tid >> 5;
@@ -146,6 +146,8 @@ __global__ void __launch_bounds__(256) dg_rhs_tc_kernel(const RhsParams p) {
   const int ntiles = (p.K + TE - 1) / TE;
   const float* qin = static_cast<const float*>(p.q_in);
   const double tnow = p.t_dev ? *p.t_dev + p.t : p.t;
+  // scalar parameters converted once to FP32
+  const float cax = (float)p.ax, cay = (float)p.ay, cca = (float)p.ca, ccb = (float)p.cb, cdt = (float)p.dt;
 
   if (tid == 0) {
     for (int i = 0; i < 4; ++i) mbar_init(&bar[i], 1);
@@ -162,10 +164,10 @@ __global__ void __launch_bounds__(256) dg_rhs_tc_kernel(const RhsParams p) {
   auto issue = [&](int tile, int b) {
     const int k0 = tile * TE, ne = min(TE, p.K - k0);
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    const uint32_t bq = ne * ESTR * 4, bg = ne * 16 * 8, bn = ne * 16;
+    const uint32_t bq = ne * ESTR * 4, bg = ne * 16 * 4, bn = ne * 16;
     mbar_arrive_expect_tx(&bar[b], bq + bg + bn);
     bulk_g2s(bufQ(b), qin + (size_t)k0 * ESTR, bq, &bar[b]);
-    bulk_g2s(bufG(b), p.geom + (size_t)k0 * 16, bg, &bar[b]);
+    bulk_g2s(bufG(b), static_cast<const float*>(p.geom) + (size_t)k0 * 16, bg, &bar[b]);
     bulk_g2s(bufN(b), p.nbr + k0, bn, &bar[b]);
   };
   if (tid == 0) {
@@ -192,7 +194,7 @@ __global__ void __launch_bounds__(256) dg_rhs_tc_kernel(const RhsParams p) {
     if (!ok) break;
     ph[b] ^= 1;
     const float* sQ = bufQ(b);
-    const double* sG = bufG(b);
+    const float* sG = bufG(b);
     const int4* sN = bufN(b);
     const bool mine = er < ne && j0 < NC && jn > 0;
     const size_t base = (size_t)(k0 + er) * ESTR + (size_t)fo * NpP + j0;
@@ -240,8 +242,8 @@ __global__ void __launch_bounds__(256) dg_rhs_tc_kernel(const RhsParams p) {
     //      alpha_j = -(rx F_x + ry F_y)_j, beta_j = -(sx F_x + sy F_y)_j of the
     //      flux F of output field f; 4 nodes per 16-byte store
     if (er < ne) {
-      const double* g = sG + er * 16;
-      const float rx = (float)g[0], ry = (float)g[1], sx = (float)g[2], sy = (float)g[3];
+      const float* g = sG + er * 16;
+      const float rx = g[0], ry = g[1], sx = g[2], sy = g[3];
       const float* qe = sQ + er * ESTR;
 #pragma unroll 2
       for (int c = half; c < NpP / 4; c += 2) {
@@ -249,7 +251,7 @@ __global__ void __launch_bounds__(256) dg_rhs_tc_kernel(const RhsParams p) {
         float al[4], be[4];
         if (P == PHYS_ADV) {
           const float4 u = *reinterpret_cast<const float4*>(qe + j);
-          const float cr = -((float)p.ax * rx + (float)p.ay * ry), cs = -((float)p.ax * sx + (float)p.ay * sy);
+          const float cr = -(cax * rx + cay * ry), cs = -(cax * sx + cay * sy);
           al[0] = cr * u.x; al[1] = cr * u.y; al[2] = cr * u.z; al[3] = cr * u.w;
           be[0] = cs * u.x; be[1] = cs * u.y; be[2] = cs * u.z; be[3] = cs * u.w;
         } else {
@@ -294,14 +296,14 @@ __global__ void __launch_bounds__(256) dg_rhs_tc_kernel(const RhsParams p) {
       const int x = tid + s2 * NT;
       if (x >= ne * NFACE) continue;
       const int e = x / NFACE, fm = x - e * NFACE, f = fm / Nfp;
-      const double* g = sG + e * 16;
+      const float* g = sG + e * 16;
       const float* a = av[s2];
       const float* bb = bv[s2];
-      const float nx = (float)g[8 + f], ny = (float)g[11 + f];
-      const float sc = (float)(-g[5 + f] / g[4]);
+      const float nx = g[8 + f], ny = g[11 + f];
+      const float sc = g[5 + f] * g[4];  // -faceJ/J
       float dl[NF];
       if (P == PHYS_ADV) {
-        const float an = (float)p.ax * nx + (float)p.ay * ny;
+        const float an = cax * nx + cay * ny;
         dl[0] = an >= 0.0f ? 0.0f : an * (bb[0] - a[0]);
       } else if (P == PHYS_TM) {
         // Ez* - Ez- = (-dEz + ny dHx - nx dHy)/2, n x H* - n x H- = (ny (Hx+ - Hx-) - nx (Hy+ - Hy-) + dEz)/2
@@ -360,7 +362,7 @@ __global__ void __launch_bounds__(256) dg_rhs_tc_kernel(const RhsParams p) {
           for (int j = 0; j < 16; j += 4)
             if (j < jn) *reinterpret_cast<float4*>(out + base + j) = make_float4(rv(j), rv(j + 1), rv(j + 2), rv(j + 3));
         } else if (p.mode == MODE_LSERK) {
-          const float ca = (float)p.ca, cb = (float)p.cb, dt = (float)p.dt;
+          const float ca = cca, cb = ccb, dt = cdt;
 #pragma unroll
           for (int j = 0; j < 16; j += 4)
             if (j < jn) {
@@ -376,7 +378,7 @@ __global__ void __launch_bounds__(256) dg_rhs_tc_kernel(const RhsParams p) {
             }
         } else {
           float* q0 = static_cast<float*>(p.q0);
-          const float co = (float)p.ca, wa = (float)p.cb;
+          const float co = cca, wa = ccb;
           for (int j = 0; j < jn && j0 + j < Np; ++j) {
             const size_t o = base + j;
             if (p.stage == 0) {

@@ -40,7 +40,7 @@ struct V2Config {
   static constexpr int FSTR = (O::Nface + 3) / 4 * 4;  // padded face-flux row
   static constexpr int kItems = (TE * O::Nface + kThreads - 1) / kThreads;
   static constexpr uint32_t kMat = MatLayout<float, N>::kBytes;
-  static constexpr uint32_t kQ = TE * ESTR * 4, kG = TE * 16 * 8, kN = TE * 16;
+  static constexpr uint32_t kQ = TE * ESTR * 4, kG = TE * 16 * 4, kN = TE * 16;
   static constexpr uint32_t kBuf = kQ + kG + kN;  // one tile buffer (16-byte multiples)
   static constexpr uint32_t oBar = 0;
   static constexpr uint32_t oMats = 32;
@@ -63,7 +63,7 @@ __global__ void __launch_bounds__(V2Config<N, P, G_, EPT_>::kThreads) dg_rhs_v2_
   const float* sMat = reinterpret_cast<const float*>(smem + C::oMats);
   float* sF = reinterpret_cast<float*>(smem + C::oFlux);
   auto bufQ = [&](int b) { return reinterpret_cast<float*>(smem + C::oBuf + b * C::kBuf); };
-  auto bufG = [&](int b) { return reinterpret_cast<double*>(smem + C::oBuf + b * C::kBuf + C::kQ); };
+  auto bufG = [&](int b) { return reinterpret_cast<float*>(smem + C::oBuf + b * C::kBuf + C::kQ); };
   auto bufN = [&](int b) { return reinterpret_cast<int4*>(smem + C::oBuf + b * C::kBuf + C::kQ + C::kG); };
 
   const int tid = threadIdx.x;
@@ -71,6 +71,8 @@ __global__ void __launch_bounds__(V2Config<N, P, G_, EPT_>::kThreads) dg_rhs_v2_
   const int ntiles = (p.K + TE - 1) / TE;
   const float* qin = static_cast<const float*>(p.q_in);
   const double tnow = p.t_dev ? *p.t_dev + p.t : p.t;
+  // scalar parameters converted once to FP32
+  const float cax = (float)p.ax, cay = (float)p.ay, cca = (float)p.ca, ccb = (float)p.cb, cdt = (float)p.dt;
 
   if (tid == 0) {
     mbar_init(&bar[0], 1);
@@ -85,10 +87,10 @@ __global__ void __launch_bounds__(V2Config<N, P, G_, EPT_>::kThreads) dg_rhs_v2_
   auto issue = [&](int tile, int b) {
     const int k0 = tile * TE, ne = min(TE, p.K - k0);
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    const uint32_t bq = ne * ESTR * 4, bg = ne * 16 * 8, bn = ne * 16;
+    const uint32_t bq = ne * ESTR * 4, bg = ne * 16 * 4, bn = ne * 16;
     mbar_arrive_expect_tx(&bar[b], bq + bg + bn);
     bulk_g2s(bufQ(b), qin + (size_t)k0 * ESTR, bq, &bar[b]);
-    bulk_g2s(bufG(b), p.geom + (size_t)k0 * 16, bg, &bar[b]);
+    bulk_g2s(bufG(b), static_cast<const float*>(p.geom) + (size_t)k0 * 16, bg, &bar[b]);
     bulk_g2s(bufN(b), p.nbr + k0, bn, &bar[b]);
   };
 
@@ -97,7 +99,7 @@ __global__ void __launch_bounds__(V2Config<N, P, G_, EPT_>::kThreads) dg_rhs_v2_
     bulk_g2s(const_cast<float*>(sMat), p.mats, C::kMat, &bar[2]);
     if ((int)blockIdx.x < ntiles) issue(blockIdx.x, 0);
   }
-  if (!mbar_wait(&bar[2], 0, p.status)) return;
+  if (!__syncthreads_and(mbar_wait(&bar[2], 0, p.status))) return;  // uniform exit on a timeout
 
   // operator rows of node ni in registers
   float dr[Np], ds[Np], lt[NFACE];
@@ -116,10 +118,10 @@ __global__ void __launch_bounds__(V2Config<N, P, G_, EPT_>::kThreads) dg_rhs_v2_
     const int k0 = tile * TE, ne = min(TE, p.K - k0);
     const int nxt = tile + gridDim.x;
     if (tid == 0 && nxt < ntiles) issue(nxt, b ^ 1);
-    if (!mbar_wait(&bar[b], ph[b], p.status)) return;
+    if (!__syncthreads_and(mbar_wait(&bar[b], ph[b], p.status))) return;
     ph[b] ^= 1;
     const float* sQ = bufQ(b);
-    const double* sG = bufG(b);
+    const float* sG = bufG(b);
     const int4* sN = bufN(b);
 
     // ---- face nodes: gather first, then fluxes
@@ -161,13 +163,13 @@ __global__ void __launch_bounds__(V2Config<N, P, G_, EPT_>::kThreads) dg_rhs_v2_
         if (item[s] < 0) continue;
         const int x = item[s];
         const int e = x / NFACE, fm = x - e * NFACE, f = fm / Nfp;
-        const double* g = sG + e * 16;
-        const float nx = (float)g[8 + f], ny = (float)g[11 + f], fJ = (float)g[5 + f];
+        const float* g = sG + e * 16;
+        const float nx = g[8 + f], ny = g[11 + f], fJ = g[5 + f];
         const float* a = av[s];
         const float* bb = bv[s];
         float* fo = sF + e * NF * FSTR + fm;
         if (P == PHYS_ADV) {
-          const float an = (float)p.ax * nx + (float)p.ay * ny;
+          const float an = cax * nx + cay * ny;
           fo[0] = ((an >= 0.0f) ? a[0] : bb[0]) * an * fJ;
         } else if (P == PHYS_TM) {
           const float w = (a[2] + bb[2]) + ny * (a[0] - bb[0]) - nx * (a[1] - bb[1]);
@@ -231,13 +233,13 @@ __global__ void __launch_bounds__(V2Config<N, P, G_, EPT_>::kThreads) dg_rhs_v2_
 #pragma unroll
           for (int c = 0; c < NF; ++c) lf[c] = fmaf(lt[m], fe[c * FSTR + m], lf[c]);
         }
-        const double* g = sG + e * 16;
-        const float rx = (float)g[0], ry = (float)g[1], sx = (float)g[2], sy = (float)g[3];
-        const float ilJ = (float)(-1.0 / g[4]);
+        const float* g = sG + e * 16;
+        const float rx = g[0], ry = g[1], sx = g[2], sy = g[3];
+        const float ilJ = g[4];  // -1/J
         float rhs[NF];
         if (P == PHYS_ADV) {
           const float dx = rx * ur[0] + sx * us[0], dy = ry * ur[0] + sy * us[0];
-          rhs[0] = (float)p.ax * dx + (float)p.ay * dy + ilJ * lf[0];
+          rhs[0] = cax * dx + cay * dy + ilJ * lf[0];
         } else if (P == PHYS_TM) {
           rhs[0] = (ry * ur[2] + sy * us[2]) + ilJ * lf[0];
           rhs[1] = -(rx * ur[2] + sx * us[2]) + ilJ * lf[1];
@@ -254,7 +256,7 @@ __global__ void __launch_bounds__(V2Config<N, P, G_, EPT_>::kThreads) dg_rhs_v2_
 #pragma unroll
           for (int c = 0; c < NF; ++c) out[base + c * NpP] = rhs[c];
         } else if (p.mode == MODE_LSERK) {
-          const float ca = (float)p.ca, cb = (float)p.cb, dt = (float)p.dt;
+          const float ca = cca, cb = ccb, dt = cdt;
 #pragma unroll
           for (int c = 0; c < NF; ++c) {
             const size_t o = base + c * NpP;
@@ -264,7 +266,7 @@ __global__ void __launch_bounds__(V2Config<N, P, G_, EPT_>::kThreads) dg_rhs_v2_
           }
         } else {
           float* q0 = static_cast<float*>(p.q0);
-          const float co = (float)p.ca, wa = (float)p.cb;
+          const float co = cca, wa = ccb;
 #pragma unroll
           for (int c = 0; c < NF; ++c) {
             const size_t o = base + c * NpP;

@@ -25,6 +25,9 @@ struct dgc_handle_s {
   int32_t* d_nbr = nullptr;   // [K][4]
   double* d_bxy = nullptr;    // boundary face node coordinates
   double* d_tau = nullptr;    // [K][4] laplace penalty per face
+  double* d_kgeom64 = nullptr;  // [K][16] kernel geometry records (dgc::kernel_geometry), FP64
+  float* d_kgeom32 = nullptr;   // [K][16] the same, rounded once to FP32
+  float* d_tau32 = nullptr;     // [K][4] laplace penalty, FP32
   void* d_mats64[2] = {nullptr, nullptr};  // weak, strong (transposed, padded)
   void* d_mats32[2] = {nullptr, nullptr};
   void* d_tc_b = nullptr;     // FP32 tensor-core operand [Dr | Ds | LIFT] (weak form, split TF32)

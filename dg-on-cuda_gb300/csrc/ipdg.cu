@@ -187,9 +187,9 @@ dgk::IpdgParams base(const dgc_handle_s* h) {
   dgk::IpdgParams p{};
   p.K = h->K;
   p.dirichlet = h->desc.dirichlet;
-  p.geom = h->d_geom;
+  p.geom = sizeof(R) == 8 ? (const void*)h->d_kgeom64 : (const void*)h->d_kgeom32;
   p.nbr = reinterpret_cast<const int4*>(h->d_nbr);
-  p.tau = h->d_tau;
+  p.tau = sizeof(R) == 8 ? (const void*)h->d_tau : (const void*)h->d_tau32;
   p.mats = sizeof(R) == 8 ? h->d_mats64[1] : h->d_mats32[1];
   p.mass = sizeof(R) == 8 ? h->ipdg->mass64 : h->ipdg->mass32;
   p.binv = sizeof(R) == 8 ? (const void*)h->ipdg->binv64 : (const void*)h->ipdg->binv32;

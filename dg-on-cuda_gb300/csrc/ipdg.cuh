@@ -42,9 +42,9 @@ struct CgScalars {
 struct IpdgParams {
   int K;
   int dirichlet;
-  const double* geom;   // [K][16]
+  const void* geom;     // [K][16] kernel geometry records, in R (slot 4 = -1/J, 14 = -J)
   const int4* nbr;      // [K]
-  const double* tau;    // [K][4]
+  const void* tau;      // [K][4] penalty per face, in R
   const void* mats;     // strong-form DrT | DsT | LT (R)
   const void* mass;     // M (Np x Np, R), symmetric
   // grad pass
@@ -89,9 +89,9 @@ struct IpdgConfig {
   static constexpr uint32_t oC = oB + TE * O::NpP * sizeof(R);       // tile field C (u for jumps / r)
   static constexpr uint32_t oD = oC + TE * O::NpP * sizeof(R);       // tile field D (b / Ap)
   static constexpr uint32_t oGeom = oD + TE * O::NpP * sizeof(R);
-  static constexpr uint32_t oNbr = oGeom + TE * 16 * sizeof(double);
+  static constexpr uint32_t oNbr = oGeom + TE * 16 * sizeof(R);
   static constexpr uint32_t oTau = oNbr + TE * 16;
-  static constexpr uint32_t oF = oTau + TE * 4 * sizeof(double);     // face work: 2 x TE x Nface
+  static constexpr uint32_t oF = oTau + TE * 4 * sizeof(R);          // face work: 2 x TE x Nface
   static constexpr uint32_t oW = oF + 2 * TE * O::Nface * sizeof(R); // node work: TE x NpP
   static constexpr uint32_t oRed = (oW + TE * O::NpP * sizeof(R) + 15) / 16 * 16;  // 2 x 8 warps doubles
   static constexpr uint32_t kSmem = oRed + 16 * sizeof(double);
@@ -121,9 +121,9 @@ struct IpdgTile {
   __device__ R* B() const { return reinterpret_cast<R*>(smem + C::oB); }
   __device__ R* Cc() const { return reinterpret_cast<R*>(smem + C::oC); }
   __device__ R* Dd() const { return reinterpret_cast<R*>(smem + C::oD); }
-  __device__ double* G() const { return reinterpret_cast<double*>(smem + C::oGeom); }
+  __device__ R* G() const { return reinterpret_cast<R*>(smem + C::oGeom); }
   __device__ int4* Nb() const { return reinterpret_cast<int4*>(smem + C::oNbr); }
-  __device__ double* Tau() const { return reinterpret_cast<double*>(smem + C::oTau); }
+  __device__ R* Tau() const { return reinterpret_cast<R*>(smem + C::oTau); }
   __device__ R* F0() const { return reinterpret_cast<R*>(smem + C::oF); }
   __device__ R* F1() const { return reinterpret_cast<R*>(smem + C::oF) + TE * NFACE; }
   __device__ R* W() const { return reinterpret_cast<R*>(smem + C::oW); }
@@ -147,29 +147,33 @@ struct IpdgTile {
       bulk_g2s(smem + C::oMats, mats, C::kMatBytes, bar);
       if (mass) bulk_g2s(smem + C::oMass, mass, C::kMassBytes, bar);
     }
-    const bool ok = mbar_wait(bar, phase, status);
+    // the barrier is re-armed by the first load(): every thread must have
+    // observed this phase first (a fast tile copy could otherwise complete the
+    // next phase before a slow warp polls this one); the AND also makes a
+    // timed-out wait exit the whole CTA
+    const bool ok = __syncthreads_and(mbar_wait(bar, phase, status));
     phase ^= 1;
     return ok;
   }
 
   // Bulk-load up to four node fields plus geometry / neighbours / tau of a tile.
-  __device__ bool load(int k0, int ne, const R* a, const R* b, const R* c, const R* d, const double* geom,
-                       const int4* nbr, const double* tau, int* status) {
+  __device__ bool load(int k0, int ne, const R* a, const R* b, const R* c, const R* d, const void* geom,
+                       const int4* nbr, const void* tau, int* status) {
     if (threadIdx.x == 0) {
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       const uint32_t bf = ne * NpP * sizeof(R);
-      uint32_t tot = ne * 16 * sizeof(double) + ne * 16 + (tau ? ne * 4 * sizeof(double) : 0);
+      uint32_t tot = ne * 16 * sizeof(R) + ne * 16 + (tau ? ne * 4 * sizeof(R) : 0);
       tot += (a ? bf : 0) + (b ? bf : 0) + (c ? bf : 0) + (d ? bf : 0);
       mbar_arrive_expect_tx(bar, tot);
       if (a) bulk_g2s(A(), a + (size_t)k0 * NpP, bf, bar);
       if (b) bulk_g2s(B(), b + (size_t)k0 * NpP, bf, bar);
       if (c) bulk_g2s(Cc(), c + (size_t)k0 * NpP, bf, bar);
       if (d) bulk_g2s(Dd(), d + (size_t)k0 * NpP, bf, bar);
-      bulk_g2s(G(), geom + (size_t)k0 * 16, ne * 16 * sizeof(double), bar);
+      bulk_g2s(G(), static_cast<const R*>(geom) + (size_t)k0 * 16, ne * 16 * sizeof(R), bar);
       bulk_g2s(Nb(), nbr + k0, ne * 16, bar);
-      if (tau) bulk_g2s(Tau(), tau + (size_t)k0 * 4, ne * 4 * sizeof(double), bar);
+      if (tau) bulk_g2s(Tau(), static_cast<const R*>(tau) + (size_t)k0 * 4, ne * 4 * sizeof(R), bar);
     }
-    const bool ok = mbar_wait(bar, phase, status);
+    const bool ok = __syncthreads_and(mbar_wait(bar, phase, status));
     phase ^= 1;
     return ok;
   }
@@ -187,15 +191,21 @@ __global__ void __launch_bounds__(256) ipdg_grad_kernel(const IpdgParams p) {
   extern __shared__ __align__(128) unsigned char smem[];
   if (MODE == GRAD_PCG && p.cg->done) return;
   T t{smem};
+  // beta = rz_new / rz_old: one FP64 division per CTA, broadcast through shared
+  // memory (t.init's barrier publishes it)
+  __shared__ R s_beta;
+  if (threadIdx.x == 0) {
+    s_beta = (R)0;
+    if (MODE == GRAD_PCG && !p.first) {
+      const int s = p.slot, sp = (s + 2) % 3;
+      s_beta = (R)(p.cg->rz[s] / p.cg->rz[sp]);
+    }
+  }
   if (!t.init(p.mats, nullptr, p.status)) return;
   const R* u_in = static_cast<const R*>(p.u);
   R* pv = static_cast<R*>(p.p);
   const R* pold = static_cast<const R*>(p.p_old);
-  R beta = (R)0;
-  if (MODE == GRAD_PCG && !p.first) {
-    const int s = p.slot, sp = (s + 2) % 3;
-    beta = (R)(p.cg->rz[s] / p.cg->rz[sp]);
-  }
+  const R beta = s_beta;
   if (MODE == GRAD_PCG && blockIdx.x == 0 && threadIdx.x == 0) p.cg->pAp = 0.0;
   const int ntiles = (p.K + TE - 1) / TE;
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
@@ -216,7 +226,7 @@ __global__ void __launch_bounds__(256) ipdg_grad_kernel(const IpdgParams p) {
     // jumps on face nodes
     for (int it = threadIdx.x; it < ne * NFACE; it += blockDim.x) {
       const int e = it / NFACE, fm = it - e * NFACE, f = fm / Nfp, d = fm - f * Nfp;
-      const double* g = t.G() + e * 16;
+      const R* g = t.G() + e * 16;
       const int nb = nb_of<R, N>(t.Nb()[e], f);
       const R um = sU[e * NpP + fmask<N>(f, d)];
       R du;
@@ -254,8 +264,8 @@ __global__ void __launch_bounds__(256) ipdg_grad_kernel(const IpdgParams p) {
         lx = fma(l, fx[m], lx);
         ly = fma(l, fy[m], ly);
       }
-      const double* g = t.G() + e * 16;
-      const R ilJ = (R)(-1.0 / g[4]);
+      const R* g = t.G() + e * 16;
+      const R ilJ = g[4];  // -1/J
       const size_t o = (size_t)(k0 + e) * NpP + i;
       static_cast<R*>(p.qx)[o] = (R)g[0] * ur + (R)g[2] * us + ilJ * lx;
       static_cast<R*>(p.qy)[o] = (R)g[1] * ur + (R)g[3] * us + ilJ * ly;
@@ -291,7 +301,7 @@ __global__ void __launch_bounds__(256) ipdg_div_kernel(const IpdgParams p) {
       return;
     for (int it = threadIdx.x; it < ne * NFACE; it += blockDim.x) {
       const int e = it / NFACE, fm = it - e * NFACE, f = fm / Nfp, d = fm - f * Nfp;
-      const double* g = t.G() + e * 16;
+      const R* g = t.G() + e * 16;
       const int nb = nb_of<R, N>(t.Nb()[e], f);
       const int nd = fmask<N>(f, d);
       const R nx = (R)g[8 + f], ny = (R)g[11 + f];
@@ -340,8 +350,8 @@ __global__ void __launch_bounds__(256) ipdg_div_kernel(const IpdgParams p) {
       const R* fe = t.F0() + e * NFACE;
 #pragma unroll 3
       for (int m = 0; m < NFACE; ++m) lf = fma(t.LT()[m * Np + i], fe[m], lf);
-      const double* g = t.G() + e * 16;
-      au = ((R)g[0] * xr + (R)g[2] * xs) + ((R)g[1] * yr + (R)g[3] * ys) + (R)(-1.0 / g[4]) * lf;
+      const R* g = t.G() + e * 16;
+      au = ((R)g[0] * xr + (R)g[2] * xs) + ((R)g[1] * yr + (R)g[3] * ys) + g[4] * lf;  // g[4] = -1/J
     }
     if (!spd) {
       if (act) static_cast<R*>(p.out)[(size_t)(k0 + e) * NpP + i] = au;
@@ -354,8 +364,8 @@ __global__ void __launch_bounds__(256) ipdg_div_kernel(const IpdgParams p) {
         R s = 0;
 #pragma unroll 5
         for (int j = 0; j < Np; ++j) s = fma(t.M()[j * Np + i], we[j], s);
-        const double* g = t.G() + e * 16;
-        s *= (R)(-g[4]);
+        const R* g = t.G() + e * 16;
+        s *= g[14];  // -J
         const size_t o = (size_t)(k0 + e) * NpP + i;
         if (MODE == DIV_RESID) {
           const R r = t.Dd()[e * NpP + i] - s;
@@ -383,10 +393,13 @@ __global__ void __launch_bounds__(256) pcg_update_kernel(const IpdgParams p) {
   constexpr int TE = IpdgConfig<R, N>::TE, BSTR = IpdgConfig<R, N>::BSTR;
   __shared__ R sr[TE * NpP];
   __shared__ double red[16];
+  __shared__ R s_alpha;
   CgScalars* cg = p.cg;
   if (cg->done) return;
   const int s = p.slot, s1 = (s + 1) % 3;
-  const R alpha = (R)(cg->rz[s] / cg->pAp);
+  if (threadIdx.x == 0) s_alpha = (R)(cg->rz[s] / cg->pAp);  // one FP64 division per CTA
+  __syncthreads();
+  const R alpha = s_alpha;
   R* x = static_cast<R*>(p.x);
   R* r = static_cast<R*>(p.r);
   R* z = static_cast<R*>(p.z);

@@ -67,6 +67,25 @@ enum GeomSlot : int {
 };
 constexpr int kGeomStride = 16;
 
+// Geometry record read by the stage kernels, stored in the kernel's own
+// arithmetic type (FP64 or FP32).  Slots 0-3 and 5-13 are those of the FP64
+// record; slot 4 holds -1/J (the lift scale) and slot 14 holds -J (the mass
+// scale of the SPD form), so that an FP32 kernel performs no FP64 arithmetic.
+enum KernelGeomSlot : int { KG_NEG_INV_J = 4, KG_NEG_J = 14 };
+
+template <typename R>
+std::vector<R> kernel_geometry(const std::vector<double>& geom, int K) {
+  std::vector<R> g((size_t)K * kGeomStride, R(0));
+  for (int k = 0; k < K; ++k) {
+    const double* s = &geom[(size_t)k * kGeomStride];
+    R* d = &g[(size_t)k * kGeomStride];
+    for (int i = 0; i < 14; ++i) d[i] = (R)s[i];
+    d[KG_NEG_INV_J] = (R)(-1.0 / s[G_J]);
+    d[KG_NEG_J] = (R)(-s[G_J]);
+  }
+  return g;
+}
+
 struct MeshData {
   int K = 0, nv = 0, N = 0, Np = 0, Nfp = 0;
   std::vector<double> vx, vy;

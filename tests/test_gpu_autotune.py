@@ -67,3 +67,22 @@ def test_autotune_selects_and_caches(tmp_path, monkeypatch):
     c2, t2 = D2.autotune(measure=False)
     assert c2 == chosen and t2 is None
     assert D2.info.rhs_tile == D.info.rhs_tile
+
+
+@pytest.mark.parametrize("prec", [dg.F32, dg.F64])
+def test_variants_repeatable_at_scale(prec):
+    """K = 32768, N = 6: every variant gives bitwise-repeatable RHS values over
+    many launches (persistent CTAs over several tiles each) and no barrier
+    wait expires."""
+    m = meshes.jittered_square(128, 5)
+    D = dg.Discretization(m, "maxwell_te", 6, prec)
+    o = oracle.Oracle(m.xy, m.cells, 6)
+    q = D.upload(o.exact(oracle.problem(oracle.MAXWELL_TE, 1.0, 1.0, 0), 0.1))
+    for v in range(D.num_variants()):
+        D.set_variant(v)
+        ref = D.rhs(q, 0.1).clone()
+        out = D.empty_state()
+        for _ in range(40):
+            D.rhs(q, 0.1, out=out)
+            assert torch.equal(out, ref), v
+        D.check()

@@ -135,3 +135,35 @@ def test_laplace_handle_rejects_time_stepping():
     A = dg.Discretization(m, "advection", 2, dg.F64)
     with pytest.raises(dg.DgcError, match="LAPLACE"):
         A.laplace(A.empty_state())
+
+
+@pytest.mark.parametrize("prec", [dg.F64, dg.F32])
+def test_apply_repeatable_at_scale(prec):
+    """Many CTAs, several tiles each: repeated applies are bitwise identical and
+    no barrier wait expires (a barrier re-armed before every warp had observed
+    its previous phase used to leave CTAs waiting out their time limit)."""
+    m = meshes.jittered_square(128, 7)   # K = 32768
+    D = dg.Discretization(m, "laplace", 4, prec, tau=dg.TAU_SCALED)
+    x, _ = D.node_xy()
+    u = np.random.default_rng(1).standard_normal(x.size)
+    U = D.upload(u.astype(np.float32) if prec == dg.F32 else u)
+    first = D.download(D.spd(U))
+    for _ in range(30):
+        assert np.array_equal(D.download(D.spd(U)), first)
+    lap = D.download(D.laplace(U))
+    for _ in range(10):
+        assert np.array_equal(D.download(D.laplace(U)), lap)
+    D.check()
+
+
+def test_mixed_ir_converges_at_scale():
+    m = meshes.jittered_square(128, 7)   # K = 32768, N = 4
+    D = dg.Discretization(m, "laplace", 4, dg.F64, tau=dg.TAU_SCALED)
+    x, y = D.node_xy()
+    f = 2 * np.pi ** 2 * np.sin(np.pi * x) * np.sin(np.pi * y)
+    b = D.mass(D.upload(f.reshape(-1)))
+    xs, st = D.pcg(b, mode=dg.SOLVE_MIXED_IR, rtol=1e-10, inner_rtol=1e-4, maxit=20000)
+    assert st["converged"] and st["final_relres"] <= 1e-10
+    ex = (np.sin(np.pi * x) * np.sin(np.pi * y)).reshape(-1)
+    assert relerr(D.download(xs).reshape(-1), ex) < 1e-6
+    D.check()
