@@ -40,6 +40,16 @@ SEED = 2026
 METRIC = "GDOF/s (Maxwell TE N=6 K=32768, LSERK4, mixed FP32 vs FP64 plain)"
 UNIT = "GDOF/s"
 WORKLOAD = "maxwell_te_pec_cavity_k32768_n6_lserk4"
+# FP32 stage-kernel variants at order 6 (dgc_set_variant / dgc_autotune)
+STAGE_KERNELS = {
+    0: "dgk::dg_rhs_kernel<float,6,PHYS_TE>",
+    1: "dgk::dg_rhs_v2_kernel<6,PHYS_TE,8,4>",
+    2: "dgk::dg_rhs_v2_kernel<6,PHYS_TE,4,8>",
+    3: "dgk::dg_rhs_v2_kernel<6,PHYS_TE,4,4>",
+    4: "dgk::dg_rhs_tc_kernel<6,PHYS_TE> (tcgen05, split TF32)",
+    5: "dgk::dg_rhs_blk_kernel<6,PHYS_TE,1>",
+    6: "dgk::dg_rhs_blk_kernel<6,PHYS_TE,2>",
+}
 
 
 def dist_env():
@@ -357,15 +367,15 @@ def main():
 
     # roofline of the dominant kernel (the fused RHS + LSERK4 stage): compulsory
     # bytes per element = read q, read res, write res, write q (3 fields x Np x 4 B
-    # each) + 14 FP64 geometric factors + 3 int32 neighbour indices
-    alg_bytes_elem = 4 * 3 * Np * 4 + 14 * 8 + 3 * 4
+    # each) + 14 FP32 geometric factors + 3 int32 neighbour indices
+    alg_bytes_elem = 4 * 3 * Np * 4 + 14 * 4 + 3 * 4
     alg_bytes = alg_bytes_elem * K
     launch_ms = float(stage_ms.mean())
     achieved = alg_bytes / (launch_ms * 1e-3) / 1e9
     peak, peak_kind = measured_peak()
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": read_traffic(), "peak_source": peak_kind,
-                "kernel": "dgk::dg_rhs_kernel<float,6,PHYS_TE> (LSERK4 stage)",
+                "kernel": STAGE_KERNELS.get(tuned, "variant %s" % tuned) + " (LSERK4 stage)",
                 "alg_bytes_per_launch": alg_bytes, "alg_bytes_per_element": alg_bytes_elem,
                 "launch_ms": launch_ms, "stage_ms": [float(v) for v in stage_ms.mean(axis=0)],
                 "tile": {"variant": tuned, "elements_per_tile": D32.info.rhs_tile,

@@ -114,6 +114,21 @@ int upload_operators(dgc_handle_s* h, int form) {
   if (!h->d_mats32[form]) CK(cudaMalloc(&h->d_mats32[form], m32.size() * sizeof(float)));
   CK(cudaMemcpy(h->d_mats64[form], m64.data(), m64.size() * sizeof(double), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(h->d_mats32[form], m32.data(), m32.size() * sizeof(float), cudaMemcpyHostToDevice));
+  if (form == 0) {
+    // register-blocked kernel operand: rows j of Dr^T, Ds^T (j < Np) and m of
+    // LIFT^T (m < 3 Nfp), each padded with zeros to NpP columns
+    const int Np = re.Np, NF = 3 * re.Nfp, NpP = dgc::padded_nodes(re.N);
+    std::vector<float> bk((size_t)(2 * Np + NF) * NpP, 0.0f);
+    for (int j = 0; j < Np; ++j)
+      for (int i = 0; i < Np; ++i) {
+        bk[(size_t)j * NpP + i] = (float)Dr[(size_t)i * Np + j];
+        bk[(size_t)(Np + j) * NpP + i] = (float)Ds[(size_t)i * Np + j];
+      }
+    for (int m = 0; m < NF; ++m)
+      for (int i = 0; i < Np; ++i) bk[(size_t)(2 * Np + m) * NpP + i] = (float)L[(size_t)i * NF + m];
+    if (!h->d_blk_b) CK(cudaMalloc(&h->d_blk_b, bk.size() * sizeof(float)));
+    CK(cudaMemcpy(h->d_blk_b, bk.data(), bk.size() * sizeof(float), cudaMemcpyHostToDevice));
+  }
   if (form == 1 && re.N <= 6) {
     // tensor-core operand (the FP32 tcgen05 kernel evaluates the strong form):
     // row n = output node, K = [Dr(n,:) pad | Ds(n,:) pad | LIFT(n,:)] with the
@@ -259,6 +274,7 @@ void device_free(dgc_handle_s* h) {
     cudaFree(h->d_mats32[f]);
   }
   cudaFree(h->d_tc_b);
+  cudaFree(h->d_blk_b);
   ipdg_free(h);
 }
 
@@ -391,6 +407,7 @@ dgk::RhsParams base_params(dgc_handle h) {
   p.bxy = h->d_bxy;
   p.mats = h->prec == DGC_F64 ? h->d_mats64[0] : h->d_mats32[0];
   p.mats_tc = h->prec == DGC_F32 ? h->d_tc_b : nullptr;
+  p.mats_blk = h->prec == DGC_F32 ? h->d_blk_b : nullptr;
   p.ax = h->desc.ax;
   p.ay = h->desc.ay;
   p.gx0 = h->desc.gx0;

@@ -47,6 +47,7 @@ struct RhsParams {
   const double* bxy;  // boundary face nodes [nbf][Nfp][2]
   const void* mats;   // DrT | DsT | LT, each padded to 16 bytes
   const void* mats_tc;// FP32 tensor-core operand [Dr | Ds | LIFT] (split TF32, core-matrix layout)
+  const void* mats_blk;// FP32 rows of Dr^T | Ds^T | LIFT^T, each padded to NpP columns (weak form)
   double t, dt;       // time of the operator evaluation (offset when t_dev is set), step size
   const double* t_dev;// optional device-resident base time: operator time = *t_dev + t
   double ca, cb;      // LSERK: a_k, b_k | RK4: output coefficient, accumulator weight
@@ -54,7 +55,19 @@ struct RhsParams {
   double gx0, gy0, gw;
   int bc, mode, stage;
   int* status;
+  // FP32 copies of ax, ay, ca, cb, dt, filled by rhs_dispatch<float> so that
+  // FP32 kernels convert nothing on the (slow) FP64 pipe
+  float fax, fay, fca, fcb, fdt;
 };
+
+inline RhsParams with_f32_scalars(RhsParams p) {
+  p.fax = (float)p.ax;
+  p.fay = (float)p.ay;
+  p.fca = (float)p.ca;
+  p.fcb = (float)p.cb;
+  p.fdt = (float)p.dt;
+  return p;
+}
 
 template <typename R, int N>
 struct MatLayout {
@@ -118,7 +131,9 @@ __global__ void __launch_bounds__(256) dg_rhs_kernel(const RhsParams p) {
   const R* qin = static_cast<const R*>(p.q_in);
   const double tnow = p.t_dev ? *p.t_dev + p.t : p.t;
   // scalar parameters converted once to the kernel type
-  const R cax = (R)p.ax, cay = (R)p.ay, cca = (R)p.ca, ccb = (R)p.cb, cdt = (R)p.dt;
+  constexpr bool f32 = sizeof(R) == 4;
+  const R cax = f32 ? (R)p.fax : (R)p.ax, cay = f32 ? (R)p.fay : (R)p.ay;
+  const R cca = f32 ? (R)p.fca : (R)p.ca, ccb = f32 ? (R)p.fcb : (R)p.cb, cdt = f32 ? (R)p.fdt : (R)p.dt;
 
   if (tid == 0) {
     mbar_init(bar, 1);

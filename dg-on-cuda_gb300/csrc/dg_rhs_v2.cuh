@@ -71,8 +71,8 @@ __global__ void __launch_bounds__(V2Config<N, P, G_, EPT_>::kThreads) dg_rhs_v2_
   const int ntiles = (p.K + TE - 1) / TE;
   const float* qin = static_cast<const float*>(p.q_in);
   const double tnow = p.t_dev ? *p.t_dev + p.t : p.t;
-  // scalar parameters converted once to FP32
-  const float cax = (float)p.ax, cay = (float)p.ay, cca = (float)p.ca, ccb = (float)p.cb, cdt = (float)p.dt;
+  // FP32 copies of the scalar parameters (rhs_dispatch<float>)
+  const float cax = p.fax, cay = p.fay, cca = p.fca, ccb = p.fcb, cdt = p.fdt;
 
   if (tid == 0) {
     mbar_init(&bar[0], 1);

@@ -30,7 +30,8 @@ struct dgc_handle_s {
   float* d_tau32 = nullptr;     // [K][4] laplace penalty, FP32
   void* d_mats64[2] = {nullptr, nullptr};  // weak, strong (transposed, padded)
   void* d_mats32[2] = {nullptr, nullptr};
-  void* d_tc_b = nullptr;     // FP32 tensor-core operand [Dr | Ds | LIFT] (weak form, split TF32)
+  void* d_tc_b = nullptr;     // FP32 tensor-core operand [Dr | Ds | LIFT] (strong form, split TF32)
+  void* d_blk_b = nullptr;    // FP32 operand of the register-blocked kernel (weak form, rows padded to NpP)
   int* d_status = nullptr;    // device-side error word
   double* d_time = nullptr;   // simulation time for graph-replayed steps
   dgk::LaunchInfo rhs_info;

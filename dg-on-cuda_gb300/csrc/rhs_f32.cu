@@ -4,32 +4,27 @@
 
 namespace dgk {
 
-// orders 1..6: variant v of rhs_f32_variant (rhs_launch.cuh); orders 7, 8:
-// dg_rhs_kernel
+// orders 1..6: variant v of rhs_f32_variant (rhs_launch.cuh), compiled per
+// order in rhs_f32_n<N>.cu; orders 7, 8: dg_rhs_kernel (v = 0) and the
+// register-blocked dg_rhs_blk_kernel (v = 1, 2), compiled here
 template <int N>
 static cudaError_t by_phys(int P, int v, const RhsParams& p, int sm, cudaStream_t s, LaunchInfo* info) {
+  const RhsParams* pp = info ? nullptr : &p;
   if constexpr (N <= 6) {
-    return rhs_v2_order<N>(P, v, info ? nullptr : &p, sm, s, info);
+    return rhs_v2_order<N>(P, v, pp, sm, s, info);
   } else {
-    if (info) {
-      switch (P) {
-        case PHYS_ADV: return rhs_configure<float, N, PHYS_ADV>(info);
-        case PHYS_TM: return rhs_configure<float, N, PHYS_TM>(info);
-        case PHYS_TE: return rhs_configure<float, N, PHYS_TE>(info);
-        default: return cudaErrorInvalidValue;
-      }
-    }
     switch (P) {
-      case PHYS_ADV: return rhs_launch<float, N, PHYS_ADV>(p, sm, s);
-      case PHYS_TM: return rhs_launch<float, N, PHYS_TM>(p, sm, s);
-      case PHYS_TE: return rhs_launch<float, N, PHYS_TE>(p, sm, s);
+      case PHYS_ADV: return rhs_f32_variant<N, PHYS_ADV>(v, pp, sm, s, info);
+      case PHYS_TM: return rhs_f32_variant<N, PHYS_TM>(v, pp, sm, s, info);
+      case PHYS_TE: return rhs_f32_variant<N, PHYS_TE>(v, pp, sm, s, info);
       default: return cudaErrorInvalidValue;
     }
   }
 }
 
 template <>
-cudaError_t rhs_dispatch<float>(int N, int P, int v, const RhsParams& p, int sm, cudaStream_t s, LaunchInfo* info) {
+cudaError_t rhs_dispatch<float>(int N, int P, int v, const RhsParams& p_in, int sm, cudaStream_t s, LaunchInfo* info) {
+  const RhsParams p = with_f32_scalars(p_in);
   switch (N) {
     case 1: return by_phys<1>(P, v, p, sm, s, info);
     case 2: return by_phys<2>(P, v, p, sm, s, info);
@@ -43,6 +38,8 @@ cudaError_t rhs_dispatch<float>(int N, int P, int v, const RhsParams& p, int sm,
   }
 }
 
-int rhs_num_variants(int prec_f32, int N) { return (prec_f32 && N <= 6) ? kF32Variants : 1; }
+int rhs_num_variants(int prec_f32, int N) {
+  return prec_f32 ? (N <= 6 ? kF32Variants : kF32VariantsHigh) : 1;
+}
 
 }  // namespace dgk

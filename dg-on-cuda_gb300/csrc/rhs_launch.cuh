@@ -55,6 +55,7 @@ int rhs_num_variants(int prec_f32, int N);
 
 }  // namespace dgk
 
+#include "dg_rhs_blk.cuh"
 #include "dg_rhs_tc.cuh"
 #include "dg_rhs_v2.cuh"
 
@@ -127,16 +128,57 @@ cudaError_t rhs_tc(const RhsParams* p, int sm_count, cudaStream_t s, LaunchInfo*
   return cudaGetLastError();
 }
 
+template <int N, int P, int EPT, int MAP>
+cudaError_t rhs_blk(const RhsParams* p, int sm_count, cudaStream_t s, LaunchInfo* info) {
+  using C = BlkConfig<N, P, EPT, MAP>;
+  static std::once_flag once;
+  static cudaError_t st = cudaSuccess;
+  static int bps = 0;
+  std::call_once(once, [] {
+    st = cudaFuncSetAttribute(dg_rhs_blk_kernel<N, P, EPT, MAP>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::kSmem);
+    if (st == cudaSuccess)
+      st = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, dg_rhs_blk_kernel<N, P, EPT, MAP>, C::kThreads,
+                                                         C::kSmem);
+  });
+  if (st != cudaSuccess) return st;
+  if (info) {
+    info->threads = C::kThreads;
+    info->tile = C::TE;
+    info->smem = C::kSmem;
+    info->blocks_per_sm = bps;
+    return cudaSuccess;
+  }
+  if (!p->mats_blk) return cudaErrorInvalidValue;
+  const int ntiles = (p->K + C::TE - 1) / C::TE;
+  int grid = sm_count * (bps > 0 ? bps : 1);
+  if (grid > ntiles) grid = ntiles;
+  dg_rhs_blk_kernel<N, P, EPT, MAP><<<grid, C::kThreads, C::kSmem, s>>>(*p);
+  return cudaGetLastError();
+}
+
 // FP32 variants at orders 1..6: 0 = one thread per element-node (dg_rhs_kernel),
-// 1..3 = register-blocked tile shapes (dg_rhs_v2_kernel), 4 = tensor cores
-// (dg_rhs_tc_kernel)
-constexpr int kF32Variants = 5;
+// 1..3 = register-blocked-by-node tile shapes (dg_rhs_v2_kernel), 4 = tensor
+// cores (dg_rhs_tc_kernel), 5, 6 = 4-node x 1 or 2 element blocks
+// (dg_rhs_blk_kernel, mapping 0), 7 = 4-node x 1 element blocks with
+// warp-uniform operator loads (mapping 1).  Orders 7, 8: 0 = dg_rhs_kernel,
+// 1, 2, 3 = dg_rhs_blk_kernel (EPT 1, EPT 2, mapping 1).
+constexpr int kF32Variants = 8;
+constexpr int kF32VariantsHigh = 4;
 
 template <int N, int P>
 cudaError_t rhs_f32_variant(int v, const RhsParams* p, int sm, cudaStream_t s, LaunchInfo* info) {
   if (v == 0) return info ? rhs_configure<float, N, P>(info) : rhs_launch<float, N, P>(*p, sm, s);
-  if (v >= 1 && v <= 3) return rhs_v2<N, P>(v - 1, p, sm, s, info);
-  if (v == 4) return rhs_tc<N, P>(p, sm, s, info);
+  if constexpr (N <= 6) {
+    if (v >= 1 && v <= 3) return rhs_v2<N, P>(v - 1, p, sm, s, info);
+    if (v == 4) return rhs_tc<N, P>(p, sm, s, info);
+    if (v == 5) return rhs_blk<N, P, 1, 0>(p, sm, s, info);
+    if (v == 6) return rhs_blk<N, P, 2, 0>(p, sm, s, info);
+    if (v == 7) return rhs_blk<N, P, 1, 1>(p, sm, s, info);
+  } else {
+    if (v == 1) return rhs_blk<N, P, 1, 0>(p, sm, s, info);
+    if (v == 2) return rhs_blk<N, P, 2, 0>(p, sm, s, info);
+    if (v == 3) return rhs_blk<N, P, 1, 1>(p, sm, s, info);
+  }
   return cudaErrorInvalidValue;
 }
 
