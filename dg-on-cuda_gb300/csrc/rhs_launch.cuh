@@ -3,6 +3,7 @@
 // fit on the GPU at once (occupancy x SM count), capped by the tile count.
 #pragma once
 
+#include <algorithm>
 #include <mutex>
 
 #include "dg_rhs.cuh"
@@ -57,6 +58,7 @@ int rhs_num_variants(int prec_f32, int N);
 
 #include "dg_rhs_blk.cuh"
 #include "dg_rhs_tc.cuh"
+#include "dg_rhs_tct.cuh"
 #include "dg_rhs_v2.cuh"
 
 namespace dgk {
@@ -128,6 +130,55 @@ cudaError_t rhs_tc(const RhsParams* p, int sm_count, cudaStream_t s, LaunchInfo*
   return cudaGetLastError();
 }
 
+template <int N, int P>
+cudaError_t rhs_tct(const RhsParams* p, int sm_count, cudaStream_t s, LaunchInfo* info) {
+  using C = TctConfig<N, P>;
+  static std::once_flag once;
+  static cudaError_t st = cudaSuccess;
+  static int bps = 0;
+  std::call_once(once, [] {
+    const void* fn = (const void*)dg_rhs_tct_kernel<N, P>;
+    st = cudaFuncSetAttribute(dg_rhs_tct_kernel<N, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, C::kSmemLaunch);
+    if (st == cudaSuccess)
+      st = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, dg_rhs_tct_kernel<N, P>, C::kThreads, C::kSmemLaunch);
+    // The occupancy query reports one CTA per SM for kernels that allocate
+    // tensor memory; the resident count is the smallest of the register,
+    // shared-memory, thread and TMEM-column limits (CTAs of this kernel never
+    // wait on each other, so an estimate above the true count only queues
+    // CTAs).
+    cudaFuncAttributes fa{};
+    int dev = 0, smem_sm = 0, resv = 0, regs_sm = 0, thr_sm = 0;
+    if (st == cudaSuccess) st = cudaFuncGetAttributes(&fa, fn);
+    if (st == cudaSuccess) st = cudaGetDevice(&dev);
+    if (st == cudaSuccess) st = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    if (st == cudaSuccess) st = cudaDeviceGetAttribute(&resv, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+    if (st == cudaSuccess) st = cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
+    if (st == cudaSuccess) st = cudaDeviceGetAttribute(&thr_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev);
+    if (st == cudaSuccess) {
+      const int regs_warp = (fa.numRegs * 32 + 255) / 256 * 256;
+      int n = regs_sm / (regs_warp * (C::kThreads / 32));
+      n = std::min(n, smem_sm / ((int)C::kSmemLaunch + (int)fa.sharedSizeBytes + resv));
+      n = std::min(n, thr_sm / C::kThreads);
+      n = std::min(n, 512 / (int)C::kTmemCols);
+      bps = std::max(bps, n);
+    }
+  });
+  if (st != cudaSuccess) return st;
+  if (info) {
+    info->threads = C::kThreads;
+    info->tile = C::TE;
+    info->smem = C::kSmemLaunch;
+    info->blocks_per_sm = bps;
+    return cudaSuccess;
+  }
+  if (!p->mats_tc) return cudaErrorInvalidValue;
+  const int ntiles = (p->K + C::TE - 1) / C::TE;
+  int grid = sm_count * (bps > 0 ? bps : 1);
+  if (grid > ntiles) grid = ntiles;
+  dg_rhs_tct_kernel<N, P><<<grid, C::kThreads, C::kSmemLaunch, s>>>(*p);
+  return cudaGetLastError();
+}
+
 template <int N, int P, int EPT, int MAP>
 cudaError_t rhs_blk(const RhsParams* p, int sm_count, cudaStream_t s, LaunchInfo* info) {
   using C = BlkConfig<N, P, EPT, MAP>;
@@ -160,9 +211,10 @@ cudaError_t rhs_blk(const RhsParams* p, int sm_count, cudaStream_t s, LaunchInfo
 // 1..3 = register-blocked-by-node tile shapes (dg_rhs_v2_kernel), 4 = tensor
 // cores (dg_rhs_tc_kernel), 5, 6 = 4-node x 1 or 2 element blocks
 // (dg_rhs_blk_kernel, mapping 0), 7 = 4-node x 1 element blocks with
-// warp-uniform operator loads (mapping 1).  Orders 7, 8: 0 = dg_rhs_kernel,
-// 1, 2, 3 = dg_rhs_blk_kernel (EPT 1, EPT 2, mapping 1).
-constexpr int kF32Variants = 8;
+// warp-uniform operator loads (mapping 1), 8 = tensor cores with the A operand
+// in TMEM (dg_rhs_tct_kernel).  Orders 7, 8: 0 = dg_rhs_kernel, 1, 2, 3 =
+// dg_rhs_blk_kernel (EPT 1, EPT 2, mapping 1).
+constexpr int kF32Variants = 9;
 constexpr int kF32VariantsHigh = 4;
 
 template <int N, int P>
@@ -174,6 +226,7 @@ cudaError_t rhs_f32_variant(int v, const RhsParams* p, int sm, cudaStream_t s, L
     if (v == 5) return rhs_blk<N, P, 1, 0>(p, sm, s, info);
     if (v == 6) return rhs_blk<N, P, 2, 0>(p, sm, s, info);
     if (v == 7) return rhs_blk<N, P, 1, 1>(p, sm, s, info);
+    if (v == 8) return rhs_tct<N, P>(p, sm, s, info);
   } else {
     if (v == 1) return rhs_blk<N, P, 1, 0>(p, sm, s, info);
     if (v == 2) return rhs_blk<N, P, 2, 0>(p, sm, s, info);
