@@ -51,6 +51,7 @@ STAGE_KERNELS = {
     6: "dgk::dg_rhs_blk_kernel<6,PHYS_TE,2>",
     7: "dgk::dg_rhs_blk_kernel<6,PHYS_TE,1> (warp-uniform operator loads)",
     8: "dgk::dg_rhs_tct_kernel<6,PHYS_TE> (tcgen05, A in TMEM, split TF32)",
+    9: "dgk::dg_rhs_tcp_kernel<6,PHYS_TE> (tcgen05, A in TMEM, warp-specialized pipeline)",
 }
 
 

@@ -379,7 +379,9 @@ __global__ void __launch_bounds__(256) dg_rhs_tc_kernel(const RhsParams p) {
         } else {
           float* q0 = static_cast<float*>(p.q0);
           const float co = cca, wa = ccb;
-          for (int j = 0; j < jn && j0 + j < Np; ++j) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {  // constant indices keep rhs[] in registers
+            if (j >= jn || j0 + j >= Np) continue;
             const size_t o = base + j;
             if (p.stage == 0) {
               aux[o] = rhs[j];

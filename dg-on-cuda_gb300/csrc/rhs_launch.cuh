@@ -59,6 +59,7 @@ int rhs_num_variants(int prec_f32, int N);
 #include "dg_rhs_blk.cuh"
 #include "dg_rhs_tc.cuh"
 #include "dg_rhs_tct.cuh"
+#include "dg_rhs_tcp.cuh"
 #include "dg_rhs_v2.cuh"
 
 namespace dgk {
@@ -179,6 +180,36 @@ cudaError_t rhs_tct(const RhsParams* p, int sm_count, cudaStream_t s, LaunchInfo
   return cudaGetLastError();
 }
 
+// warp-specialized pipelined tensor-memory kernel: one 512-thread CTA per SM
+// (it owns all 512 TMEM columns); advection runs the tct kernel instead
+template <int N, int P>
+cudaError_t rhs_tcp(const RhsParams* p, int sm_count, cudaStream_t s, LaunchInfo* info) {
+  if constexpr (P == PHYS_ADV) {
+    return rhs_tct<N, P>(p, sm_count, s, info);
+  } else {
+    using C = TcpConfig<N, P>;
+    static std::once_flag once;
+    static cudaError_t st = cudaSuccess;
+    std::call_once(once, [] {
+      st = cudaFuncSetAttribute(dg_rhs_tcp_kernel<N, P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                C::kSmemLaunch);
+    });
+    if (st != cudaSuccess) return st;
+    if (info) {
+      info->threads = C::kThreads;
+      info->tile = C::TE;
+      info->smem = C::kSmemLaunch;
+      info->blocks_per_sm = 1;
+      return cudaSuccess;
+    }
+    if (!p->mats_tc) return cudaErrorInvalidValue;
+    const int ntiles = (p->K + C::TE - 1) / C::TE;
+    const int grid = std::min(ntiles, sm_count);
+    dg_rhs_tcp_kernel<N, P><<<grid, C::kThreads, C::kSmemLaunch, s>>>(*p);
+    return cudaGetLastError();
+  }
+}
+
 template <int N, int P, int EPT, int MAP>
 cudaError_t rhs_blk(const RhsParams* p, int sm_count, cudaStream_t s, LaunchInfo* info) {
   using C = BlkConfig<N, P, EPT, MAP>;
@@ -212,9 +243,10 @@ cudaError_t rhs_blk(const RhsParams* p, int sm_count, cudaStream_t s, LaunchInfo
 // cores (dg_rhs_tc_kernel), 5, 6 = 4-node x 1 or 2 element blocks
 // (dg_rhs_blk_kernel, mapping 0), 7 = 4-node x 1 element blocks with
 // warp-uniform operator loads (mapping 1), 8 = tensor cores with the A operand
-// in TMEM (dg_rhs_tct_kernel).  Orders 7, 8: 0 = dg_rhs_kernel, 1, 2, 3 =
-// dg_rhs_blk_kernel (EPT 1, EPT 2, mapping 1).
-constexpr int kF32Variants = 9;
+// in TMEM (dg_rhs_tct_kernel), 9 = its warp-specialized pipelined form
+// (dg_rhs_tcp_kernel, Maxwell; advection runs variant 8).  Orders 7, 8: 0 =
+// dg_rhs_kernel, 1, 2, 3 = dg_rhs_blk_kernel (EPT 1, EPT 2, mapping 1).
+constexpr int kF32Variants = 10;
 constexpr int kF32VariantsHigh = 4;
 
 template <int N, int P>
@@ -227,6 +259,7 @@ cudaError_t rhs_f32_variant(int v, const RhsParams* p, int sm, cudaStream_t s, L
     if (v == 6) return rhs_blk<N, P, 2, 0>(p, sm, s, info);
     if (v == 7) return rhs_blk<N, P, 1, 1>(p, sm, s, info);
     if (v == 8) return rhs_tct<N, P>(p, sm, s, info);
+    if (v == 9) return rhs_tcp<N, P>(p, sm, s, info);
   } else {
     if (v == 1) return rhs_blk<N, P, 1, 0>(p, sm, s, info);
     if (v == 2) return rhs_blk<N, P, 2, 0>(p, sm, s, info);
