@@ -102,6 +102,40 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* s
   }
 }
 
+// mbar_wait for waits that are expected to be long (a warp-specialized
+// pipeline stage waiting for another stage): after a few polls the thread
+// sleeps between polls (32 ns doubling to 512 ns), so that waiting warps leave
+// their scheduler's issue slots to the warps doing the work.  Same one-second
+// limit and error record as mbar_wait.
+__device__ __forceinline__ bool mbar_wait_backoff(uint64_t* bar, uint32_t parity, int* status) {
+  const uint32_t a = smem_u32(bar);
+  uint64_t t0 = 0;
+  uint32_t ns = 32;
+  for (uint32_t it = 0;; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if (it == 4) t0 = globaltimer_ns();
+    if (it > 4) {
+      __nanosleep(ns);
+      if (ns < 512) ns <<= 1;
+      if ((it & 63) == 0 && globaltimer_ns() - t0 > 1000000000ull) {
+        if (status && atomicCAS(status, kErrNone, kErrBarrierTimeout) == kErrNone) {
+          unsigned long long* rec = reinterpret_cast<unsigned long long*>(status + 2);
+          rec[0] = globaltimer_ns() - t0;
+          rec[1] = 0;
+          rec[2] = it;
+        }
+        return false;
+      }
+    }
+  }
+}
+
 template <typename R>
 struct Vec16;
 template <>

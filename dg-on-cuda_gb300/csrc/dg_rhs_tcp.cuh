@@ -4,9 +4,13 @@
 // and tile layout (32 elements, field-major rows); the work of a tile is split
 // into stages run by different warps on different tiles at the same time:
 //
-//   CTRL  warp 15, lane 0   bulk loads (3 tile buffers), tcgen05.mma + commit
-//   FACE  warps 3, 7, 11    face tasks (element, face): gathers, flux jumps,
-//                           gamma rows in shared memory (2 buffers)
+//   MMA   warp 15, lane 0   tcgen05.mma + commit
+//   LOAD  warp 15, lane 1   bulk loads of the tiles (NB buffers), as far ahead
+//                           as the epilogue releases buffers
+//   FACE  warps 3, 7, 11    face tasks (element, face): the neighbour gathers
+//                           of tile i + 1 are issued before the flux jumps of
+//                           tile i are computed; gamma rows in shared memory
+//                           (2 buffers)
 //   BUILD warps 0-2, 4-6    alpha / beta / gamma columns of A -> TMEM (2 A buffers)
 //   EPI   warps 8-10, 12-14 D -> stage update and global stores (2 D buffers)
 //
@@ -17,14 +21,14 @@
 // CTA.  One CTA per SM: the 512 TMEM columns hold A x 2 and D x 2 (each D =
 // D_a | D_b of 2 NC + NC columns, two MMAs per K step as in dg_rhs_tct).
 //
-// Barrier phases (tile i of the CTA, buffers s = i % 3, g = i % 2):
-//   dfull[s]  bulk copy of tile i landed            -> FACE, BUILD, EPI
+// Barrier phases (tile i of the CTA, buffers s = i % NB, g = i % 2):
+//   dfull[s]  bulk copy of tile i landed            -> FACE (from tile i - 1), BUILD, EPI
 //   gfull[g]  gamma rows of tile i written          -> BUILD
 //   gempty[g] gamma rows of tile i consumed         -> FACE (tile i + 2)
 //   afull[g]  A of tile i complete in TMEM          -> CTRL
 //   mdone[g]  MMA of tile i complete (commit)       -> EPI, BUILD (tile i + 2)
 //   dempty[g] D of tile i read                      -> CTRL (tile i + 2)
-//   dfree[s]  tile buffer of tile i released        -> CTRL (load of tile i + 3)
+//   dfree[s]  tile buffer of tile i released        -> LOAD (tile i + NB)
 // No waiter can fall a whole phase behind: each next completion depends on
 // the waiter's own later progress.
 #pragma once
@@ -44,12 +48,16 @@ struct TcpConfig {
   static constexpr uint32_t kBBytes = T::kBBytes;
   static constexpr uint32_t kQ = T::kQ, kG = T::kG, kN = T::kN, kBuf = T::kBuf;
   static constexpr uint32_t kGam = T::kGam;  // column-major [GC][ROWS]
-  // shared memory: 16 mbarriers + TMEM address | B hi, lo | gamma x 2 | tiles x 3
+  // tile buffers: a buffer stays in use from its load through the face,
+  // build, MMA and epilogue stages, so the ring depth bounds the tile period
+  static constexpr int NB = 4;
+  static_assert(NB <= 8, "barrier slots");
+  // shared memory: 27 mbarriers + TMEM address | B hi, lo | gamma x 2 | tiles x NB
   static constexpr uint32_t oBar = 0;
   static constexpr uint32_t oB = 256;
   static constexpr uint32_t oGam = oB + 2 * kBBytes;
   static constexpr uint32_t oBuf = oGam + 2 * kGam;
-  static constexpr uint32_t kSmem = oBuf + 3 * kBuf;
+  static constexpr uint32_t kSmem = oBuf + NB * kBuf;
   // requested at launch: more than half an SM's 233472 B, so a second CTA
   // (whose 512-column TMEM allocation would have to wait) is never co-resident
   static constexpr uint32_t kSmemLaunch = kSmem > 116800u ? kSmem : 116800u;
@@ -59,13 +67,13 @@ struct TcpConfig {
 };
 
 // mbarrier slots
-enum : int { TB_DFULL = 0, TB_GFULL = 3, TB_GEMPTY = 5, TB_AFULL = 7, TB_MDONE = 9, TB_DEMPTY = 11,
-             TB_DFREE = 13, TB_BFULL = 16, TB_COUNT = 17 };
+enum : int { TB_DFULL = 0, TB_GFULL = 8, TB_GEMPTY = 10, TB_AFULL = 12, TB_MDONE = 14, TB_DEMPTY = 16,
+             TB_DFREE = 18, TB_BFULL = 26, TB_COUNT = 27 };  // tile-buffer slots sized for up to 8 buffers
 
 template <int N, int P>
 __global__ void __launch_bounds__(512, 1) dg_rhs_tcp_kernel(const RhsParams p) {
   using C = TcpConfig<N, P>;
-  constexpr int Np = C::Np, NpP = C::NpP, TE = C::TE, ESTR = C::ESTR;
+  constexpr int Np = C::Np, NpP = C::NpP, TE = C::TE, ESTR = C::ESTR, NB = C::NB;
   constexpr int KP = C::KP, KG = C::KG, GC = C::GC, NC = C::NC, SBO = C::SBO, ROWS = C::ROWS;
 
   extern __shared__ __align__(128) unsigned char smem[];
@@ -89,7 +97,7 @@ __global__ void __launch_bounds__(512, 1) dg_rhs_tcp_kernel(const RhsParams p) {
   const bool aux_tile = p.mode == MODE_LSERK;
 
   if (tid == 0) {
-    for (int s = 0; s < 3; ++s) {
+    for (int s = 0; s < NB; ++s) {
       mbar_init(&bar[TB_DFULL + s], 1);
       mbar_init(&bar[TB_DFREE + s], 192);
     }
@@ -116,15 +124,16 @@ __global__ void __launch_bounds__(512, 1) dg_rhs_tcp_kernel(const RhsParams p) {
 
   bool ok = true;  // this thread's waits have all completed (a wait that expires turns it off)
   auto wait = [&](int slot, uint32_t parity) {
-    if (ok) ok = mbar_wait(&bar[slot], parity, p.status);
+    if (ok) ok = mbar_wait_backoff(&bar[slot], parity, p.status);
   };
   auto tile_of = [&](int i) { return (int)blockIdx.x + i * (int)gridDim.x; };
 
   if (warp == 15) {
-    // ================================================================ CTRL
-    if (lane == 0) {
-      auto load = [&](int i) {
-        const int s = i % 3, k0 = tile_of(i) * TE, ne = min(TE, p.K - k0);
+    if (lane == 1) {
+      // ============================================================== LOAD
+      for (int i = 0; i < nt; ++i) {
+        const int s = i % NB, k0 = tile_of(i) * TE, ne = min(TE, p.K - k0);
+        if (i >= NB) wait(TB_DFREE + s, ((i - NB) / NB) & 1);  // epilogue of tile i - NB done
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         const uint32_t bq = ne * ESTR * 4, bg = ne * 16 * 4, bn = ne * 16;
         mbar_arrive_expect_tx(&bar[TB_DFULL + s], bq + (aux_tile ? bq : 0) + bg + bn);
@@ -132,10 +141,11 @@ __global__ void __launch_bounds__(512, 1) dg_rhs_tcp_kernel(const RhsParams p) {
         if (aux_tile) bulk_g2s(bufR(s), static_cast<const float*>(p.aux) + (size_t)k0 * ESTR, bq, &bar[TB_DFULL + s]);
         bulk_g2s(bufG(s), static_cast<const float*>(p.geom) + (size_t)k0 * 16, bg, &bar[TB_DFULL + s]);
         bulk_g2s(bufN(s), p.nbr + k0, bn, &bar[TB_DFULL + s]);
-      };
+      }
+    } else if (lane == 0) {
+      // ============================================================== MMA
       mbar_arrive_expect_tx(&bar[TB_BFULL], 2 * C::kBBytes);
       bulk_g2s(Bhi, p.mats_tc, 2 * C::kBBytes, &bar[TB_BFULL]);
-      for (int i = 0; i < 2 && i < nt; ++i) load(i);
       wait(TB_BFULL, 0);
       const uint32_t bH = smem_u32(Bhi);  // B_hi, with B_lo directly after it
       for (int i = 0; i < nt; ++i) {
@@ -152,11 +162,6 @@ __global__ void __launch_bounds__(512, 1) dg_rhs_tcp_kernel(const RhsParams p) {
           tc_mma_tf32_ta(tD + 2 * NC, tAl + (uint32_t)(8 * s2), dB, C::kIdesc, acc);
         }
         tc_commit(&bar[TB_MDONE + g]);
-        // refill: tile i + 2 goes to the buffer tile i - 1 used
-        if (i + 2 < nt) {
-          if (i >= 1) wait(TB_DFREE + (i - 1) % 3, ((i - 1) / 3) & 1);
-          load(i + 2);
-        }
       }
       // the last MMA completes before TMEM is released
       if (nt > 0) wait(TB_MDONE + ((nt - 1) & 1), ((nt - 1) >> 1) & 1);
@@ -165,12 +170,29 @@ __global__ void __launch_bounds__(512, 1) dg_rhs_tcp_kernel(const RhsParams p) {
     // ================================================================ FACE
     const int fid = (warp >> 2) * 32 + lane;  // 0..95: (face, element) task of each tile
     const int f = fid / TE, e = fid - f * TE;
-    for (int i = 0; i < nt; ++i) {
-      const int s = i % 3, g = i & 1, k0 = tile_of(i) * TE, ne = min(TE, p.K - k0);
-      wait(TB_DFULL + s, (i / 3) & 1);
+    constexpr int Nfp = C::Nfp;
+    float bc[Nfp][3], bx[Nfp][3];  // neighbour traces of the current / next tile
+    int nbc = -1, nbx = -1;
+    auto gather = [&](int i, float (&b)[Nfp][3], int& nb) {
+      const int s = i % NB, k0 = tile_of(i) * TE, ne = min(TE, p.K - k0);
+      wait(TB_DFULL + s, (i / NB) & 1);
+      nb = -1;
+      if (e < ne) nb = face_gather<N, P>(p, e, f, k0, ne, bufQ(s), bufN(s), qin, b);
+    };
+    // one step: issue the gathers of tile i + 1 into `nxt`, then compute tile
+    // i from `cur` (gathered one step earlier); unrolled by two so that the
+    // buffers swap roles without a register copy that would wait for the loads
+    auto step = [&](int i, float (&cur)[Nfp][3], int nbcur, float (&nxt)[Nfp][3], int& nbnxt) {
+      const int s = i % NB, g = i & 1, k0 = tile_of(i) * TE, ne = min(TE, p.K - k0);
+      if (i + 1 < nt) gather(i + 1, nxt, nbnxt);
       if (i >= 2) wait(TB_GEMPTY + g, ((i - 2) >> 1) & 1);
-      if (e < ne) tct_face_task<N, P>(p, e, f, k0, ne, bufQ(s), bufG(s), bufN(s), qin, gam(g), cax, cay);
+      if (e < ne) face_flux<N, P>(e, f, nbcur, bufQ(s), bufG(s), cur, gam(g), cax, cay);
       mbar_arrive(&bar[TB_GFULL + g]);
+    };
+    if (nt > 0) gather(0, bc, nbc);
+    for (int i = 0; i < nt; i += 2) {
+      step(i, bc, nbc, bx, nbx);
+      if (i + 1 < nt) step(i + 1, bx, nbx, bc, nbc);
     }
   } else if (warp < 8) {
     // ================================================================ BUILD
@@ -179,8 +201,8 @@ __global__ void __launch_bounds__(512, 1) dg_rhs_tcp_kernel(const RhsParams p) {
     // zero both A buffers of this warp's lanes once (padding never rewritten)
     for (int c = 4 * half; c < 4 * KP; c += 8) tmem_st4(tRow + c, 0.0f, 0.0f, 0.0f, 0.0f);
     for (int i = 0; i < nt; ++i) {
-      const int s = i % 3, g = i & 1, k0 = tile_of(i) * TE, ne = min(TE, p.K - k0);
-      wait(TB_DFULL + s, (i / 3) & 1);
+      const int s = i % NB, g = i & 1, k0 = tile_of(i) * TE, ne = min(TE, p.K - k0);
+      wait(TB_DFULL + s, (i / NB) & 1);
       if (i >= 2) wait(TB_MDONE + g, ((i - 2) >> 1) & 1);  // MMA of tile i - 2 no longer reads A[g]
       tc_fence_after();
       __syncwarp();  // tcgen05.st below is warp-collective
@@ -236,8 +258,8 @@ __global__ void __launch_bounds__(512, 1) dg_rhs_tcp_kernel(const RhsParams p) {
     float* out = static_cast<float*>(p.out);
     float* aux = static_cast<float*>(p.aux);
     for (int i = 0; i < nt; ++i) {
-      const int s = i % 3, g = i & 1, k0 = tile_of(i) * TE, ne = min(TE, p.K - k0);
-      wait(TB_DFULL + s, (i / 3) & 1);
+      const int s = i % NB, g = i & 1, k0 = tile_of(i) * TE, ne = min(TE, p.K - k0);
+      wait(TB_DFULL + s, (i / NB) & 1);
       wait(TB_MDONE + g, (i >> 1) & 1);
       tc_fence_after();
       __syncwarp();  // tcgen05.ld below is warp-collective

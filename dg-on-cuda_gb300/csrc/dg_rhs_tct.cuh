@@ -104,27 +104,25 @@ struct TctConfig {
   static_assert(ROWS <= 128 && TE % 32 == 0, "one field per lane quadrant");
 };
 
-// One face task: the Nfp nodes of face f of tile element e.  Gathers the own
-// and neighbour traces, forms the jump of the upwind flux against the own
-// flux, gamma = -(faceJ / J) (f* - n.F(q-)), and writes it to the element's
-// gamma rows (field-major) of the column-major gamma buffer.
+// Face tasks: the Nfp nodes of face f of tile element e, in two steps so that
+// a caller can issue the gathers of one tile before computing the fluxes of
+// another.
+//   face_gather: neighbour traces of an interior face (tile element: shared
+//     memory, other elements: global memory) or the prescribed boundary values
+//     (advection); returns the neighbour code (kn << 2 | fn, or < 0 on the
+//     boundary).
+//   face_flux: own traces, PEC reflection on boundary faces (Maxwell), the jump
+//     of the upwind flux against the own flux, gamma = -(faceJ / J)
+//     (f* - n.F(q-)), written to the element's gamma rows (field-major) of the
+//     column-major gamma buffer.
 template <int N, int P>
-__device__ __forceinline__ void tct_face_task(const RhsParams& p, int e, int f, int k0, int ne, const float* sQ,
-                                              const float* sG, const int4* sN, const float* qin, float* sGam,
-                                              float cax, float cay) {
+__device__ __forceinline__ int face_gather(const RhsParams& p, int e, int f, int k0, int ne, const float* sQ,
+                                           const int4* sN, const float* qin,
+                                           float (&b)[Order<N>::Nfp][PhysTraits<P>::Nf]) {
   using C = TctConfig<N, P>;
-  constexpr int Nfp = C::Nfp, NpP = C::NpP, NF = C::Nf, ESTR = C::ESTR, ROWS = C::ROWS, TE = C::TE;
+  constexpr int Nfp = C::Nfp, NpP = C::NpP, NF = C::Nf, ESTR = C::ESTR;
   const int4 n4 = sN[e];
   const int nb = f == 0 ? n4.x : (f == 1 ? n4.y : n4.z);
-  const float* g = sG + e * 16;
-  const float nx = g[8 + f], ny = g[11 + f];
-  const float sc = g[5 + f] * g[4];  // -faceJ / J
-  const float* qe = sQ + e * ESTR;
-  float a[Nfp][NF], b[Nfp][NF];
-#pragma unroll
-  for (int d = 0; d < Nfp; ++d)
-#pragma unroll
-    for (int c = 0; c < NF; ++c) a[d][c] = qe[c * NpP + fmask<N>(f, d)];
   if (nb >= 0) {
     const int kn = nb >> 2, fn = nb & 3;
     if (kn >= k0 && kn < k0 + ne) {
@@ -148,7 +146,26 @@ __device__ __forceinline__ void tct_face_task(const RhsParams& p, int e, int f, 
       const double xx = p.bxy[((size_t)bf * Nfp + d) * 2], yy = p.bxy[((size_t)bf * Nfp + d) * 2 + 1];
       b[d][0] = (float)adv_exact(p, tnow, xx, yy);
     }
-  } else {
+  }
+  return nb;
+}
+
+template <int N, int P>
+__device__ __forceinline__ void face_flux(int e, int f, int nb, const float* sQ, const float* sG,
+                                          float (&b)[Order<N>::Nfp][PhysTraits<P>::Nf], float* sGam, float cax,
+                                          float cay) {
+  using C = TctConfig<N, P>;
+  constexpr int Nfp = C::Nfp, NpP = C::NpP, NF = C::Nf, ESTR = C::ESTR, ROWS = C::ROWS, TE = C::TE;
+  const float* g = sG + e * 16;
+  const float nx = g[8 + f], ny = g[11 + f];
+  const float sc = g[5 + f] * g[4];  // -faceJ / J
+  const float* qe = sQ + e * ESTR;
+  float a[Nfp][NF];
+#pragma unroll
+  for (int d = 0; d < Nfp; ++d)
+#pragma unroll
+    for (int c = 0; c < NF; ++c) a[d][c] = qe[c * NpP + fmask<N>(f, d)];
+  if (nb < 0 && P != PHYS_ADV) {
 #pragma unroll
     for (int d = 0; d < Nfp; ++d) {
       if (P == PHYS_TM) {  // PEC: H+ = H-, Ez+ = -Ez-
@@ -180,6 +197,15 @@ __device__ __forceinline__ void tct_face_task(const RhsParams& p, int e, int f, 
 #pragma unroll
     for (int c = 0; c < NF; ++c) sGam[(f * Nfp + d) * ROWS + c * TE + e] = dl[c] * sc;
   }
+}
+
+template <int N, int P>
+__device__ __forceinline__ void tct_face_task(const RhsParams& p, int e, int f, int k0, int ne, const float* sQ,
+                                              const float* sG, const int4* sN, const float* qin, float* sGam,
+                                              float cax, float cay) {
+  float b[Order<N>::Nfp][PhysTraits<P>::Nf];
+  const int nb = face_gather<N, P>(p, e, f, k0, ne, sQ, sN, qin, b);
+  face_flux<N, P>(e, f, nb, sQ, sG, b, sGam, cax, cay);
 }
 
 template <int N, int P>
