@@ -185,6 +185,144 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
+POISSON_NSIDE, POISSON_ORDER, POISSON_SEED = 256, 4, 4242
+
+
+def fourier_rhs(x, y, seed: int, modes: int = 32):
+    """Sum of `modes` sine modes sin(kx pi (x+1)/2) sin(ky pi (y+1)/2), kx, ky in
+    1..8 drawn from `seed`, amplitudes ~ N(0, |k|^-3) (zero on the boundary)."""
+    rng = np.random.default_rng(seed)
+    f = np.zeros_like(x)
+    for _ in range(modes):
+        kx, ky = rng.integers(1, 9, size=2)
+        a = rng.normal(0.0, (kx * kx + ky * ky) ** -0.75)
+        f += a * np.sin(kx * np.pi * (x + 1) / 2) * np.sin(ky * np.pi * (y + 1) / 2)
+    return f
+
+
+def measure_poisson(dg, meshes):
+    """IPDG Poisson -lap u = f, Dirichlet u = 0, jittered 256x256 mesh (K = 131072),
+    N = 4, tau = (N+1)^2 / h: FP64 block-Jacobi PCG against FP32 inner PCG in
+    FP64 iterative refinement, both to 1e-10 relative FP64 residual, for the
+    manufactured solution sin(pi x) sin(pi y) and a 32-mode Fourier right-hand side."""
+    import torch
+    m = meshes.jittered_square(POISSON_NSIDE, POISSON_SEED)
+    D = dg.Discretization(m, "laplace", POISSON_ORDER, dg.F64, tau=dg.TAU_SCALED, dirichlet=True)
+    x, y = D.node_xy()
+    D.block_jacobi()
+    out = {"workload": f"ipdg_poisson_dirichlet_k{D.K}_n{POISSON_ORDER}", "num_cells": D.K,
+           "order": POISSON_ORDER, "rtol": 1e-10, "cases": {}}
+    cases = {"manufactured": 2 * np.pi ** 2 * np.sin(np.pi * x) * np.sin(np.pi * y),
+             "fourier32": fourier_rhs(x, y, POISSON_SEED)}
+    for name, f in cases.items():
+        b = D.mass(D.upload(f.reshape(-1)))
+        res = {}
+        sols = {}
+        for mode, tag in ((dg.SOLVE_FP64_PCG, "fp64_pcg"), (dg.SOLVE_MIXED_IR, "mixed_ir")):
+            D.pcg(b, mode=mode, rtol=1e-10, maxit=40000, check=False)  # warm-up (graphs, preconditioner)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            xs, st = D.pcg(b, mode=mode, rtol=1e-10, maxit=40000, check=False)
+            torch.cuda.synchronize()
+            st["wall_s"] = time.perf_counter() - t0
+            sols[tag] = D.download(xs).reshape(-1)
+            res[tag] = {k: st[k] for k in ("iterations", "outer_iterations", "converged", "final_relres", "wall_s")}
+        ref = sols["fp64_pcg"]
+        res["rel_l2_mixed_vs_fp64"] = float(np.linalg.norm(sols["mixed_ir"] - ref) / np.linalg.norm(ref))
+        if name == "manufactured":
+            ex = (np.sin(np.pi * x) * np.sin(np.pi * y)).reshape(-1)
+            for tag in sols:
+                res[tag]["rel_l2_vs_exact"] = float(np.linalg.norm(sols[tag] - ex) / np.linalg.norm(ex))
+        res["speedup_mixed_vs_fp64"] = res["fp64_pcg"]["wall_s"] / res["mixed_ir"]["wall_s"]
+        out["cases"][name] = res
+    D.check()
+    return out
+
+
+BATCH_INSTANCES, BATCH_SEED, BATCH_STEPS = 96, 777, 10
+
+
+def measure_batched(dg, meshes):
+    """96 independent FP32 instances (advection with a random velocity direction
+    and Gaussian pulse, or a Maxwell TE / TM cavity mode) on jittered meshes with
+    n log-uniform in [8, 160] squares per side and N uniform in {2..8}: aggregate
+    GDOF/s of the batched persistent launches (one launch per LSERK4 stage for
+    all instances, the step replayed from a CUDA graph) against the same steps
+    as per-instance sequential launches of the same tile code."""
+    import torch
+    rng = np.random.default_rng(BATCH_SEED)
+    insts = []
+    for i in range(BATCH_INSTANCES):
+        n = int(round(np.exp(rng.uniform(np.log(8), np.log(160)))))
+        N = int(rng.integers(2, 9))
+        kind = ["advection", "maxwell_te", "maxwell_tm"][int(rng.integers(0, 3))]
+        m = meshes.jittered_square(n, BATCH_SEED + i)
+        if kind == "advection":
+            th = rng.uniform(0, 2 * np.pi)
+            ax, ay = float(np.cos(th)), float(np.sin(th))
+            D = dg.Discretization(m, kind, N, dg.F32, ax=ax, ay=ay, bc=dg.BC_GAUSS,
+                                  gx0=float(rng.uniform(-0.5, 0.5)), gy0=float(rng.uniform(-0.5, 0.5)), gw=0.02)
+            x, y = D.node_xy()
+            q = np.exp(-((x - D.desc.gx0) ** 2 + (y - D.desc.gy0) ** 2) / 0.02)[None]
+        else:
+            D = dg.Discretization(m, kind, N, dg.F32)
+            x, y = D.node_xy()
+            q = np.zeros((3,) + x.shape)
+            # TE: Hz = cos cos; TM: Ez = sin sin (both PEC cavity modes)
+            q[2] = (np.cos(np.pi * x) * np.cos(np.pi * y) if kind == "maxwell_te"
+                    else np.sin(np.pi * x) * np.sin(np.pi * y))
+        D.set_variant(0)
+        insts.append((D, q.reshape(-1), 0.5 * D.info.min_edge / (N + 1) ** 2))
+    dofs = sum(D.Nf * D.Np * D.K for D, _, _ in insts)
+    B = dg.Batch([D for D, _, _ in insts])
+    dts = [dt for *_, dt in insts]
+    qa = [D.upload(q) for D, q, _ in insts]
+    qb = [D.empty_state() for D, *_ in insts]
+    rs = [D.empty_state() for D, *_ in insts]
+    B.lserk4_run(qa, qb, rs, [0.0] * len(insts), dts, 4, graph=True)  # warm-up (even: back in qa)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l0 = B.launch_count()
+    ev0.record()
+    fin = B.lserk4_run(qa, qb, rs, [0.0] * len(insts), dts, BATCH_STEPS, graph=True)
+    ev1.record()
+    torch.cuda.synchronize()
+    batched_ms = ev0.elapsed_time(ev1)
+    batch_launches = B.launch_count() - l0
+    # sequential: the same steps, instance after instance, 5 launches per step each
+    sa = [D.upload(q) for D, q, _ in insts]
+    sb = [D.empty_state() for D, *_ in insts]
+    sr = [D.empty_state() for D, *_ in insts]
+    for (D, *_), a, b, r, dt in zip(insts, sa, sb, sr, dts):
+        for s in range(4):
+            D.lserk4_step(a if s % 2 == 0 else b, b if s % 2 == 0 else a, r, s * dt, dt)
+    torch.cuda.synchronize()
+    ev0.record()
+    for (D, *_), a, b, r, dt in zip(insts, sa, sb, sr, dts):
+        x, y = a, b
+        for s in range(BATCH_STEPS):
+            D.lserk4_step(x, y, r, s * dt, dt)
+            x, y = y, x
+    ev1.record()
+    torch.cuda.synchronize()
+    seq_ms = ev0.elapsed_time(ev1)
+    seq_fin = sb if BATCH_STEPS % 2 else sa
+    diff = max(float((f - g).abs().max()) / max(float(g.abs().max()), 1e-30) for f, g in zip(fin, seq_fin))
+    B.close()
+    for D, *_ in insts:
+        D.check()
+    Ks = [D.K for D, *_ in insts]
+    return {"workload": f"batched_{len(insts)}_instances", "instances": len(insts),
+            "dofs_total": dofs, "K_range": [min(Ks), max(Ks)],
+            "orders": sorted({D.N for D, *_ in insts}), "steps": BATCH_STEPS,
+            "batched": {"gdofs": dofs * 5 * BATCH_STEPS / (batched_ms * 1e-3) / 1e9, "ms": batched_ms,
+                        "launches_per_step": batch_launches / BATCH_STEPS, "graph": True},
+            "sequential": {"gdofs": dofs * 5 * BATCH_STEPS / (seq_ms * 1e-3) / 1e9, "ms": seq_ms,
+                           "launches_per_step": 5 * len(insts)},
+            "speedup_batched_vs_sequential": seq_ms / batched_ms,
+            "max_rel_diff_batched_vs_sequential": diff}
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -290,6 +428,8 @@ def main():
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 plain-path timing")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end (host buffer) timing")
     ap.add_argument("--variant", type=int, default=-1, help="force an RHS kernel variant instead of autotuning")
+    ap.add_argument("--no-poisson", action="store_true", help="skip the IPDG Poisson solver comparison")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched-instances comparison")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -391,6 +531,12 @@ def main():
     accuracy = None
     if rank == 0 and D64 is not None and not args.no_accuracy:
         accuracy = measure_accuracy(dg, D32, D64, q_init, x, y, dt)
+    poisson = None
+    if rank == 0 and not args.no_poisson:
+        poisson = measure_poisson(dg, meshes)
+    batched = None
+    if rank == 0 and not args.no_batched:
+        batched = measure_batched(dg, meshes)
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         csteps = 10
@@ -406,7 +552,7 @@ def main():
                 "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu,
                 "clocks": clocks, "fp64_plain": fp64,
                 "speedup_mixed_vs_fp64": (value / ws / fp64["value"]) if fp64 else None,
-                "accuracy": accuracy, "wall_s_timed_region": wall}
+                "accuracy": accuracy, "poisson": poisson, "batched": batched, "wall_s_timed_region": wall}
         print(json.dumps(line))
     if ws > 1:
         import torch.distributed as tdist

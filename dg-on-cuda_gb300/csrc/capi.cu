@@ -435,6 +435,11 @@ int check_time_dependent(dgc_handle h) {
 
 }  // namespace
 
+namespace dgc {
+dgk::RhsParams rhs_base_params(dgc_handle_s* h) { return base_params(h); }
+const double* lserk_coeffs(int which) { return which == 0 ? kRkA : (which == 1 ? kRkB : kRkC); }
+}  // namespace dgc
+
 extern "C" int dgc_rhs(dgc_handle h, const void* q, double t, void* out, void* stream) {
   if (!h || !q || !out) return fail(DGC_ERR_ARG, "null argument");
   if (int rc = check_time_dependent(h)) return rc;

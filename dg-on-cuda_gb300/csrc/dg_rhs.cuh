@@ -108,189 +108,223 @@ __device__ __forceinline__ double adv_exact(const RhsParams& p, double t, double
   return 0.0;
 }
 
+// Shared-memory view of the tile layout of dg_rhs_kernel (RhsConfig).
 template <typename R, int N, int P>
-__global__ void __launch_bounds__(256) dg_rhs_kernel(const RhsParams p) {
+struct V1Smem {
+  using C = RhsConfig<R, N, P>;
+  uint64_t* bar;
+  R *sDrT, *sDsT, *sLT, *sQ, *sG, *sF;
+  int4* sN;
+  __device__ explicit V1Smem(unsigned char* smem) {
+    constexpr int kD = MatLayout<R, N>::kD;
+    bar = reinterpret_cast<uint64_t*>(smem + C::oBar);
+    sDrT = reinterpret_cast<R*>(smem + C::oMats);
+    sDsT = sDrT + kD;
+    sLT = sDrT + 2 * kD;
+    sQ = reinterpret_cast<R*>(smem + C::oQ);
+    sG = reinterpret_cast<R*>(smem + C::oGeom);
+    sN = reinterpret_cast<int4*>(smem + C::oNbr);
+    sF = reinterpret_cast<R*>(smem + C::oFlux);
+  }
+};
+
+// Bulk-copy the operator matrices of p into shared memory.  Every thread has
+// observed the completed phase before the function returns (the caller
+// re-arms the same barrier next); false if the wait expired.
+template <typename R, int N, int P>
+__device__ __forceinline__ bool rhs_v1_load_mats(const RhsParams& p, const V1Smem<R, N, P>& s, uint32_t& phase) {
+  if (threadIdx.x == 0) {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    mbar_arrive_expect_tx(s.bar, MatLayout<R, N>::kBytes);
+    bulk_g2s(s.sDrT, p.mats, MatLayout<R, N>::kBytes, s.bar);
+  }
+  // All threads must have observed this phase before thread 0 re-arms the
+  // barrier for a tile: otherwise a fast tile copy can complete the next
+  // phase before a slow warp polls this one, and that warp would then wait
+  // for a phase that never comes.  The AND also makes a timed-out wait exit
+  // the whole CTA.
+  const bool ok = __syncthreads_and(mbar_wait(s.bar, phase, p.status));
+  phase ^= 1;
+  return ok;
+}
+
+// One tile of the stage: the ne (<= TE) elements from k0 -- bulk load of
+// state / geometry / neighbours, numerical fluxes on the face nodes, volume
+// and lift contractions (one thread per element-node), stage epilogue.
+// Ends with a CTA barrier; false if a wait expired.
+template <typename R, int N, int P>
+__device__ __forceinline__ bool rhs_v1_tile(const RhsParams& p, const V1Smem<R, N, P>& s, uint32_t& phase, int k0,
+                                            int ne) {
   using O = Order<N>;
   using C = RhsConfig<R, N, P>;
   constexpr int Np = O::Np, Nfp = O::Nfp, NpP = O::NpP, NFACE = O::Nface;
-  constexpr int TE = C::TE, NF = C::Nf, ESTR = C::ESTR;
-  constexpr int kD = MatLayout<R, N>::kD;
-
-  extern __shared__ __align__(128) unsigned char smem[];
-  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + C::oBar);
-  R* sDrT = reinterpret_cast<R*>(smem + C::oMats);
-  R* sDsT = sDrT + kD;
-  R* sLT = sDrT + 2 * kD;
-  R* sQ = reinterpret_cast<R*>(smem + C::oQ);
-  R* sG = reinterpret_cast<R*>(smem + C::oGeom);
-  int4* sN = reinterpret_cast<int4*>(smem + C::oNbr);
-  R* sF = reinterpret_cast<R*>(smem + C::oFlux);
-
+  constexpr int NF = C::Nf, ESTR = C::ESTR;
   const int tid = threadIdx.x;
-  const int ntiles = (p.K + TE - 1) / TE;
   const R* qin = static_cast<const R*>(p.q_in);
-  const double tnow = p.t_dev ? *p.t_dev + p.t : p.t;
-  // scalar parameters converted once to the kernel type
+  // scalar parameters in the kernel type
   constexpr bool f32 = sizeof(R) == 4;
   const R cax = f32 ? (R)p.fax : (R)p.ax, cay = f32 ? (R)p.fay : (R)p.ay;
   const R cca = f32 ? (R)p.fca : (R)p.ca, ccb = f32 ? (R)p.fcb : (R)p.cb, cdt = f32 ? (R)p.fdt : (R)p.dt;
-
+  R* sQ = s.sQ;
+  R* sG = s.sG;
+  int4* sN = s.sN;
+  R* sF = s.sF;
+  const R* sDrT = s.sDrT;
+  const R* sDsT = s.sDsT;
+  const R* sLT = s.sLT;
   if (tid == 0) {
-    mbar_init(bar, 1);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    const uint32_t bq = ne * ESTR * sizeof(R), bg = ne * 16 * sizeof(R), bn = ne * 16;
+    mbar_arrive_expect_tx(s.bar, bq + bg + bn);
+    bulk_g2s(sQ, qin + (size_t)k0 * ESTR, bq, s.bar);
+    bulk_g2s(sG, static_cast<const R*>(p.geom) + (size_t)k0 * 16, bg, s.bar);
+    bulk_g2s(sN, p.nbr + k0, bn, s.bar);
+  }
+  if (!__syncthreads_and(mbar_wait(s.bar, phase, p.status))) return false;
+  phase ^= 1;
+  // ---- numerical fluxes on the tile's face nodes, scaled by faceJ
+  for (int it = tid; it < ne * NFACE; it += blockDim.x) {
+    const int e = it / NFACE, fm = it - e * NFACE, f = fm / Nfp, d = fm - f * Nfp;
+    const R* g = sG + e * 16;
+    const int nb = f == 0 ? sN[e].x : (f == 1 ? sN[e].y : sN[e].z);
+    const int nd = fmask<N>(f, d);
+    const R* qa = sQ + e * ESTR;
+    const R nx = (R)g[8 + f], ny = (R)g[11 + f], fJ = (R)g[5 + f];
+    R a[NF], b[NF];
+#pragma unroll
+    for (int c = 0; c < NF; ++c) a[c] = qa[c * NpP + nd];
+    if (nb >= 0) {
+      const int kn = nb >> 2, fn = nb & 3, nd2 = fmask<N>(fn, Nfp - 1 - d);
+      if (kn >= k0 && kn < k0 + ne) {
+        const R* qb = sQ + (kn - k0) * ESTR;
+#pragma unroll
+        for (int c = 0; c < NF; ++c) b[c] = qb[c * NpP + nd2];
+      } else {
+        const R* qb = qin + (size_t)kn * ESTR;
+#pragma unroll
+        for (int c = 0; c < NF; ++c) b[c] = ldg(qb + c * NpP + nd2);
+      }
+    } else if (P == PHYS_ADV) {
+      const int bf = -1 - nb;
+      const double x = p.bxy[((size_t)bf * Nfp + d) * 2], y = p.bxy[((size_t)bf * Nfp + d) * 2 + 1];
+      b[0] = (R)adv_exact(p, p.t_dev ? *p.t_dev + p.t : p.t, x, y);
+    } else if (P == PHYS_TM) {  // PEC: H+ = H-, Ez+ = -Ez-
+      b[0] = a[0]; b[1] = a[1]; b[2] = -a[2];
+    } else {                    // PEC: E+ = -E-, Hz+ = Hz-
+      b[0] = -a[0]; b[1] = -a[1]; b[2] = a[2];
+    }
+    R* fo = sF + e * NF * NFACE + fm;
+    if (P == PHYS_ADV) {
+      const R an = cax * nx + cay * ny;
+      fo[0] = ((an >= (R)0) ? a[0] : b[0]) * an * fJ;
+    } else if (P == PHYS_TM) {
+      const R d0 = a[0] - b[0], d1 = a[1] - b[1], s2 = a[2] + b[2];
+      const R w = s2 + ny * d0 - nx * d1;
+      fo[0] = (R)0.5 * ny * w * fJ;
+      fo[NFACE] = -(R)0.5 * nx * w * fJ;
+      fo[2 * NFACE] = (R)0.5 * (ny * (a[0] + b[0]) - nx * (a[1] + b[1]) + a[2] - b[2]) * fJ;
+    } else {
+      const R d0 = a[0] - b[0], d1 = a[1] - b[1], s2 = a[2] + b[2];
+      const R w = s2 - ny * d0 + nx * d1;
+      fo[0] = -(R)0.5 * ny * w * fJ;
+      fo[NFACE] = (R)0.5 * nx * w * fJ;
+      fo[2 * NFACE] = (R)0.5 * (nx * (a[1] + b[1]) - ny * (a[0] + b[0]) + a[2] - b[2]) * fJ;
+    }
+  }
+  __syncthreads();
+
+  // ---- volume + lift + epilogue: one (element, node) per thread
+  if (tid < ne * Np) {
+    const int e = tid / Np, i = tid - e * Np;
+    const R* qe = sQ + e * ESTR;
+    R ur[NF], us[NF], lf[NF];
+#pragma unroll
+    for (int c = 0; c < NF; ++c) ur[c] = us[c] = lf[c] = (R)0;
+#pragma unroll 4
+    for (int j = 0; j < Np; ++j) {
+      const R dr = sDrT[j * Np + i], ds = sDsT[j * Np + i];
+#pragma unroll
+      for (int c = 0; c < NF; ++c) {
+        const R v = qe[c * NpP + j];
+        ur[c] = fma(dr, v, ur[c]);
+        us[c] = fma(ds, v, us[c]);
+      }
+    }
+    const R* fe = sF + e * NF * NFACE;
+#pragma unroll 3
+    for (int m = 0; m < NFACE; ++m) {
+      const R l = sLT[m * Np + i];
+#pragma unroll
+      for (int c = 0; c < NF; ++c) lf[c] = fma(l, fe[c * NFACE + m], lf[c]);
+    }
+    const R* g = sG + e * 16;
+    const R rx = (R)g[0], ry = (R)g[1], sx = (R)g[2], sy = (R)g[3];
+    const R ilJ = g[4];  // -1/J
+    R rhs[NF];
+    if (P == PHYS_ADV) {
+      const R dx = rx * ur[0] + sx * us[0], dy = ry * ur[0] + sy * us[0];
+      rhs[0] = cax * dx + cay * dy + ilJ * lf[0];
+    } else if (P == PHYS_TM) {  // Hx' = Dy Ez, Hy' = -Dx Ez, Ez' = -Dx Hy + Dy Hx
+      rhs[0] = (ry * ur[2] + sy * us[2]) + ilJ * lf[0];
+      rhs[1] = -(rx * ur[2] + sx * us[2]) + ilJ * lf[1];
+      rhs[2] = -(rx * ur[1] + sx * us[1]) + (ry * ur[0] + sy * us[0]) + ilJ * lf[2];
+    } else {                    // Ex' = -Dy Hz, Ey' = Dx Hz, Hz' = Dx Ey - Dy Ex
+      rhs[0] = -(ry * ur[2] + sy * us[2]) + ilJ * lf[0];
+      rhs[1] = (rx * ur[2] + sx * us[2]) + ilJ * lf[1];
+      rhs[2] = (rx * ur[1] + sx * us[1]) - (ry * ur[0] + sy * us[0]) + ilJ * lf[2];
+    }
+    const size_t base = (size_t)(k0 + e) * ESTR + i;
+    R* out = static_cast<R*>(p.out);
+    R* aux = static_cast<R*>(p.aux);
+    if (p.mode == MODE_RHS) {
+#pragma unroll
+      for (int c = 0; c < NF; ++c) out[base + c * NpP] = rhs[c];
+    } else if (p.mode == MODE_LSERK) {
+#pragma unroll
+      for (int c = 0; c < NF; ++c) {
+        const size_t o = base + c * NpP;
+        const R r = cca * aux[o] + cdt * rhs[c];
+        aux[o] = r;
+        out[o] = qe[c * NpP + i] + ccb * r;
+      }
+    } else {  // classical RK4 stage
+      R* q0 = static_cast<R*>(p.q0);
+      const R co = cca, wa = ccb;
+#pragma unroll
+      for (int c = 0; c < NF; ++c) {
+        const size_t o = base + c * NpP;
+        if (p.stage == 0) {
+          aux[o] = rhs[c];
+          out[o] = qe[c * NpP + i] + co * rhs[c];
+        } else if (p.stage < 3) {
+          aux[o] = aux[o] + wa * rhs[c];
+          out[o] = q0[o] + co * rhs[c];
+        } else {
+          q0[o] = q0[o] + co * (aux[o] + rhs[c]);
+        }
+      }
+    }
+  }
+  __syncthreads();
+  return true;
+}
+
+template <typename R, int N, int P>
+__global__ void __launch_bounds__(256) dg_rhs_kernel(const RhsParams p) {
+  using C = RhsConfig<R, N, P>;
+  extern __shared__ __align__(128) unsigned char smem[];
+  const V1Smem<R, N, P> s(smem);
+  const int ntiles = (p.K + C::TE - 1) / C::TE;
+  if (threadIdx.x == 0) {
+    mbar_init(s.bar, 1);
     fence_barrier_init();
   }
   __syncthreads();
   uint32_t phase = 0;
-  if (tid == 0) {
-    mbar_arrive_expect_tx(bar, MatLayout<R, N>::kBytes);
-    bulk_g2s(sDrT, p.mats, MatLayout<R, N>::kBytes, bar);
-  }
-  // All threads must have observed the matrix phase before thread 0 re-arms
-  // the same barrier for the first tile: otherwise a fast tile copy can
-  // complete the next phase before a slow warp polls this one, and that warp
-  // would then wait for a phase that never comes.  The AND also makes a
-  // timed-out wait exit the whole CTA.
-  if (!__syncthreads_and(mbar_wait(bar, phase, p.status))) return;
-  phase ^= 1;
-
+  if (!rhs_v1_load_mats<R, N, P>(p, s, phase)) return;
   for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const int k0 = tile * TE;
-    const int ne = min(TE, p.K - k0);
-    if (tid == 0) {
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      const uint32_t bq = ne * ESTR * sizeof(R), bg = ne * 16 * sizeof(R), bn = ne * 16;
-      mbar_arrive_expect_tx(bar, bq + bg + bn);
-      bulk_g2s(sQ, qin + (size_t)k0 * ESTR, bq, bar);
-      bulk_g2s(sG, static_cast<const R*>(p.geom) + (size_t)k0 * 16, bg, bar);
-      bulk_g2s(sN, p.nbr + k0, bn, bar);
-    }
-    if (!__syncthreads_and(mbar_wait(bar, phase, p.status))) return;
-    phase ^= 1;
-
-    // ---- numerical fluxes on the tile's face nodes, scaled by faceJ
-    for (int it = tid; it < ne * NFACE; it += blockDim.x) {
-      const int e = it / NFACE, fm = it - e * NFACE, f = fm / Nfp, d = fm - f * Nfp;
-      const R* g = sG + e * 16;
-      const int nb = f == 0 ? sN[e].x : (f == 1 ? sN[e].y : sN[e].z);
-      const int nd = fmask<N>(f, d);
-      const R* qa = sQ + e * ESTR;
-      const R nx = (R)g[8 + f], ny = (R)g[11 + f], fJ = (R)g[5 + f];
-      R a[NF], b[NF];
-#pragma unroll
-      for (int c = 0; c < NF; ++c) a[c] = qa[c * NpP + nd];
-      if (nb >= 0) {
-        const int kn = nb >> 2, fn = nb & 3, nd2 = fmask<N>(fn, Nfp - 1 - d);
-        if (kn >= k0 && kn < k0 + ne) {
-          const R* qb = sQ + (kn - k0) * ESTR;
-#pragma unroll
-          for (int c = 0; c < NF; ++c) b[c] = qb[c * NpP + nd2];
-        } else {
-          const R* qb = qin + (size_t)kn * ESTR;
-#pragma unroll
-          for (int c = 0; c < NF; ++c) b[c] = ldg(qb + c * NpP + nd2);
-        }
-      } else if (P == PHYS_ADV) {
-        const int bf = -1 - nb;
-        const double x = p.bxy[((size_t)bf * Nfp + d) * 2], y = p.bxy[((size_t)bf * Nfp + d) * 2 + 1];
-        b[0] = (R)adv_exact(p, tnow, x, y);
-      } else if (P == PHYS_TM) {  // PEC: H+ = H-, Ez+ = -Ez-
-        b[0] = a[0]; b[1] = a[1]; b[2] = -a[2];
-      } else {                    // PEC: E+ = -E-, Hz+ = Hz-
-        b[0] = -a[0]; b[1] = -a[1]; b[2] = a[2];
-      }
-      R* fo = sF + e * NF * NFACE + fm;
-      if (P == PHYS_ADV) {
-        const R an = cax * nx + cay * ny;
-        fo[0] = ((an >= (R)0) ? a[0] : b[0]) * an * fJ;
-      } else if (P == PHYS_TM) {
-        const R d0 = a[0] - b[0], d1 = a[1] - b[1], s2 = a[2] + b[2];
-        const R w = s2 + ny * d0 - nx * d1;
-        fo[0] = (R)0.5 * ny * w * fJ;
-        fo[NFACE] = -(R)0.5 * nx * w * fJ;
-        fo[2 * NFACE] = (R)0.5 * (ny * (a[0] + b[0]) - nx * (a[1] + b[1]) + a[2] - b[2]) * fJ;
-      } else {
-        const R d0 = a[0] - b[0], d1 = a[1] - b[1], s2 = a[2] + b[2];
-        const R w = s2 - ny * d0 + nx * d1;
-        fo[0] = -(R)0.5 * ny * w * fJ;
-        fo[NFACE] = (R)0.5 * nx * w * fJ;
-        fo[2 * NFACE] = (R)0.5 * (nx * (a[1] + b[1]) - ny * (a[0] + b[0]) + a[2] - b[2]) * fJ;
-      }
-    }
-    __syncthreads();
-
-    // ---- volume + lift + epilogue: one (element, node) per thread
-    if (tid < ne * Np) {
-      const int e = tid / Np, i = tid - e * Np;
-      const R* qe = sQ + e * ESTR;
-      R ur[NF], us[NF], lf[NF];
-#pragma unroll
-      for (int c = 0; c < NF; ++c) ur[c] = us[c] = lf[c] = (R)0;
-#pragma unroll 4
-      for (int j = 0; j < Np; ++j) {
-        const R dr = sDrT[j * Np + i], ds = sDsT[j * Np + i];
-#pragma unroll
-        for (int c = 0; c < NF; ++c) {
-          const R v = qe[c * NpP + j];
-          ur[c] = fma(dr, v, ur[c]);
-          us[c] = fma(ds, v, us[c]);
-        }
-      }
-      const R* fe = sF + e * NF * NFACE;
-#pragma unroll 3
-      for (int m = 0; m < NFACE; ++m) {
-        const R l = sLT[m * Np + i];
-#pragma unroll
-        for (int c = 0; c < NF; ++c) lf[c] = fma(l, fe[c * NFACE + m], lf[c]);
-      }
-      const R* g = sG + e * 16;
-      const R rx = (R)g[0], ry = (R)g[1], sx = (R)g[2], sy = (R)g[3];
-      const R ilJ = g[4];  // -1/J
-      R rhs[NF];
-      if (P == PHYS_ADV) {
-        const R dx = rx * ur[0] + sx * us[0], dy = ry * ur[0] + sy * us[0];
-        rhs[0] = cax * dx + cay * dy + ilJ * lf[0];
-      } else if (P == PHYS_TM) {  // Hx' = Dy Ez, Hy' = -Dx Ez, Ez' = -Dx Hy + Dy Hx
-        rhs[0] = (ry * ur[2] + sy * us[2]) + ilJ * lf[0];
-        rhs[1] = -(rx * ur[2] + sx * us[2]) + ilJ * lf[1];
-        rhs[2] = -(rx * ur[1] + sx * us[1]) + (ry * ur[0] + sy * us[0]) + ilJ * lf[2];
-      } else {                    // Ex' = -Dy Hz, Ey' = Dx Hz, Hz' = Dx Ey - Dy Ex
-        rhs[0] = -(ry * ur[2] + sy * us[2]) + ilJ * lf[0];
-        rhs[1] = (rx * ur[2] + sx * us[2]) + ilJ * lf[1];
-        rhs[2] = (rx * ur[1] + sx * us[1]) - (ry * ur[0] + sy * us[0]) + ilJ * lf[2];
-      }
-      const size_t base = (size_t)(k0 + e) * ESTR + i;
-      R* out = static_cast<R*>(p.out);
-      R* aux = static_cast<R*>(p.aux);
-      if (p.mode == MODE_RHS) {
-#pragma unroll
-        for (int c = 0; c < NF; ++c) out[base + c * NpP] = rhs[c];
-      } else if (p.mode == MODE_LSERK) {
-#pragma unroll
-        for (int c = 0; c < NF; ++c) {
-          const size_t o = base + c * NpP;
-          const R r = cca * aux[o] + cdt * rhs[c];
-          aux[o] = r;
-          out[o] = qe[c * NpP + i] + ccb * r;
-        }
-      } else {  // classical RK4 stage
-        R* q0 = static_cast<R*>(p.q0);
-        const R co = cca, wa = ccb;
-#pragma unroll
-        for (int c = 0; c < NF; ++c) {
-          const size_t o = base + c * NpP;
-          if (p.stage == 0) {
-            aux[o] = rhs[c];
-            out[o] = qe[c * NpP + i] + co * rhs[c];
-          } else if (p.stage < 3) {
-            aux[o] = aux[o] + wa * rhs[c];
-            out[o] = q0[o] + co * rhs[c];
-          } else {
-            q0[o] = q0[o] + co * (aux[o] + rhs[c]);
-          }
-        }
-      }
-    }
-    __syncthreads();
+    const int k0 = tile * C::TE;
+    if (!rhs_v1_tile<R, N, P>(p, s, phase, k0, min(C::TE, p.K - k0))) return;
   }
 }
 

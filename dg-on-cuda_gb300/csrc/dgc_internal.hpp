@@ -54,5 +54,9 @@ void device_free(dgc_handle_s* h);
 int ipdg_init(dgc_handle_s* h);
 void ipdg_free(dgc_handle_s* h);
 void ipdg_operators_changed(dgc_handle_s* h);
+// stage-kernel parameters of a handle (geometry, operators, physics; no buffers)
+dgk::RhsParams rhs_base_params(dgc_handle_s* h);
+// LSERK4 (Carpenter-Kennedy) coefficients: 0 -> a_k, 1 -> b_k, 2 -> c_k (5 each)
+const double* lserk_coeffs(int which);
 
 }  // namespace dgc

@@ -109,6 +109,13 @@ def lib():
             L.dgc_ref_nodes.argtypes = [C.c_int, _dp, _dp]
             L.dgc_ref_operator.argtypes = [C.c_int, C.c_int, _dp]
             L.dgc_host_mesh.argtypes = [C.c_int, _dp, C.c_int, _ip, C.c_int, _dp, _ip, C.POINTER(C.c_int)]
+            L.dgc_batch_create.argtypes = [C.POINTER(_vp), C.c_int, C.POINTER(_vp)]
+            L.dgc_batch_destroy.argtypes = [_vp]
+            L.dgc_batch_lserk4_step.argtypes = [_vp, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp), _dp, _dp, _vp]
+            L.dgc_batch_lserk4_run.argtypes = [_vp, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp), _dp, _dp,
+                                               C.c_int, C.c_int, C.POINTER(C.c_int), _vp]
+            L.dgc_batch_launch_count.restype = C.c_int64
+            L.dgc_batch_launch_count.argtypes = [_vp]
             _lib = L
     return _lib
 
@@ -333,3 +340,51 @@ class Discretization:
         if rc != 0 and not (rc == ERR_NOT_CONVERGED and not check):
             _check(rc)
         return x, st.as_dict()
+
+
+class Batch:
+    """Many independent FP32 advection / Maxwell discretizations advanced together:
+    every LSERK4 stage of every instance is one persistent launch (dgc_batch_*)."""
+
+    def __init__(self, discretizations):
+        self.items = list(discretizations)
+        n = len(self.items)
+        arr = (_vp * n)(*[d._h for d in self.items])
+        h = _vp()
+        _check(lib().dgc_batch_create(arr, n, C.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().dgc_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def _ptrs(ts):
+        return (_vp * len(ts))(*[_ptr(t) for t in ts])
+
+    def lserk4_step(self, q_in, q_out, res, t, dt, stream=None):
+        """One step of every instance: q_in[i] -> q_out[i] at times t[i], steps dt[i]."""
+        tt = np.ascontiguousarray(t, dtype=np.float64)
+        dd = np.ascontiguousarray(dt, dtype=np.float64)
+        _check(lib().dgc_batch_lserk4_step(self._h, self._ptrs(q_in), self._ptrs(q_out), self._ptrs(res), tt, dd,
+                                           _stream(stream)))
+        return q_out
+
+    def lserk4_run(self, qa, qb, res, t0, dt, nsteps: int, graph: bool = True, stream=None):
+        """nsteps steps from qa; returns the list of tensors holding the results."""
+        tt = np.ascontiguousarray(t0, dtype=np.float64)
+        dd = np.ascontiguousarray(dt, dtype=np.float64)
+        fin = C.c_int()
+        _check(lib().dgc_batch_lserk4_run(self._h, self._ptrs(qa), self._ptrs(qb), self._ptrs(res), tt, dd,
+                                          int(nsteps), int(graph), C.byref(fin), _stream(stream)))
+        return list(qb) if fin.value else list(qa)
+
+    def launch_count(self) -> int:
+        return int(lib().dgc_batch_launch_count(self._h))

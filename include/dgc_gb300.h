@@ -174,6 +174,35 @@ int dgc_lserk4_stage(dgc_handle h, int stage, const void* q_in, void* q_out, voi
 int dgc_lserk4_run(dgc_handle h, void* qa, void* qb, void* res, double t0, double dt, int nsteps,
                    int use_graph, void** final_state, void* stream);
 
+/* ---- batches: many independent problems in one persistent launch --------- */
+
+/* A batch over existing FP32 advection / Maxwell handles (any mix of orders
+ * and mesh sizes).  Every LSERK4 stage of every instance runs in ONE launch:
+ * persistent CTAs take work items (instance, run of tiles) from a device
+ * queue ordered by decreasing cost, and evaluate them with the same tile code
+ * as the handles' variant-0 stage kernel, so a batched step is bitwise equal
+ * to per-instance dgc_lserk4_step calls with that variant.  The handles must
+ * outlive the batch.  No reference counterpart (the reference integrates one
+ * problem per process). */
+typedef struct dgc_batch_s* dgc_batch;
+int dgc_batch_create(const dgc_handle* handles, int num_instances, dgc_batch* out);
+int dgc_batch_destroy(dgc_batch b);
+
+/* One LSERK4 step of every instance i: q_in[i] -> q_out[i] (q_in[i] is scratch
+ * afterwards), res[i] its residual register, at time t[i] with step dt[i]. */
+int dgc_batch_lserk4_step(dgc_batch b, void* const* q_in, void* const* q_out, void* const* res, const double* t,
+                          double const* dt, void* stream);
+
+/* nsteps steps from qa[i] at time t0[i]; buffers ping-pong between qa and qb.
+ * *final_in_qb is set to 1 when the results are in qb (odd step counts).  With
+ * use_graph != 0 the step (5 stage launches and the per-instance clocks) is
+ * replayed from a captured CUDA graph. */
+int dgc_batch_lserk4_run(dgc_batch b, void* const* qa, void* const* qb, void* const* res, const double* t0,
+                         const double* dt, int nsteps, int use_graph, int* final_in_qb, void* stream);
+
+/* Kernels launched through the batch so far. */
+int64_t dgc_batch_launch_count(dgc_batch b);
+
 /* ---- laplace_2d (DGC_LAPLACE handles; scalar field, native layout) -------- */
 
 /* out = A u, the discrete Laplacian with homogeneous boundary data (all faces
