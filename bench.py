@@ -166,9 +166,16 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def read_traffic():
-    """DRAM bytes per launch of the stage kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "dg_rhs_maxwell_te_n6_fp32.md")
+# committed ncu summaries of the stage-kernel variants on this workload
+PROFILES = {5: "dg_rhs_blk_maxwell_te_n6_fp32.md", 9: "dg_rhs_tcp_maxwell_te_n6_fp32.md"}
+
+
+def read_traffic(variant):
+    """DRAM bytes per launch of the chosen stage kernel from its committed ncu
+    summary (None when no summary covers that variant)."""
+    if variant not in PROFILES:
+        return None
+    path = os.path.join(ROOT, "profiles", PROFILES[variant])
     try:
         txt = open(path).read()
         m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", txt)
@@ -517,7 +524,7 @@ def main():
     achieved = alg_bytes / (launch_ms * 1e-3) / 1e9
     peak, peak_kind = measured_peak()
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": read_traffic(), "peak_source": peak_kind,
+                "frac": achieved / peak, "traffic": read_traffic(tuned), "peak_source": peak_kind,
                 "kernel": STAGE_KERNELS.get(tuned, "variant %s" % tuned) + " (LSERK4 stage)",
                 "alg_bytes_per_launch": alg_bytes, "alg_bytes_per_element": alg_bytes_elem,
                 "launch_ms": launch_ms, "stage_ms": [float(v) for v in stage_ms.mean(axis=0)],
