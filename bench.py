@@ -246,6 +246,137 @@ def measure_poisson(dg, meshes):
     return out
 
 
+LEARN_NSIDE, LEARN_ORDER, LEARN_SEED = 128, 4, 5151
+LEARN_TRAIN, LEARN_HELD = 1600, 400            # the full sequence: 2000 solves
+LEARN_TRAIN_SAMPLE, LEARN_HELD_SAMPLE = 16, 8  # the bounded sample timed here
+LEARN_SNAPSHOTS = (4, 16, 64, 256, 1024)       # PCG iterates giving residual / error pairs
+
+
+def smooth_rhs(x, y, index: int, modes: int = 24):
+    """Right-hand side `index` of the learned-preconditioner sequence: `modes` sine
+    modes sin(kx pi (x+1)/2) sin(ky pi (y+1)/2), kx, ky in 1..8, amplitudes
+    ~ N(0, |k|^-2), seeded by the index (zero on the boundary)."""
+    rng = np.random.default_rng(LEARN_SEED * 100003 + index)
+    f = np.zeros_like(x)
+    for _ in range(modes):
+        kx, ky = rng.integers(1, 9, size=2)
+        f += rng.normal(0.0, (kx * kx + ky * ky) ** -0.5) * np.sin(kx * np.pi * (x + 1) / 2) * \
+            np.sin(ky * np.pi * (y + 1) / 2)
+    return f
+
+
+def measure_learned(dg, meshes):
+    """Learned preconditioner on IPDG Poisson (Dirichlet, jittered 128x128 mesh,
+    K = 32768, N = 4): residual / error pairs from plain block-Jacobi PCG iterates
+    of the first training solves train the 4-layer width-64 message-passing network
+    (BF16 weights, FP32 accumulation, energy-norm loss, Adam); on held-out solves
+    the learned solve (truncated flexible CG with the network, block-Jacobi PCG as
+    fallback and judge once its break-even budget is spent) is timed against plain
+    FP64 block-Jacobi PCG and the mixed FP32/FP64 refinement, all to 1e-10 relative
+    FP64 residual.  A bounded sample of the 2000-solve sequence (1600 train / 400
+    held out): the first LEARN_TRAIN_SAMPLE training and LEARN_HELD_SAMPLE held-out
+    right-hand sides."""
+    import torch
+    m = meshes.jittered_square(LEARN_NSIDE, LEARN_SEED)
+    D = dg.Discretization(m, "laplace", LEARN_ORDER, dg.F64, tau=dg.TAU_SCALED, dirichlet=True)
+    x, y = D.node_xy()
+    D.block_jacobi()
+    c = float(np.sqrt(D.K * D.Np))
+    net = dg.MPNN(D, layers=4, seed=LEARN_SEED)
+    bj = dg.MPNN(D, layers=1, seed=0)               # zero output layer: M(r) = Binv r
+
+    def rhs(i):
+        return D.mass(D.upload(smooth_rhs(x, y, i).reshape(-1)))
+
+    def sync_time(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = fn()
+        torch.cuda.synchronize()
+        return r, time.perf_counter() - t0
+
+    # training pairs: x = r c/|r|, t = (e - Binv r) c/|r| at PCG iterates x_k, e = x* - x_k
+    t0 = time.perf_counter()
+    X, T, pcg_its = [], [], []
+    for i in range(LEARN_TRAIN_SAMPLE):
+        b = rhs(i)
+        xs, st = D.pcg(b, rtol=1e-10)
+        pcg_its.append(st["iterations"])
+        for k in LEARN_SNAPSHOTS:
+            xk, _ = D.pcg(b, rtol=1e-30, maxit=k, check=False)
+            r = b - D.spd(xk)
+            nr = float(torch.linalg.norm(r))
+            X.append((r * (c / nr)).float())
+            T.append(((xs - xk - bj.precondition(r)) * (c / nr)).float())
+    torch.cuda.synchronize()
+    datagen_s = time.perf_counter() - t0
+    sigma = float(torch.sqrt(torch.mean(torch.stack([torch.mean(t.double() ** 2) for t in T]))))
+    T = [t / sigma for t in T]
+    rng = np.random.default_rng(LEARN_SEED)
+    losses, batch, epochs = [], 8, 30
+    t0 = time.perf_counter()
+    for ep in range(epochs):
+        order = rng.permutation(len(X))
+        el = [net.train_step(torch.cat([X[j] for j in order[i:i + batch]]),
+                             torch.cat([T[j] for j in order[i:i + batch]]), lr=3e-4)[0]
+              for i in range(0, len(X), batch)]
+        losses.append(float(np.mean(el)))
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    w = net.get_weights()
+    w[-(D.NpP * 64 + D.NpP):] *= sigma               # targets were trained in units of sigma
+    net.set_weights(w)
+
+    # per-iteration costs and the flexible-CG budget beyond which it cannot beat plain PCG
+    b0 = rhs(0)
+    (_, st_p), tp = sync_time(lambda: D.pcg(b0, rtol=1e-10))
+    (_, st_f), tf = sync_time(lambda: net.fpcg(b0, rtol=1e-30, maxit=300, check=False))
+    it_p, it_f = tp / st_p["iterations"], tf / max(st_f["iterations"], 1)
+    budget = int(np.median(pcg_its) * it_p / it_f)
+    _, t_fwd = sync_time(lambda: [net.forward(X[0]) for _ in range(20)])
+
+    held = {"fp64_pcg": [], "mixed_ir": [], "learned": []}
+    fell = 0
+    agree = []
+    for i in range(LEARN_HELD_SAMPLE):
+        b = rhs(LEARN_TRAIN + i)
+        (xp, sp), tp = sync_time(lambda: D.pcg(b, rtol=1e-10))
+        (_, sm), tm = sync_time(lambda: D.pcg(b, mode=dg.SOLVE_MIXED_IR, rtol=1e-10))
+        (xl, sl), tl = sync_time(lambda: net.solve(b, rtol=1e-10, fcg_maxit=budget))
+        fell += int(sl["fell_back"])
+        held["fp64_pcg"].append((sp["iterations"], tp, sp["final_relres"]))
+        held["mixed_ir"].append((sm["iterations"], tm, sm["final_relres"]))
+        held["learned"].append((sl["iterations"], tl, sl["final_relres"], sl["inner_iterations"]))
+        agree.append(float(torch.linalg.norm(xl - xp) / torch.linalg.norm(xp)))
+    D.check()
+
+    def summary(rows):
+        its = [r[0] for r in rows]
+        ts = [r[1] for r in rows]
+        return {"iterations_median": float(np.median(its)), "wall_s_p50": float(np.percentile(ts, 50)),
+                "wall_s_p95": float(np.percentile(ts, 95)), "wall_s_total": float(np.sum(ts)),
+                "max_final_relres": float(max(r[2] for r in rows))}
+
+    out = {"workload": f"ipdg_poisson_dirichlet_k{D.K}_n{LEARN_ORDER}_learned_precond",
+           "num_cells": D.K, "order": LEARN_ORDER, "rtol": 1e-10,
+           "sequence": {"solves": LEARN_TRAIN + LEARN_HELD, "train": LEARN_TRAIN, "held_out": LEARN_HELD,
+                        "rhs": "24 Fourier modes, amplitudes ~ N(0, |k|^-2), seeded per solve"},
+           "sample": {"train_solves": LEARN_TRAIN_SAMPLE, "held_out_solves": LEARN_HELD_SAMPLE,
+                      "pairs": len(X), "snapshots": list(LEARN_SNAPSHOTS)},
+           "network": {"layers": 4, "width": 64, "params": net.num_params, "weights": "bf16 (fp32 masters)",
+                       "accumulate": "fp32", "loss": "energy norm |y - t|_S^2 / |t|_S^2",
+                       "optimizer": f"Adam lr 3e-4, batch {batch}, {epochs} epochs",
+                       "forward_ms": t_fwd / 20 * 1e3},
+           "datagen_s": datagen_s, "train_s": train_s, "loss_per_epoch": losses,
+           "pcg_iteration_ms": it_p * 1e3, "fcg_iteration_ms": it_f * 1e3, "fcg_budget": budget,
+           "held_out": {k: summary(v) for k, v in held.items()},
+           "fallback_count": fell,
+           "max_rel_l2_learned_vs_fp64_pcg": float(max(agree))}
+    out["speedup_learned_vs_fp64_pcg"] = out["held_out"]["fp64_pcg"]["wall_s_total"] / \
+        out["held_out"]["learned"]["wall_s_total"]
+    return out
+
+
 BATCH_INSTANCES, BATCH_SEED, BATCH_STEPS = 96, 777, 10
 
 
@@ -356,6 +487,7 @@ def measure_e2e(D32, bufs, res, flush, stream, t, dt, steps, ws, dofs, barrier):
     """Per step through the C ABI with pinned host buffers: H2D of the state,
     one LSERK4 step (dgc_lserk4_step), D2H of the new state."""
     import torch
+    from dgc_gb300 import replicas
     h_state = torch.empty(D32.state_len, dtype=torch.float32, pin_memory=True)
     h_state.copy_(bufs[0].cpu())
     h_out = torch.empty_like(h_state)
@@ -369,14 +501,10 @@ def measure_e2e(D32, bufs, res, flush, stream, t, dt, steps, ws, dofs, barrier):
         h_out.copy_(bufs[1], non_blocking=True)
         evs[it][1].record(stream)
     barrier()
-    ms = float(np.mean([a.elapsed_time(b) for a, b in evs]))
-    if ws > 1:
-        import torch.distributed as tdist
-        tt = torch.tensor([ms], device="cuda")
-        tdist.all_reduce(tt, op=tdist.ReduceOp.MAX)
-        ms = float(tt.item())
+    ms = replicas.max_over_ranks(float(np.mean([a.elapsed_time(b) for a, b in evs])), device="cuda")
     nbytes = D32.state_len * 4
-    return {"value": ws * dofs * 5 / (ms * 1e-3) / 1e9, "unit": UNIT, "h2d_bytes_per_step": nbytes,
+    return {"value": replicas.job_throughput(dofs * 5, ms * 1e-3, ws) / 1e9, "unit": UNIT,
+            "h2d_bytes_per_step": nbytes,
             "d2h_bytes_per_step": nbytes, "ms_per_step": ms,
             "path": "dgc_lserk4_step via ctypes, pinned host state in and out every step"}
 
@@ -437,6 +565,7 @@ def main():
     ap.add_argument("--variant", type=int, default=-1, help="force an RHS kernel variant instead of autotuning")
     ap.add_argument("--no-poisson", action="store_true", help="skip the IPDG Poisson solver comparison")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-instances comparison")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-preconditioner comparison")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -444,7 +573,7 @@ def main():
 
     import torch
     import dgc_gb300 as dg
-    from dgc_gb300 import meshes
+    from dgc_gb300 import meshes, replicas
 
     ws, rank, local = dist_env()
     torch.cuda.set_device(local)
@@ -507,13 +636,9 @@ def main():
     stage_ms = np.array([[events[i][s].elapsed_time(events[i][s + 1]) for s in range(5)]
                          for i in range(args.steps)])
     D32.check()
-    my_ms = float(step_ms.mean())
-    if ws > 1:
-        import torch.distributed as tdist
-        tt = torch.tensor([my_ms], device="cuda")
-        tdist.all_reduce(tt, op=tdist.ReduceOp.MAX)
-        my_ms = float(tt.item())
-    value = ws * dofs * 5 / (my_ms * 1e-3) / 1e9
+    # replicas: every rank advances its own copy; slowest rank's time, all ranks' work
+    my_ms = replicas.max_over_ranks(float(step_ms.mean()), device="cuda")
+    value = replicas.job_throughput(dofs * 5, my_ms * 1e-3, ws) / 1e9
 
     # roofline of the dominant kernel (the fused RHS + LSERK4 stage): compulsory
     # bytes per element = read q, read res, write res, write q (3 fields x Np x 4 B
@@ -544,6 +669,9 @@ def main():
     batched = None
     if rank == 0 and not args.no_batched:
         batched = measure_batched(dg, meshes)
+    learned = None
+    if rank == 0 and not args.no_learned:
+        learned = measure_learned(dg, meshes)
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         csteps = 10
@@ -559,7 +687,8 @@ def main():
                 "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu,
                 "clocks": clocks, "fp64_plain": fp64,
                 "speedup_mixed_vs_fp64": (value / ws / fp64["value"]) if fp64 else None,
-                "accuracy": accuracy, "poisson": poisson, "batched": batched, "wall_s_timed_region": wall}
+                "accuracy": accuracy, "poisson": poisson, "batched": batched, "learned_precond": learned,
+                "wall_s_timed_region": wall}
         print(json.dumps(line))
     if ws > 1:
         import torch.distributed as tdist

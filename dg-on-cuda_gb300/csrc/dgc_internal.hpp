@@ -54,6 +54,11 @@ void device_free(dgc_handle_s* h);
 int ipdg_init(dgc_handle_s* h);
 void ipdg_free(dgc_handle_s* h);
 void ipdg_operators_changed(dgc_handle_s* h);
+// block-Jacobi inverse of the SPD laplace form (built once), and z = Binv r (FP64)
+int ipdg_build_preconditioner(dgc_handle_s* h, cudaStream_t s);
+int ipdg_block_jacobi_apply(dgc_handle_s* h, const double* r, double* z, cudaStream_t s);
+// out = S u with the FP32 kernels (any laplace handle; one field, native layout)
+int ipdg_spd_apply_f32(dgc_handle_s* h, const float* u, float* out, cudaStream_t s);
 // stage-kernel parameters of a handle (geometry, operators, physics; no buffers)
 dgk::RhsParams rhs_base_params(dgc_handle_s* h);
 // LSERK4 (Carpenter-Kennedy) coefficients: 0 -> a_k, 1 -> b_k, 2 -> c_k (5 each)

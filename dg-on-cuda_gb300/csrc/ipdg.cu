@@ -237,6 +237,31 @@ int ipdg_build_preconditioner(dgc_handle_s* h, cudaStream_t s) {
   return DGC_OK;
 }
 
+// z = Binv r elementwise (FP64, native layout; padding nodes of z set to 0)
+__global__ void k_bj_apply(int K, int Np, int NpP, int bstr, const double* __restrict__ binv,
+                           const double* __restrict__ r, double* __restrict__ z) {
+  const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (g >= (int64_t)K * NpP) return;
+  const int k = (int)(g / NpP), i = (int)(g % NpP);
+  double s = 0.0;
+  if (i < Np) {
+    const double* B = binv + (size_t)k * bstr;
+    const double* rk = r + (size_t)k * NpP;
+    for (int j = 0; j < Np; ++j) s += B[j * Np + i] * rk[j];
+  }
+  z[g] = s;
+}
+
+int ipdg_block_jacobi_apply(dgc_handle_s* h, const double* r, double* z, cudaStream_t s) {
+  if (int rc = ipdg_build_preconditioner(h, s)) return rc;
+  const int64_t n = (int64_t)h->K * h->NpP;
+  k_bj_apply<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(h->K, h->Np, h->NpP, h->ipdg->bstr, h->ipdg->binv64, r,
+                                                        z);
+  CKI(cudaGetLastError());
+  ++h->launches;
+  return DGC_OK;
+}
+
 int upload_ipdg_matrices(dgc_handle_s* h) {
   IpdgState* st = h->ipdg;
   const int Np = h->Np, NF = 3 * h->Nfp;
@@ -267,9 +292,11 @@ int ipdg_init(dgc_handle_s* h) {
   h->ipdg = st;
   const int Np = h->Np, NF = 3 * h->Nfp;
   st->bstr = (Np * Np + 3) / 4 * 4;
-  if (h->desc.tau == DGC_TAU_ONE) {
+  if (h->desc.tau == DGC_TAU_ONE) {  // both penalty copies (FP64 and FP32 kernels)
     std::vector<double> ones((size_t)4 * h->K, 1.0);
+    std::vector<float> ones32((size_t)4 * h->K, 1.0f);
     CKI(cudaMemcpy(h->d_tau, ones.data(), ones.size() * 8, cudaMemcpyHostToDevice));
+    CKI(cudaMemcpy(h->d_tau32, ones32.data(), ones32.size() * 4, cudaMemcpyHostToDevice));
   }
   CKI(cudaMalloc(&st->mass64, (size_t)st->bstr * 8));
   CKI(cudaMalloc(&st->mass32, (size_t)st->bstr * 4));
@@ -450,6 +477,11 @@ int true_residual(dgc_handle_s* h, const double* b64, const double* x64, double*
 }
 
 }  // namespace
+
+int ipdg_spd_apply_f32(dgc_handle_s* h, const float* u, float* out, cudaStream_t s) {
+  if (int rc = check_laplace(h)) return rc;
+  return apply<float>(h, dgk::IK_DIV_SPD, u, out, nullptr, nullptr, s);
+}
 
 }  // namespace dgc
 

@@ -24,6 +24,7 @@ BC_SINSIN, BC_GAUSS, BC_ZERO = 0, 1, 2
 TAU_ONE, TAU_SCALED = 0, 1
 LAYOUT_NATIVE, LAYOUT_REF_CPU, LAYOUT_REF_GPU = 0, 1, 2
 OP_DR_WEAK, OP_DS_WEAK, OP_LIFT, OP_DR_STRONG, OP_DS_STRONG, OP_MASS, OP_V = range(7)
+MPNN_LOSS_L2, MPNN_LOSS_ENERGY = 0, 1
 PHYSICS = {"advection": ADVECTION, "maxwell_tm": MAXWELL_TM, "maxwell_te": MAXWELL_TE, "laplace": LAPLACE}
 
 
@@ -101,6 +102,12 @@ def lib():
             L.dgc_laplace_apply.argtypes = [_vp, _vp, _vp, _vp]
             L.dgc_laplace_spd_apply.argtypes = [_vp, _vp, _vp, _vp]
             L.dgc_mass_apply.argtypes = [_vp, _vp, _vp, _vp]
+            L.dgc_boundary_nodes.argtypes = [_vp, _dp]
+            L.dgc_write_data_file.argtypes = [C.c_char_p, C.c_int64, _dp, _dp, _dp, C.c_void_p]
+            L.dgc_save_state.argtypes = [_vp, C.c_char_p, _vp, C.c_double, _vp]
+            L.dgc_load_state.argtypes = [_vp, C.c_char_p, _vp, C.POINTER(C.c_double), _vp]
+            L.dgc_grad_apply.argtypes = [_vp, _vp, _vp, _vp, _vp, C.c_double, _vp]
+            L.dgc_div_apply.argtypes = [_vp, _vp, _vp, _vp, _vp, _vp, C.c_double, _vp]
             L.dgc_pcg_solve.argtypes = [_vp, _vp, _vp, C.POINTER(SolveOpts), C.POINTER(SolveStats), _vp]
             L.dgc_block_jacobi.argtypes = [_vp, _vp, _vp]
             L.dgc_num_variants.argtypes = [_vp]
@@ -116,6 +123,19 @@ def lib():
                                                C.c_int, C.c_int, C.POINTER(C.c_int), _vp]
             L.dgc_batch_launch_count.restype = C.c_int64
             L.dgc_batch_launch_count.argtypes = [_vp]
+            L.dgc_mpnn_create.argtypes = [_vp, C.c_int, C.c_uint64, C.POINTER(_vp)]
+            L.dgc_mpnn_destroy.argtypes = [_vp]
+            L.dgc_mpnn_num_params.restype = C.c_int64
+            L.dgc_mpnn_num_params.argtypes = [_vp]
+            L.dgc_mpnn_get_weights.argtypes = [_vp, C.c_void_p]
+            L.dgc_mpnn_set_weights.argtypes = [_vp, C.c_void_p]
+            L.dgc_mpnn_train_step.argtypes = [_vp, _vp, _vp, C.c_int, C.c_float, C.POINTER(C.c_float), _vp, _vp]
+            L.dgc_mpnn_forward.argtypes = [_vp, _vp, _vp, _vp]
+            L.dgc_mpnn_set_loss.argtypes = [_vp, C.c_int]
+            L.dgc_mpnn_precondition.argtypes = [_vp, _vp, _vp, _vp]
+            L.dgc_fpcg_solve.argtypes = [_vp, _vp, _vp, _vp, C.POINTER(SolveOpts), C.POINTER(SolveStats), _vp]
+            L.dgc_learned_solve.argtypes = [_vp, _vp, _vp, _vp, C.POINTER(SolveOpts), C.c_int,
+                                            C.POINTER(SolveStats), C.POINTER(C.c_int), _vp]
             _lib = L
     return _lib
 
@@ -162,6 +182,14 @@ def host_mesh(mesh, order: int):
     nb = C.c_int(0)
     _check(lib().dgc_host_mesh(xy.size // 2, xy, K, cells, order, geom, nbr, C.byref(nb)))
     return geom.reshape(K, 16), nbr.reshape(K, 4), nb.value
+
+
+def write_data_file(path: str, x, y, u, ref=None) -> None:
+    """The reference drivers' visualisation text file (dgc_write_data_file); host arrays."""
+    f = lambda a: np.ascontiguousarray(a, dtype=np.float64).reshape(-1)  # noqa: E731
+    x, y, u = f(x), f(y), f(u)
+    r = None if ref is None else f(ref)
+    _check(lib().dgc_write_data_file(os.fsencode(path), x.size, x, y, u, None if r is None else r.ctypes.data))
 
 
 class Discretization:
@@ -306,6 +334,49 @@ class Discretization:
                                     C.byref(fin), _stream(stream)))
         return qa if fin.value == _ptr(qa) else qb
 
+    # ---------------------------------------------------------------- checkpoints
+    def save_state(self, path: str, q, t: float, stream=None) -> None:
+        _check(lib().dgc_save_state(self._h, os.fsencode(path), _ptr(q), t, _stream(stream)))
+
+    def load_state(self, path: str, q=None, stream=None):
+        """Returns (q, t)."""
+        q = self.empty_state(zero=False) if q is None else q
+        t = C.c_double(0.0)
+        _check(lib().dgc_load_state(self._h, os.fsencode(path), _ptr(q), C.byref(t), _stream(stream)))
+        return q, t.value
+
+    # ---------------------------------------------------------------- grad_2d / div_2d
+    def boundary_nodes(self) -> np.ndarray:
+        """Boundary face node coordinates, (num_boundary_faces * Nfp, 2)."""
+        xy = np.zeros(max(self.info.num_boundary_faces * self.Nfp, 1) * 2)
+        _check(lib().dgc_boundary_nodes(self._h, xy))
+        return xy[:2 * self.info.num_boundary_faces * self.Nfp].reshape(-1, 2)
+
+    @staticmethod
+    def _bdata(g):
+        import torch
+        if g is None:
+            return None, None
+        t = g if isinstance(g, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(g, dtype=np.float64))
+        t = t.to(device="cuda", dtype=torch.float64).contiguous()
+        return t, _ptr(t)
+
+    def grad(self, u, g=None, sign: float = 1.0, out=None, stream=None):
+        """(gx, gy) = weak-form gradient of the scalar field u (central flux); boundary
+        exterior value g[b] + sign * u- at boundary node b."""
+        gx, gy = (self.empty_state(), self.empty_state()) if out is None else out
+        keep, gp = self._bdata(g)
+        _check(lib().dgc_grad_apply(self._h, _ptr(u), _ptr(gx), _ptr(gy), gp, sign, _stream(stream)))
+        return gx, gy
+
+    def div(self, ux, uy, gx=None, gy=None, sign: float = 1.0, out=None, stream=None):
+        """Weak-form divergence of (ux, uy) (central flux)."""
+        out = self.empty_state() if out is None else out
+        kx, px = self._bdata(gx)
+        ky, py = self._bdata(gy)
+        _check(lib().dgc_div_apply(self._h, _ptr(ux), _ptr(uy), _ptr(out), px, py, sign, _stream(stream)))
+        return out
+
     # ---------------------------------------------------------------- laplace_2d
     def laplace(self, u, out=None, stream=None):
         out = self.empty_state() if out is None else out
@@ -388,3 +459,102 @@ class Batch:
 
     def launch_count(self) -> int:
         return int(lib().dgc_batch_launch_count(self._h))
+
+
+class MPNN:
+    """Learned preconditioner of a Dirichlet laplace Discretization: a message-passing
+    network over element adjacency (width 64), BF16 weights, FP32 accumulation,
+    used as M(r) = Binv r + (|r|/c) net(c r/|r|), c = sqrt(K Np), inside truncated
+    flexible CG (dgc_mpnn_*, dgc_fpcg_solve)."""
+
+    WIDTH = 64
+
+    def __init__(self, disc, layers: int = 4, seed: int = 0):
+        self.disc = disc
+        self.layers = layers
+        h = _vp()
+        _check(lib().dgc_mpnn_create(disc._h, layers, seed, C.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().dgc_mpnn_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def num_params(self) -> int:
+        return int(lib().dgc_mpnn_num_params(self._h))
+
+    def set_loss(self, kind: int):
+        """MPNN_LOSS_ENERGY (default: |d|_S^2 / |t|_S^2) or MPNN_LOSS_L2 (|d|^2 / |t|^2)."""
+        _check(lib().dgc_mpnn_set_loss(self._h, kind))
+
+    def get_weights(self) -> np.ndarray:
+        w = np.zeros(self.num_params, dtype=np.float32)
+        _check(lib().dgc_mpnn_get_weights(self._h, w.ctypes.data))
+        return w
+
+    def set_weights(self, w: np.ndarray):
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        assert w.size == self.num_params
+        _check(lib().dgc_mpnn_set_weights(self._h, w.ctypes.data))
+
+    def train_step(self, x, t, lr: float = 0.0, want_grad: bool = False, stream=None):
+        """x, t: device FP32 tensors of S fields (S * K * NpP); returns (loss, grad or None)."""
+        import torch
+        S = x.numel() // (self.disc.K * self.disc.NpP)
+        grad = torch.empty(self.num_params, dtype=torch.float32, device="cuda") if want_grad else None
+        loss = C.c_float()
+        _check(lib().dgc_mpnn_train_step(self._h, _ptr(x), _ptr(t), S, float(lr), C.byref(loss),
+                                         _ptr(grad) if grad is not None else None, _stream(stream)))
+        return float(loss.value), grad
+
+    def forward(self, x, stream=None):
+        import torch
+        y = torch.empty_like(x)
+        _check(lib().dgc_mpnn_forward(self._h, _ptr(x), _ptr(y), _stream(stream)))
+        return y
+
+    def precondition(self, r, stream=None):
+        import torch
+        z = torch.empty_like(r)
+        _check(lib().dgc_mpnn_precondition(self._h, _ptr(r), _ptr(z), _stream(stream)))
+        return z
+
+    def fpcg(self, b, x=None, rtol: float = 1e-10, maxit: int = 20000, window: int = 4, stream=None,
+             check: bool = True):
+        """Truncated flexible CG (window previous directions) on S x = b with this network as
+        preconditioner; returns (x, stats dict)."""
+        import torch
+        x = torch.zeros(self.disc.state_len, dtype=torch.float64, device="cuda") if x is None else x
+        opts = SolveOpts(0, rtol, maxit, 0.0, window, 0)
+        st = SolveStats()
+        rc = lib().dgc_fpcg_solve(self.disc._h, self._h, _ptr(b), _ptr(x), C.byref(opts), C.byref(st),
+                                  _stream(stream))
+        if rc != 0 and not (rc == ERR_NOT_CONVERGED and not check):
+            _check(rc)
+        return x, st.as_dict()
+
+    def solve(self, b, x=None, rtol: float = 1e-10, maxit: int = 100000, fcg_maxit: int = 1000,
+              mode: int = SOLVE_FP64_PCG, window: int = 4, stream=None, check: bool = True):
+        """Learned solve with block-Jacobi PCG (mode) as fallback and judge: flexible CG with
+        this network for at most fcg_maxit iterations, then PCG from the current iterate.
+        Returns (x, stats dict with "fell_back")."""
+        import torch
+        x = torch.zeros(self.disc.state_len, dtype=torch.float64, device="cuda") if x is None else x
+        opts = SolveOpts(mode, rtol, maxit, 1e-4, window, 1)
+        st = SolveStats()
+        fb = C.c_int(0)
+        rc = lib().dgc_learned_solve(self.disc._h, self._h, _ptr(b), _ptr(x), C.byref(opts), fcg_maxit,
+                                     C.byref(st), C.byref(fb), _stream(stream))
+        if rc != 0 and not (rc == ERR_NOT_CONVERGED and not check):
+            _check(rc)
+        d = st.as_dict()
+        d["fell_back"] = bool(fb.value)
+        return x, d

@@ -203,6 +203,29 @@ int dgc_batch_lserk4_run(dgc_batch b, void* const* qa, void* const* qb, void* co
 /* Kernels launched through the batch so far. */
 int64_t dgc_batch_launch_count(dgc_batch b);
 
+/* ---- grad_2d / div_2d (scalar-field handles: advection or laplace) ---------
+ * Boundary data: at boundary face node b the exterior trace is
+ *   u+ = g[b] + sign * u-,
+ * the form of the reference's exterior_val callbacks (e.g. Dirichlet value
+ * g_D: g = 2 g_D, sign = -1; zero jump: g = NULL, sign = +1).  Boundary nodes
+ * are numbered by boundary face (element, then face order) and the face's
+ * node order; g is an FP64 device array of num_boundary_faces * Nfp values. */
+
+/* Coordinates of the boundary face nodes, host array [num_boundary_faces][Nfp][2]. */
+int dgc_boundary_nodes(dgc_handle h, double* xy);
+
+/* Weak-form gradient with the central flux: gx, gy = grad u (replaces
+ * grad_2d::operator(), src/grad_2d.h:141-187, which writes gx over its input).
+ * u, gx, gy: scalar fields in the handle's precision and native layout. */
+int dgc_grad_apply(dgc_handle h, const void* u, void* gx, void* gy, const double* g, double sign,
+                   void* stream);
+
+/* Weak-form divergence with the central flux: out = div (ux, uy) (replaces
+ * div_2d::operator(), src/div_2d.h:148-190); gx, gy the boundary data of the
+ * two components (either may be NULL), one sign for both. */
+int dgc_div_apply(dgc_handle h, const void* ux, const void* uy, void* out, const double* gx, const double* gy,
+                  double sign, void* stream);
+
 /* ---- laplace_2d (DGC_LAPLACE handles; scalar field, native layout) -------- */
 
 /* out = A u, the discrete Laplacian with homogeneous boundary data (all faces
@@ -254,6 +277,82 @@ int dgc_pcg_solve(dgc_handle h, const double* b, double* x, const dgc_solve_opts
 
 /* The block-Jacobi inverse blocks S_kk^-1 (FP64, K x Np x Np, device). */
 int dgc_block_jacobi(dgc_handle h, double* blocks, void* stream);
+
+/* ---- learned preconditioner (no reference counterpart) ---------------------
+ * A message-passing network over element adjacency: per-element DOFs (NpP
+ * values) -> width-W features; L layers h <- h + relu(Ws h + Wn sum_nbr h + b);
+ * -> NpP outputs.  Weights are kept as FP32 masters and BF16 copies; every
+ * contraction reads the BF16 weights and accumulates in FP32.  As a
+ * preconditioner of the SPD form S (dirichlet laplace handles):
+ *   M(r) = Binv r + (|r| / c) net(c r / |r|),   c = sqrt(K Np),
+ * Binv the block-Jacobi inverse (c gives the input unit RMS per node); the
+ * network is trained to predict (e - Binv r) c / |r| from pairs of residuals
+ * r and errors e = x* - x. */
+typedef struct dgc_mpnn_s* dgc_mpnn;
+/* Initialisation from seed (width W = 64, layers L >= 1): Glorot-uniform
+ * hidden weights, zero biases, zero output layer (M starts as block-Jacobi). */
+int dgc_mpnn_create(dgc_handle h, int layers, uint64_t seed, dgc_mpnn* out);
+int dgc_mpnn_destroy(dgc_mpnn m);
+/* Number of parameters; get / set the FP32 master weights (BF16 copies follow). */
+int64_t dgc_mpnn_num_params(dgc_mpnn m);
+int dgc_mpnn_get_weights(dgc_mpnn m, float* host_out);
+int dgc_mpnn_set_weights(dgc_mpnn m, const float* host_in);
+/* Training loss over samples s with d_s = net(x_s) - t_s (padding nodes
+ * excluded):
+ *   DGC_MPNN_LOSS_ENERGY (default): mean_s d_s.S d_s / t_s.S t_s, S the SPD
+ *     laplace form applied in FP32.  For t = (e - Binv r)/|r| this is the
+ *     energy norm of the error left by one step x += M(r) from error e, which
+ *     weights the components a local network can correct;
+ *   DGC_MPNN_LOSS_L2: mean_s |d_s|^2 / |t_s|^2. */
+enum { DGC_MPNN_LOSS_L2 = 0, DGC_MPNN_LOSS_ENERGY = 1 };
+int dgc_mpnn_set_loss(dgc_mpnn m, int kind);
+/* Loss and gradients on `samples` field pairs (device, FP32, native layout,
+ * samples x K x NpP each): x the network inputs, t the targets.  grad_out
+ * (device, num_params floats) receives d loss / d weights (may be NULL);
+ * with lr > 0 one Adam step is applied afterwards (beta1 0.9, beta2 0.999,
+ * eps 1e-8). */
+int dgc_mpnn_train_step(dgc_mpnn m, const float* x, const float* t, int samples, float lr, float* loss,
+                        float* grad_out, void* stream);
+/* y = net(x) for one field (device FP32, K x NpP). */
+int dgc_mpnn_forward(dgc_mpnn m, const float* x, float* y, void* stream);
+/* z = M(r) (device FP64, native layout). */
+int dgc_mpnn_precondition(dgc_mpnn m, const double* r, double* z, void* stream);
+/* Truncated flexible CG (Notay's FCG(m)) on S x = b with M as the
+ * preconditioner, to rtol on the true FP64 residual: each direction is
+ * S-orthogonalised against the previous m, alpha = p.r / p.S p, and an
+ * iteration whose M(r).r <= 0 takes the block-Jacobi direction instead.
+ * The same options and statistics as dgc_pcg_solve; opts->max_outer is the
+ * window m (1..8, 0 = 4); mode, inner_rtol and use_graph are ignored. */
+int dgc_fpcg_solve(dgc_handle h, dgc_mpnn m, const double* b, double* x, const dgc_solve_opts* opts,
+                   dgc_solve_stats* stats, void* stream);
+
+/* Learned solve with block-Jacobi PCG as fallback and judge: dgc_fpcg_solve
+ * for at most fcg_maxit iterations; if that has not reached opts->rtol,
+ * dgc_pcg_solve (opts->mode: FP64 PCG or mixed refinement) continues from the
+ * current iterate with the remaining budget.  Either way the result meets
+ * rtol on the true FP64 residual or DGC_ERR_NOT_CONVERGED is returned.
+ * *fell_back = 1 when the fallback ran; stats->iterations counts both parts,
+ * stats->inner_iterations the flexible-CG part. */
+int dgc_learned_solve(dgc_handle h, dgc_mpnn m, const double* b, double* x, const dgc_solve_opts* opts,
+                      int fcg_maxit, dgc_solve_stats* stats, int* fell_back, void* stream);
+
+/* ---- files ------------------------------------------------------------------ */
+
+/* The reference drivers' visualisation file (Advection2DDataFile.txt,
+ * examples/advection_2d/main.cpp:164-174): "#         x         y         u",
+ * one "x  y  u" line per node (15 significant digits), a blank line, then the
+ * same block of `ref` under "#         x         y         reference solution"
+ * (omitted when ref is NULL).  Host FP64 arrays of n nodes, e.g. one field in
+ * the reference CPU layout with dgc_node_coordinates.  Needs no GPU. */
+int dgc_write_data_file(const char* path, int64_t n, const double* x, const double* y, const double* u,
+                        const double* ref);
+
+/* State checkpoint: a header (discretisation, time t, FNV-1a checksum) and the
+ * device state vector q in the native layout; synchronises the stream.  No
+ * counterpart in the reference.  dgc_load_state rejects files written for
+ * another discretisation or failing the checksum (DGC_ERR_ARG). */
+int dgc_save_state(dgc_handle h, const char* path, const void* q, double t, void* stream);
+int dgc_load_state(dgc_handle h, const char* path, void* q, double* t, void* stream);
 
 /* Synchronise the handle's device status word: DGC_OK, or DGC_ERR_DEVICE if a
  * kernel recorded an error since the last call (the word is then cleared). */
