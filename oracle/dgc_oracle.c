@@ -570,6 +570,77 @@ static void phys_matrix(const orc* o, const double* Dr, const double* Ds, int c,
   for (int i = 0; i < nn; ++i) D[i] = Dr[i] * a + Ds[i] * b;
 }
 
+/* Exterior trace at a face node: the neighbour's node (its face nodes in
+ * reverse order) or, on the boundary, g[b] + sign * interior for boundary
+ * node b -- the form of every exterior_val callback of the reference's
+ * boundary-condition objects (examples/stokes_2d/stokes_2d.h:113-187). */
+static double exterior(const orc* o, const double* u, const double* g, double sign, int c, int e, int d,
+                       double a) {
+  if (o->isB[3 * c + e]) return (g ? g[o->nbF[3 * c + e] + d] : 0.0) + sign * a;
+  int nbc = o->nbC[3 * c + e], nbf = o->nbF[3 * c + e];
+  return u[(size_t)nbc * o->Np + o->Fmask[nbf][o->Nfp - d - 1]];
+}
+
+/* grad_2d::numerical_fluxes + operator() (src/grad_2d.h:94-187): weak-form
+ * gradient with the central flux (u- + u+)/2 projected on the outward normal. */
+void orc_grad(orc* o, const double* u, const double* g, double sign, double* gx, double* gy) {
+  int Np = o->Np, Nfp = o->Nfp, K = o->K;
+  double D[ORC_MAX_NP * ORC_MAX_NP], mFx[3 * ORC_MAX_NFP], mFy[3 * ORC_MAX_NFP];
+  for (int c = 0; c < K; ++c)
+    for (int e = 0; e < 3; ++e)
+      for (int d = 0; d < Nfp; ++d) {
+        double a = u[(size_t)c * Np + o->Fmask[e][d]];
+        o->flux[(size_t)c * 3 * Nfp + e * Nfp + d] = (a + exterior(o, u, g, sign, c, e, d, a)) / 2.0;
+      }
+  for (int c = 0; c < K; ++c) {
+    size_t off = (size_t)c * Np;
+    phys_matrix(o, o->Drw, o->Dsw, c, 0, D);
+    gemv(Np, Np, D, -1.0, u + off, 0.0, gx + off);
+    phys_matrix(o, o->Drw, o->Dsw, c, 1, D);
+    gemv(Np, Np, D, -1.0, u + off, 0.0, gy + off);
+    for (int e = 0; e < 3; ++e) {
+      double fJ = o->faceJ[3 * c + e], nx = o->nx[3 * c + e], ny = o->ny[3 * c + e];
+      for (int i = 0; i < Nfp; ++i) {
+        double F = o->flux[(size_t)c * 3 * Nfp + e * Nfp + i];
+        mFx[e * Nfp + i] = F * nx * fJ;
+        mFy[e * Nfp + i] = F * ny * fJ;
+      }
+    }
+    gemv(Np, 3 * Nfp, o->Lw, 1.0 / o->J[c], mFx, 1.0, gx + off);
+    gemv(Np, 3 * Nfp, o->Lw, 1.0 / o->J[c], mFy, 1.0, gy + off);
+  }
+}
+
+/* div_2d::numerical_fluxes + operator() (src/div_2d.h:94-190): weak-form
+ * divergence with the central flux n.(u- + u+)/2. */
+void orc_div(orc* o, const double* ux, const double* uy, const double* gx, const double* gy, double sign,
+             double* out) {
+  int Np = o->Np, Nfp = o->Nfp, K = o->K;
+  double D[ORC_MAX_NP * ORC_MAX_NP], mF[3 * ORC_MAX_NFP];
+  for (int c = 0; c < K; ++c)
+    for (int e = 0; e < 3; ++e) {
+      double nx = o->nx[3 * c + e], ny = o->ny[3 * c + e];
+      for (int d = 0; d < Nfp; ++d) {
+        size_t ia = (size_t)c * Np + o->Fmask[e][d];
+        double a0 = ux[ia], a1 = uy[ia];
+        double b0 = exterior(o, ux, gx, sign, c, e, d, a0), b1 = exterior(o, uy, gy, sign, c, e, d, a1);
+        o->flux[(size_t)c * 3 * Nfp + e * Nfp + d] = ((a0 + b0) * nx + (a1 + b1) * ny) / 2.0;
+      }
+    }
+  for (int c = 0; c < K; ++c) {
+    size_t off = (size_t)c * Np;
+    phys_matrix(o, o->Drw, o->Dsw, c, 0, D);
+    gemv(Np, Np, D, -1.0, ux + off, 0.0, out + off);
+    phys_matrix(o, o->Drw, o->Dsw, c, 1, D);
+    gemv(Np, Np, D, -1.0, uy + off, 1.0, out + off);
+    for (int e = 0; e < 3; ++e) {
+      double fJ = o->faceJ[3 * c + e];
+      for (int i = 0; i < Nfp; ++i) mF[e * Nfp + i] = o->flux[(size_t)c * 3 * Nfp + e * Nfp + i] * fJ;
+    }
+    gemv(Np, 3 * Nfp, o->Lw, 1.0 / o->J[c], mF, 1.0, out + off);
+  }
+}
+
 /* ------------------------------------------------------------------------- */
 /* Right-hand sides                                                           */
 /* ------------------------------------------------------------------------- */

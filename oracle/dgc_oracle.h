@@ -89,6 +89,11 @@ void orc_laplace_apply(orc* o, int dirichlet, int tau_mode, const double* u, dou
 void orc_spd_apply(orc* o, int tau_mode, const double* u, double* out);
 void orc_spd_diag_blocks(orc* o, int tau_mode, double* blocks);
 void orc_mass_apply(orc* o, const double* f, double* out);
+/* weak-form gradient / divergence with central fluxes (grad_2d, div_2d);
+ * boundary exterior value g[b] + sign * interior at boundary node b (g may be NULL) */
+void orc_grad(orc* o, const double* u, const double* g, double sign, double* gx, double* gy);
+void orc_div(orc* o, const double* ux, const double* uy, const double* gx, const double* gy, double sign,
+             double* out);
 int orc_pcg(orc* o, int tau_mode, const double* b, double* x, double rtol, int maxit,
             double* final_relres);
 

@@ -75,6 +75,8 @@ def lib():
             L.orc_spd_apply.argtypes = [C.c_void_p, C.c_int, _dp, _dp]
             L.orc_spd_diag_blocks.argtypes = [C.c_void_p, C.c_int, _dp]
             L.orc_mass_apply.argtypes = [C.c_void_p, _dp, _dp]
+            L.orc_grad.argtypes = [C.c_void_p, _dp, C.c_void_p, C.c_double, _dp, _dp]
+            L.orc_div.argtypes = [C.c_void_p, _dp, _dp, C.c_void_p, C.c_void_p, C.c_double, _dp]
             L.orc_pcg.restype = C.c_int
             L.orc_pcg.argtypes = [C.c_void_p, C.c_int, _dp, _dp, C.c_double, C.c_int, C.POINTER(C.c_double)]
             _lib = L
@@ -200,6 +202,29 @@ class Oracle:
         u = np.ascontiguousarray(u, dtype=np.float64).reshape(-1)
         out = np.zeros_like(u)
         lib().orc_laplace_apply(self._h, int(dirichlet), tau_mode, u, out)
+        return out
+
+    @staticmethod
+    def _opt(a):
+        return None if a is None else np.ascontiguousarray(a, dtype=np.float64).reshape(-1)
+
+    def grad(self, u: np.ndarray, g=None, sign: float = 1.0):
+        """Weak-form gradient with the central flux (grad_2d); boundary exterior
+        value g[b] + sign * interior at boundary node b.  Returns (gx, gy)."""
+        u = np.ascontiguousarray(u, dtype=np.float64).reshape(-1)
+        g = self._opt(g)
+        gx, gy = np.zeros_like(u), np.zeros_like(u)
+        lib().orc_grad(self._h, u, None if g is None else g.ctypes.data, sign, gx, gy)
+        return gx, gy
+
+    def div(self, ux: np.ndarray, uy: np.ndarray, gx=None, gy=None, sign: float = 1.0) -> np.ndarray:
+        """Weak-form divergence with the central flux (div_2d)."""
+        ux = np.ascontiguousarray(ux, dtype=np.float64).reshape(-1)
+        uy = np.ascontiguousarray(uy, dtype=np.float64).reshape(-1)
+        gx, gy = self._opt(gx), self._opt(gy)
+        out = np.zeros_like(ux)
+        lib().orc_div(self._h, ux, uy, None if gx is None else gx.ctypes.data,
+                      None if gy is None else gy.ctypes.data, sign, out)
         return out
 
     def spd(self, u: np.ndarray, tau_mode: int = 1) -> np.ndarray:

@@ -10,6 +10,8 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <limits>
+#include <sstream>
 #include <string>
 #include <vector>
 
@@ -24,6 +26,8 @@
 #include "poisson_2d.h"
 #include "axpy.h"
 #include "explicit_runge_kutta.h"
+#include "grad_2d.h"
+#include "div_2d.h"
 
 using Mesh = dgc::simple_triangular_mesh_2d<double, int>;
 
@@ -49,6 +53,21 @@ struct dirichlet_all {
   bool is_dirichlet(double, double) const { return true; }
   double exterior_val(double, double, double v) const { return -v; }
   double exterior_grad_n(double, double, double g) const { return g; }
+};
+
+// boundary objects of the form u+ = g(x, y) + sign u- for grad_2d / div_2d
+struct scalar_bc {
+  double sign;
+  double exterior_val(double x, double y, double v) const {
+    return (sign < 0.0 ? 2.0 * std::sin(x) * std::cos(y) : 0.0) + sign * v;
+  }
+};
+struct vector_bc {
+  double exterior_val_x(double x, double y) const { return 2.0 * std::sin(x) * std::cos(y); }
+  double exterior_val_y(double x, double y) const { return 2.0 * x * y; }
+  std::pair<double, double> exterior_val(double x, double y, std::pair<double, double> v) const {
+    return std::make_pair(exterior_val_x(x, y) - v.first, exterior_val_y(x, y) - v.second);
+  }
 };
 
 int main(int argc, char** argv) {
@@ -147,6 +166,24 @@ int main(int argc, char** argv) {
       if (i == 0) putv("adv_rk4_1", u);
     }
     putv("adv_rk4_10", u);
+    // the visualisation file of the advection driver, written by the same
+    // stream statements (examples/advection_2d/main.cpp:164-174) into memory
+    std::vector<double> ref_v(n), px(n), py(n);
+    adv.exact_solution(t, ref_v.begin());
+    for (int i = 0; i < n; ++i) { px[i] = x[i].x(); py[i] = x[i].y(); }
+    putv("adv_x", px); putv("adv_y", py); putv("adv_exact_10", ref_v);
+    std::ostringstream file;
+    file.precision(std::numeric_limits<double>::digits10);
+    file << "#         x         y         u" << std::endl;
+    for (int i = 0; i < n; ++i)
+      file << x[i].x() << "  " << x[i].y() << "  " << u[i] << std::endl;
+    file << std::endl;
+    file << "#         x         y         reference solution" << std::endl;
+    for (int i = 0; i < n; ++i)
+      file << x[i].x() << "  " << x[i].y() << "  " << ref_v[i] << std::endl;
+    const std::string text = file.str();
+    std::vector<int> bytes(text.begin(), text.end());
+    puti("adv_datafile", bytes.data(), bytes.size());
   }
 
   // Maxwell TM cavity
@@ -196,6 +233,29 @@ int main(int argc, char** argv) {
     for (int i = 0; i < n; ++i) u[i] = std::sin(1.3 * i + 0.2) + 0.1 * std::cos(0.7 * i);
     lap(u.begin(), dirichlet_all());
     putv("lap2_out", u);
+  }
+
+  // grad_2d and div_2d (weak form, central fluxes) with boundary data
+  // u+ = 2 g - u- (g = sin x cos y; for div, (sin x cos y, x y)) and u+ = u-
+  {
+    dgc::grad_2d<double, Mesh> gr(*mesh, N);
+    dgc::div_2d<double, Mesh> dv(*mesh, N);
+    std::vector<double> u(n), v(n);
+    for (int i = 0; i < n; ++i) {
+      u[i] = std::sin(0.9 * i + 0.4) + 0.2 * std::cos(1.7 * i);
+      v[i] = std::cos(0.6 * i + 0.1) - 0.3 * std::sin(2.3 * i);
+    }
+    putv("gd_u", u);
+    putv("gd_v", v);
+    for (double sign : {-1.0, 1.0}) {
+      std::vector<double> gx(u), gy(n);
+      gr(gx.begin(), gy.begin(), scalar_bc{sign});
+      putv(sign < 0.0 ? "grad_dir_x" : "grad_mir_x", gx);
+      putv(sign < 0.0 ? "grad_dir_y" : "grad_mir_y", gy);
+    }
+    std::vector<double> d(u), w(v);
+    dv(d.begin(), w.begin(), vector_bc());
+    putv("div_dir", d);
   }
   std::fclose(g_out);
   return 0;

@@ -113,6 +113,24 @@ def test_laplace_apply(golden):
     assert relerr(out, d["lap2_out"]) < 1e-12
 
 
+def boundary_data(o):
+    """The reference harness's boundary functions at the oracle's boundary nodes:
+    grad / div exterior values 2 g - u with g = sin x cos y (and x y for div)."""
+    a = o.arrays()
+    bx, by = a["bx"], a["by"]
+    return 2 * np.sin(bx) * np.cos(by), 2 * bx * by
+
+
+def test_grad_and_div(golden):
+    N, d, o = golden
+    gs, gv = boundary_data(o)
+    gx, gy = o.grad(d["gd_u"], gs, -1.0)
+    assert relerr(gx, d["grad_dir_x"]) < 1e-12 and relerr(gy, d["grad_dir_y"]) < 1e-12
+    gx, gy = o.grad(d["gd_u"], None, 1.0)
+    assert relerr(gx, d["grad_mir_x"]) < 1e-12 and relerr(gy, d["grad_mir_y"]) < 1e-12
+    assert relerr(o.div(d["gd_u"], d["gd_v"], gs, gv, -1.0), d["div_dir"]) < 1e-12
+
+
 def test_known_answers_coarse_mesh():
     """The reference drivers' error norms on its own coarse mesh (K = 16)."""
     with open(os.path.join(GOLDEN, "ref_known_answers.json")) as f:
