@@ -103,6 +103,17 @@ def lib():
             L.dgc_laplace_spd_apply.argtypes = [_vp, _vp, _vp, _vp]
             L.dgc_mass_apply.argtypes = [_vp, _vp, _vp, _vp]
             L.dgc_boundary_nodes.argtypes = [_vp, _dp]
+            L.dgc_adv1d_create.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(_vp)]
+            L.dgc_adv1d_destroy.argtypes = [_vp]
+            L.dgc_adv1d_info.argtypes = [_vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+            L.dgc_adv1d_node_x.argtypes = [_vp, _dp]
+            L.dgc_adv1d_get_operator.argtypes = [_vp, C.c_int, _dp]
+            L.dgc_adv1d_rhs.argtypes = [_vp, _vp, C.c_double, _vp, _vp]
+            L.dgc_adv1d_rk4_step.argtypes = [_vp, _vp, C.c_double, C.c_double, C.POINTER(_vp), _vp]
+            L.dgc_adv1d_launch_count.restype = C.c_int64
+            L.dgc_adv1d_launch_count.argtypes = [_vp]
+            L.dgc_msh_read.argtypes = [C.c_char_p, C.POINTER(C.c_int), C.c_void_p, C.POINTER(C.c_int), C.c_void_p]
+            L.dgc_msh_write.argtypes = [C.c_char_p, C.c_int, _dp, C.c_int, _ip, C.c_int]
             L.dgc_write_data_file.argtypes = [C.c_char_p, C.c_int64, _dp, _dp, _dp, C.c_void_p]
             L.dgc_save_state.argtypes = [_vp, C.c_char_p, _vp, C.c_double, _vp]
             L.dgc_load_state.argtypes = [_vp, C.c_char_p, _vp, C.POINTER(C.c_double), _vp]
@@ -182,6 +193,23 @@ def host_mesh(mesh, order: int):
     nb = C.c_int(0)
     _check(lib().dgc_host_mesh(xy.size // 2, xy, K, cells, order, geom, nbr, C.byref(nb)))
     return geom.reshape(K, 16), nbr.reshape(K, 4), nb.value
+
+
+def read_msh(path: str):
+    """Triangle mesh of a Gmsh MSH 4 file (dgc_msh_read) as a meshes.Mesh."""
+    nv, K = C.c_int(0), C.c_int(0)
+    _check(lib().dgc_msh_read(os.fsencode(path), C.byref(nv), None, C.byref(K), None))
+    xy = np.zeros(2 * max(nv.value, 1))
+    cells = np.zeros(3 * max(K.value, 1), np.int32)
+    _check(lib().dgc_msh_read(os.fsencode(path), C.byref(nv), xy.ctypes.data, C.byref(K), cells.ctypes.data))
+    return meshes.Mesh(xy=xy[:2 * nv.value].reshape(-1, 2), cells=cells[:3 * K.value].reshape(-1, 3))
+
+
+def write_msh(path: str, mesh, digits: int = 0) -> None:
+    """MSH 4.1 file of a triangle mesh (dgc_msh_write); digits 0 = the reference's 6."""
+    xy = np.ascontiguousarray(mesh.xy, dtype=np.float64).reshape(-1)
+    cells = np.ascontiguousarray(mesh.cells, dtype=np.int32).reshape(-1)
+    _check(lib().dgc_msh_write(os.fsencode(path), xy.size // 2, xy, cells.size // 3, cells, digits))
 
 
 def write_data_file(path: str, x, y, u, ref=None) -> None:
@@ -411,6 +439,67 @@ class Discretization:
         if rc != 0 and not (rc == ERR_NOT_CONVERGED and not check):
             _check(rc)
         return x, st.as_dict()
+
+
+class Advection1D:
+    """The 1D advection example (dgc_adv1d_*): K cells of order N on [0, 2 pi];
+    device state [cell][node] in the given precision."""
+
+    def __init__(self, num_cells: int, order: int, precision: int = F64):
+        h = _vp()
+        _check(lib().dgc_adv1d_create(num_cells, order, precision, C.byref(h)))
+        self._h = h
+        self.K, self.N, self.np, self.precision = num_cells, order, order + 1, precision
+        hh, c = C.c_double(), C.c_double()
+        _check(lib().dgc_adv1d_info(self._h, C.byref(hh), C.byref(c)))
+        self.min_elem_size, self.wave_speed = hh.value, c.value
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().dgc_adv1d_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def torch_dtype(self):
+        import torch
+        return torch.float64 if self.precision == F64 else torch.float32
+
+    def node_x(self) -> np.ndarray:
+        x = np.zeros(self.K * self.np)
+        _check(lib().dgc_adv1d_node_x(self._h, x))
+        return x
+
+    def operator(self, which: int) -> np.ndarray:
+        out = np.zeros(self.np * self.np)
+        _check(lib().dgc_adv1d_get_operator(self._h, which, out))
+        return out.reshape(self.np, self.np)
+
+    def upload(self, u):
+        import torch
+        return torch.from_numpy(np.ascontiguousarray(u, dtype=np.float64).reshape(-1)).to(self.torch_dtype).cuda()
+
+    def empty_state(self):
+        import torch
+        return torch.zeros(self.K * self.np, dtype=self.torch_dtype, device="cuda")
+
+    def rhs(self, q, t: float, out=None, stream=None):
+        out = self.empty_state() if out is None else out
+        _check(lib().dgc_adv1d_rhs(self._h, _ptr(q), t, _ptr(out), _stream(stream)))
+        return out
+
+    def rk4_step(self, q, t: float, dt: float, work, stream=None):
+        arr = (_vp * 3)(*[_ptr(w) for w in work])
+        _check(lib().dgc_adv1d_rk4_step(self._h, _ptr(q), t, dt, arr, _stream(stream)))
+        return q
+
+    def launch_count(self) -> int:
+        return int(lib().dgc_adv1d_launch_count(self._h))
 
 
 class Batch:

@@ -336,6 +336,29 @@ int dgc_fpcg_solve(dgc_handle h, dgc_mpnn m, const double* b, double* x, const d
 int dgc_learned_solve(dgc_handle h, dgc_mpnn m, const double* b, double* x, const dgc_solve_opts* opts,
                       int fcg_maxit, dgc_solve_stats* stats, int* fell_back, void* stream);
 
+/* ---- the 1D advection example (examples/advection_1d) ---------------------
+ * u_t + c u_x = 0 on [0, 2 pi], c = 2 pi, K equal cells of N+1 Gauss-Lobatto
+ * nodes, upwind flux, inflow u(0, t) = -sin(2 pi t), outflow extrapolation
+ * (advection_1d.h:37-196).  State: device vector [cell][node] (the
+ * reference's CPU layout), K (N+1) values in the handle's precision. */
+typedef struct dgc_adv1d_s* dgc_adv1d;
+/* Replaces advection_1d(numCells, order) and create_device_object
+ * (examples/advection_1d/k_advection_1d.cu).  order in [1, 8]. */
+int dgc_adv1d_create(int num_cells, int order, int precision, dgc_adv1d* out);
+int dgc_adv1d_destroy(dgc_adv1d a);
+/* min_elem_size() and wave_speed() of the reference class. */
+int dgc_adv1d_info(dgc_adv1d a, double* min_elem_size, double* wave_speed);
+/* Node positions, host array [cell][node] (initialize_dofs). */
+int dgc_adv1d_node_x(dgc_adv1d a, double* x);
+/* Host copy of m_D (which = 0) or m_L (which = 1), (N+1) x (N+1) row-major. */
+int dgc_adv1d_get_operator(dgc_adv1d a, int which, double* out);
+/* out = L_h(q, t) (advection_1d::operator()). */
+int dgc_adv1d_rhs(dgc_adv1d a, const void* q, double t, void* out, void* stream);
+/* One classical RK4 step in place on q in 4 fused launches (dgc::rk4 with
+ * the operator and 8 axpy calls).  work: 3 state vectors of scratch. */
+int dgc_adv1d_rk4_step(dgc_adv1d a, void* q, double t, double dt, void* const* work, void* stream);
+int64_t dgc_adv1d_launch_count(dgc_adv1d a);
+
 /* ---- files ------------------------------------------------------------------ */
 
 /* The reference drivers' visualisation file (Advection2DDataFile.txt,
@@ -346,6 +369,20 @@ int dgc_learned_solve(dgc_handle h, dgc_mpnn m, const double* b, double* x, cons
  * the reference CPU layout with dgc_node_coordinates.  Needs no GPU. */
 int dgc_write_data_file(const char* path, int64_t n, const double* x, const double* y, const double* u,
                         const double* ref);
+
+/* Gmsh MSH 4 ASCII import (replaces gmsh_importer_exporter::
+ * import_triangle_mesh_2d, src/mesh/gmsh_importer_exporter.h:49-167): the
+ * triangles (element type 2) and node coordinates, node tags shifted by the
+ * smallest tag, as dgc_create takes them.  Call with vertex_xy = cells = NULL
+ * to get the counts; then with arrays whose capacities (vertices, cells) are
+ * passed in *num_vertices / *num_cells.  Node tags must run contiguously in
+ * file order (the reference assumes it; this reader checks). */
+int dgc_msh_read(const char* path, int* num_vertices, double* vertex_xy, int* num_cells, int32_t* cells);
+/* MSH 4.1 export (replaces export_triangle_mesh_2d, same file:191-213);
+ * digits = significant digits of the coordinates, 0 = 6 as the reference
+ * writes them (17 round-trips exactly). */
+int dgc_msh_write(const char* path, int num_vertices, const double* vertex_xy, int num_cells, const int32_t* cells,
+                  int digits);
 
 /* State checkpoint: a header (discretisation, time t, FNV-1a checksum) and the
  * device state vector q in the native layout; synchronises the stream.  No

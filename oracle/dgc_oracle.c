@@ -1033,3 +1033,111 @@ int orc_pcg(orc* o, int tau_mode, const double* b, double* x, double rtol, int m
   free(blk); free(binv); free(r); free(z); free(p); free(Ap);
   return conv ? it : -1;
 }
+
+/* ------------------------------------------------------------------------- */
+/* 1D advection: examples/advection_1d/advection_1d.h (u_t + c u_x = 0 on     */
+/* [0, 2 pi], c = 2 pi, K cells of N+1 Gauss-Lobatto nodes, strong form,      */
+/* upwind flux, inflow u(0, t) = -sin(2 pi t), outflow extrapolation).        */
+/* ------------------------------------------------------------------------- */
+struct orc1d {
+  int K, N, np;
+  double h, c;
+  double D[(ORC_MAX_ORDER + 1) * (ORC_MAX_ORDER + 1)], L[(ORC_MAX_ORDER + 1) * (ORC_MAX_ORDER + 1)];
+  double xr[ORC_MAX_ORDER + 1];
+  double* flux;
+  double* w[5];
+};
+
+/* advection_1d.h:91-104: V(i,j) = P_j(x_i), Dr = Vr V^-1, D = Dr 2/h, L = V V^T 2/h */
+orc1d* orc1d_create(int K, int N) {
+  if (K < 1 || N < 1 || N > ORC_MAX_ORDER) return NULL;
+  orc1d* o = calloc(1, sizeof(orc1d));
+  o->K = K; o->N = N; o->np = N + 1;
+  o->c = 2.0 * M_PI;
+  o->h = 2.0 * M_PI / K;
+  int np = o->np;
+  orc_gl_points(np, o->xr);
+  double V[(ORC_MAX_ORDER + 1) * (ORC_MAX_ORDER + 1)], Vr[(ORC_MAX_ORDER + 1) * (ORC_MAX_ORDER + 1)];
+  double Vi[(ORC_MAX_ORDER + 1) * (ORC_MAX_ORDER + 1)], Dr[(ORC_MAX_ORDER + 1) * (ORC_MAX_ORDER + 1)];
+  double VT[(ORC_MAX_ORDER + 1) * (ORC_MAX_ORDER + 1)], Mi[(ORC_MAX_ORDER + 1) * (ORC_MAX_ORDER + 1)];
+  for (int i = 0; i < np; ++i)
+    for (int j = 0; j < np; ++j) {
+      V[i * np + j] = orc_jacobi_p(0.0, 0.0, j, o->xr[i]);
+      Vr[i * np + j] = orc_jacobi_dp(0.0, 0.0, j, o->xr[i]);
+    }
+  orc_mat_inverse(np, V, Vi);
+  mat_mul(np, np, np, Vr, Vi, Dr);
+  mat_transpose(np, np, V, VT);
+  mat_mul(np, np, np, V, VT, Mi);
+  for (int i = 0; i < np * np; ++i) {
+    o->D[i] = Dr[i] * (2.0 / o->h);
+    o->L[i] = Mi[i] * (2.0 / o->h);
+  }
+  o->flux = calloc((size_t)K + 1, 8);
+  for (int i = 0; i < 5; ++i) o->w[i] = calloc((size_t)K * np, 8);
+  return o;
+}
+
+void orc1d_destroy(orc1d* o) {
+  if (!o) return;
+  free(o->flux);
+  for (int i = 0; i < 5; ++i) free(o->w[i]);
+  free(o);
+}
+
+void orc1d_operators(const orc1d* o, double* D, double* L) {
+  memcpy(D, o->D, sizeof(double) * o->np * o->np);
+  memcpy(L, o->L, sizeof(double) * o->np * o->np);
+}
+
+/* advection_1d.h:107-146: x = i h + (1 + r_j) h / 2, [cell][node] */
+void orc1d_node_x(const orc1d* o, double* x) {
+  for (int i = 0; i < o->K; ++i)
+    for (int j = 0; j < o->np; ++j) x[(size_t)i * o->np + j] = i * o->h + (1.0 + o->xr[j]) * 0.5 * o->h;
+}
+
+void orc1d_exact(const orc1d* o, double t, double* u) {
+  for (int i = 0; i < o->K; ++i)
+    for (int j = 0; j < o->np; ++j) {
+      double x = i * o->h + (1.0 + o->xr[j]) * 0.5 * o->h;
+      u[(size_t)i * o->np + j] = sin(x - o->c * t);
+    }
+}
+
+/* advection_1d.h:148-196 (alpha = 0: upwind) */
+void orc1d_rhs(orc1d* o, double t, const double* u, double* out) {
+  int np = o->np, K = o->K;
+  double c = o->c;
+  for (int i = 0; i <= K; ++i) {
+    double a = i > 0 ? u[(size_t)i * np - 1] : -sin(2.0 * M_PI * t);
+    double b = i < K ? u[(size_t)i * np] : u[(size_t)i * np - 1];
+    o->flux[i] = c * 0.5 * (a + b) + c * 0.5 * (1.0 - 0.0) * (a - b);
+  }
+  double in[ORC_MAX_ORDER + 1], ov[ORC_MAX_ORDER + 1];
+  for (int k = 0; k < K; ++k) {
+    size_t off = (size_t)k * np;
+    gemv(np, np, o->D, -c, u + off, 0.0, out + off);
+    for (int j = 0; j < np; ++j) { in[j] = 0.0; ov[j] = 0.0; }
+    in[0] = o->flux[k] - c * u[off];
+    in[np - 1] = c * u[off + np - 1] - o->flux[k + 1];
+    gemv(np, np, o->L, 1.0, in, 1.0, ov);
+    for (int j = 0; j < np; ++j) out[off + j] += ov[j];
+  }
+}
+
+/* explicit_runge_kutta.h:33-51 with axpy_n (axpy.h:112-122) */
+void orc1d_rk4_step(orc1d* o, double t, double dt, double* u) {
+  size_t n = (size_t)o->K * o->np;
+  double **w = o->w;
+  orc1d_rhs(o, t, u, w[1]);
+  axpy_n(0.5 * dt, w[1], n, u, w[0]);
+  orc1d_rhs(o, t + 0.5 * dt, w[0], w[2]);
+  axpy_n(0.5 * dt, w[2], n, u, w[0]);
+  orc1d_rhs(o, t + 0.5 * dt, w[0], w[3]);
+  axpy_n(dt, w[3], n, u, w[0]);
+  orc1d_rhs(o, t + dt, w[0], w[4]);
+  axpy_n(2.0, w[2], n, w[1], w[0]);
+  axpy_n(2.0, w[3], n, w[4], w[1]);
+  axpy_n(dt / 6.0, w[0], n, u, w[2]);
+  axpy_n(dt / 6.0, w[1], n, w[2], u);
+}

@@ -97,6 +97,16 @@ void orc_div(orc* o, const double* ux, const double* uy, const double* gx, const
 int orc_pcg(orc* o, int tau_mode, const double* b, double* x, double rtol, int maxit,
             double* final_relres);
 
+/* 1D advection (examples/advection_1d/advection_1d.h) */
+typedef struct orc1d orc1d;
+orc1d* orc1d_create(int K, int N);
+void orc1d_destroy(orc1d* o);
+void orc1d_operators(const orc1d* o, double* D, double* L);
+void orc1d_node_x(const orc1d* o, double* x);
+void orc1d_exact(const orc1d* o, double t, double* u);
+void orc1d_rhs(orc1d* o, double t, const double* u, double* out);
+void orc1d_rk4_step(orc1d* o, double t, double dt, double* u);
+
 #ifdef __cplusplus
 }
 #endif

@@ -79,6 +79,14 @@ def lib():
             L.orc_div.argtypes = [C.c_void_p, _dp, _dp, C.c_void_p, C.c_void_p, C.c_double, _dp]
             L.orc_pcg.restype = C.c_int
             L.orc_pcg.argtypes = [C.c_void_p, C.c_int, _dp, _dp, C.c_double, C.c_int, C.POINTER(C.c_double)]
+            L.orc1d_create.restype = C.c_void_p
+            L.orc1d_create.argtypes = [C.c_int, C.c_int]
+            L.orc1d_destroy.argtypes = [C.c_void_p]
+            L.orc1d_operators.argtypes = [C.c_void_p, _dp, _dp]
+            L.orc1d_node_x.argtypes = [C.c_void_p, _dp]
+            L.orc1d_exact.argtypes = [C.c_void_p, C.c_double, _dp]
+            L.orc1d_rhs.argtypes = [C.c_void_p, C.c_double, _dp, _dp]
+            L.orc1d_rk4_step.argtypes = [C.c_void_p, C.c_double, C.c_double, _dp]
             _lib = L
     return _lib
 
@@ -250,6 +258,54 @@ class Oracle:
         rel = C.c_double(0.0)
         it = lib().orc_pcg(self._h, tau_mode, b, x, rtol, maxit, C.byref(rel))
         return x, it, rel.value
+
+
+class Oracle1D:
+    """The 1D advection example (examples/advection_1d/advection_1d.h) on K cells
+    of order N; fields in the reference CPU layout [cell][node]."""
+
+    def __init__(self, K: int, N: int):
+        self._h = lib().orc1d_create(K, N)
+        if not self._h:
+            raise ValueError("orc1d_create rejected the arguments")
+        self.K, self.N, self.np = K, N, N + 1
+        self.h = 2.0 * np.pi / K
+        self.c = 2.0 * np.pi
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().orc1d_destroy(self._h)
+            self._h = None
+
+    def operators(self):
+        D = np.zeros(self.np * self.np)
+        L = np.zeros(self.np * self.np)
+        lib().orc1d_operators(self._h, D, L)
+        return D.reshape(self.np, self.np), L.reshape(self.np, self.np)
+
+    def node_x(self):
+        x = np.zeros(self.K * self.np)
+        lib().orc1d_node_x(self._h, x)
+        return x
+
+    def exact(self, t: float):
+        u = np.zeros(self.K * self.np)
+        lib().orc1d_exact(self._h, t, u)
+        return u
+
+    def rhs(self, u, t: float):
+        u = np.ascontiguousarray(u, dtype=np.float64).reshape(-1)
+        out = np.zeros_like(u)
+        lib().orc1d_rhs(self._h, t, u, out)
+        return out
+
+    def rk4(self, u, t0: float, dt: float, nsteps: int):
+        u = np.array(u, dtype=np.float64).reshape(-1)
+        t = t0
+        for _ in range(nsteps):
+            lib().orc1d_rk4_step(self._h, t, dt, u)
+            t += dt
+        return u
 
 
 def lserk4_coeffs():

@@ -3,7 +3,7 @@
 // oracle/Makefile against the reference sources; its outputs become the golden
 // vectors under tests/golden/ that pin the oracle restatement.
 //
-// usage: ref_dump (--msh file.msh | --bin mesh.bin) order out.bin
+// usage: ref_dump (--msh file.msh | --bin mesh.bin) order out.bin [export.msh]
 //   mesh.bin: int32 nv, f64 xy[2 nv], int32 K, int32 cells[3 K]
 #include <cmath>
 #include <cstdint>
@@ -258,5 +258,7 @@ int main(int argc, char** argv) {
     putv("div_dir", d);
   }
   std::fclose(g_out);
+  // optional: the mesh written back by the reference's MSH exporter
+  if (argc > 5) dgc::gmsh_importer_exporter<double, int>::export_triangle_mesh_2d(*mesh, argv[5]);
   return 0;
 }

@@ -8,7 +8,12 @@ they compute as compressed .npz files:
   ref_<mesh>_N<order>.npz   reference-element matrices, discretisation arrays,
                             one RHS and 1 / 10 classical-RK4 steps of the
                             advection (a = (1,1)) and TM-Maxwell examples, one
-                            laplace_2d apply (homogeneous Dirichlet, tau = 1)
+                            laplace_2d apply (homogeneous Dirichlet, tau = 1),
+                            grad_2d / div_2d applies, the advection driver's
+                            visualisation file, and the MSH text of the mesh
+                            (the reference's input file and its exporter's output)
+  ref_adv1d_K<K>_N<N>.npz   the 1D advection example: operators, RHS, RK4 states
+                            and the driver's error norm
   ref_known_answers.json    mean-square nodal errors of the reference drivers'
                             runs on the reference's coarse mesh (10000 RK4
                             steps of advection, Maxwell to T = 1)
@@ -67,16 +72,33 @@ def main() -> None:
         four = os.path.join(ref, "tests", "square_domain_4cells.msh")
         for N in (1, 2, 3):
             cases.append(("cells4", ["--msh", four], N))
+        cases.append(("fine", ["--msh", os.path.join(ref, "examples", "square_domain_fine.msh")], 1))
         coarse_bin = None
         for name, src, N in cases:
             out = os.path.join(tmp, f"{name}_{N}.bin")
-            subprocess.run([dump, *src, str(N), out], check=True)
+            exp = os.path.join(tmp, f"{name}_{N}.msh")
+            subprocess.run([dump, *src, str(N), out, exp], check=True)
             d = read_dump(out)
+            d["adv_datafile"] = d["adv_datafile"].astype(np.uint8)   # text, one byte per character
+            # MSH fixtures: the reference's input file (when there is one) and the
+            # reference exporter's output for this mesh, as byte arrays
+            d["msh_export"] = np.frombuffer(open(exp, "rb").read(), dtype=np.uint8)
+            if src[0] == "--msh":
+                d["msh_source"] = np.frombuffer(open(src[1], "rb").read(), dtype=np.uint8)
             np.savez_compressed(os.path.join(HERE, f"ref_{name}_N{N}.npz"), **d)
             if name == "coarse" and coarse_bin is None:
                 coarse_bin = os.path.join(tmp, "coarse.bin")
                 m = meshes.Mesh(xy=d["mesh_xy"].reshape(-1, 2), cells=d["mesh_cells"].reshape(-1, 3))
                 meshes.write_bin(m, coarse_bin)
+        # 1D advection (examples/advection_1d): operators, states after 1 / 10
+        # steps; K = 512, N = 6 also after the driver's 10000 steps
+        adv1d = os.path.join(oracle_dir, "_ref", "ref_adv1d")
+        for K1, N1, steps in ((8, 1, 10), (16, 2, 10), (48, 3, 10), (32, 4, 10), (24, 5, 10), (64, 6, 10),
+                              (512, 6, 10000)):
+            out = os.path.join(tmp, f"adv1d_{K1}_{N1}.bin")
+            subprocess.run([adv1d, str(K1), str(N1), out, str(steps)], check=True)
+            np.savez_compressed(os.path.join(HERE, f"ref_adv1d_K{K1}_N{N1}.npz"), steps=np.array([steps]),
+                                **read_dump(out))
         known = {"advection_10000_steps": {}, "maxwell_T1": {}}
         for N in range(1, 5):
             r = subprocess.run([timer, coarse_bin, str(N), "adv", "10000"], check=True,

@@ -34,10 +34,19 @@ def built():
 
 
 def golden_mesh(d):
+    """The case's mesh; read from the reference's own .msh file by dgc_msh_read
+    when the case has one (so those cases also test the importer end to end)."""
+    if "msh_source" in d.files:
+        import tempfile
+        with tempfile.TemporaryDirectory() as tmp:
+            path = os.path.join(tmp, "mesh.msh")
+            with open(path, "wb") as f:
+                f.write(bytes(d["msh_source"]))
+            return dg.read_msh(path)
     return meshes.Mesh(xy=d["mesh_xy"].reshape(-1, 2), cells=d["mesh_cells"].reshape(-1, 3))
 
 
-CASES = [f"{m}_N{n}" for m in ("jit4", "coarse") for n in range(1, 7)]
+CASES = [f"{m}_N{n}" for m in ("jit4", "coarse") for n in range(1, 7)] + ["fine_N1"]
 
 
 @pytest.mark.parametrize("case", CASES)
