@@ -12,6 +12,7 @@
 
 #include "dgc_internal.hpp"
 #include "ipdg.cuh"
+#include "ipdg_blk.cuh"
 
 namespace dgk {
 
@@ -54,6 +55,69 @@ cudaError_t ipdg_launch_n(int kind, const IpdgParams& p, int sm, cudaStream_t s)
   if (grid > ntiles) grid = ntiles;
   void* args[] = {const_cast<IpdgParams*>(&p)};
   return cudaLaunchKernel(fn, dim3(grid), dim3(256), args, smem, s);
+}
+
+// register-blocked FP32 CG kernels
+enum IpdgBlkKernel : int { IB_GRAD = 0, IB_DIV = 1, IB_UPDATE = 2 };
+
+template <int N>
+cudaError_t ipdg_blk_launch_n(int kind, const IpdgParams& p, int sm, cudaStream_t s) {
+  using B = IpdgBlk<N>;
+  static std::once_flag once[3];
+  static int bps[3];
+  static cudaError_t st[3];
+  const void* fn = kind == IB_GRAD ? (const void*)ipdg_grad_blk_kernel<N>
+                   : kind == IB_DIV ? (const void*)ipdg_div_blk_kernel<N>
+                                    : (const void*)pcg_update_blk_kernel<N>;
+  const int smem = (int)(kind == IB_GRAD ? B::kSmemGrad : kind == IB_DIV ? B::kSmemDiv : B::kSmemUpd);
+  std::call_once(once[kind], [&] {
+    st[kind] = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    // all of the unified L1 / shared storage as shared memory, so residency is
+    // set by registers (64 per thread: 4 CTAs of 256) rather than the carveout
+    if (st[kind] == cudaSuccess)
+      st[kind] = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    if (st[kind] == cudaSuccess)
+      st[kind] = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps[kind], fn, 256, smem);
+  });
+  if (st[kind] != cudaSuccess) return st[kind];
+  const int ntiles = (p.K + B::TE - 1) / B::TE;
+  int grid = sm * (bps[kind] > 0 ? bps[kind] : 1);
+  if (grid > ntiles) grid = ntiles;
+  void* args[] = {const_cast<IpdgParams*>(&p)};
+  return cudaLaunchKernel(fn, dim3(grid), dim3(256), args, smem, s);
+}
+
+cudaError_t ipdg_blk_launch(int N, int kind, const IpdgParams& p, int sm, cudaStream_t s) {
+  switch (N) {
+    case 1: return ipdg_blk_launch_n<1>(kind, p, sm, s);
+    case 2: return ipdg_blk_launch_n<2>(kind, p, sm, s);
+    case 3: return ipdg_blk_launch_n<3>(kind, p, sm, s);
+    case 4: return ipdg_blk_launch_n<4>(kind, p, sm, s);
+    case 5: return ipdg_blk_launch_n<5>(kind, p, sm, s);
+    case 6: return ipdg_blk_launch_n<6>(kind, p, sm, s);
+    case 7: return ipdg_blk_launch_n<7>(kind, p, sm, s);
+    case 8: return ipdg_blk_launch_n<8>(kind, p, sm, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t pack_binv(int N, int K, const double* binv, int bstr, float* out, cudaStream_t s) {
+  auto go = [&](auto kern, int pk) {
+    const int64_t n = (int64_t)K * pk;
+    kern<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(K, binv, bstr, out);
+    return cudaGetLastError();
+  };
+  switch (N) {
+    case 1: return go(pack_binv_kernel<1>, IpdgBlk<1>::PK);
+    case 2: return go(pack_binv_kernel<2>, IpdgBlk<2>::PK);
+    case 3: return go(pack_binv_kernel<3>, IpdgBlk<3>::PK);
+    case 4: return go(pack_binv_kernel<4>, IpdgBlk<4>::PK);
+    case 5: return go(pack_binv_kernel<5>, IpdgBlk<5>::PK);
+    case 6: return go(pack_binv_kernel<6>, IpdgBlk<6>::PK);
+    case 7: return go(pack_binv_kernel<7>, IpdgBlk<7>::PK);
+    case 8: return go(pack_binv_kernel<8>, IpdgBlk<8>::PK);
+    default: return cudaErrorInvalidValue;
+  }
 }
 
 template <typename R>
@@ -153,6 +217,9 @@ struct IpdgState {
   bool ready = false;          // preconditioner built
   double* binv64 = nullptr;
   float* binv32 = nullptr;
+  float* binv_pk32 = nullptr;  // [K][PK] packed upper triangles (register-blocked FP32 CG)
+  float* ops_blk32 = nullptr;  // rows Dr^T | Ds^T | LIFT^T, strong form, padded to NpP columns
+  float* mass_blk32 = nullptr; // rows of M padded to NpP columns
   void* mass64 = nullptr;      // padded M in FP64 / FP32
   void* mass32 = nullptr;
   double* dense64 = nullptr;   // row-major Dr | Ds | L | M (FP64) for the block set-up
@@ -193,6 +260,9 @@ dgk::IpdgParams base(const dgc_handle_s* h) {
   p.mats = sizeof(R) == 8 ? h->d_mats64[1] : h->d_mats32[1];
   p.mass = sizeof(R) == 8 ? h->ipdg->mass64 : h->ipdg->mass32;
   p.binv = sizeof(R) == 8 ? (const void*)h->ipdg->binv64 : (const void*)h->ipdg->binv32;
+  p.mats_blk = h->ipdg->ops_blk32;
+  p.mass_blk = h->ipdg->mass_blk32;
+  p.binv_pk = h->ipdg->binv_pk32;
   p.status = h->d_status;
   return p;
 }
@@ -232,7 +302,9 @@ int ipdg_build_preconditioner(dgc_handle_s* h, cudaStream_t s) {
                                    st->dense64 + (size_t)2 * h->Np * h->Np + (size_t)h->Np * 3 * h->Nfp,
                                    st->binv64, st->binv32, st->bstr, h->d_status, s);
   if (e != cudaSuccess) return cuda_err(e, "block-Jacobi set-up");
-  h->launches += 2;
+  e = dgk::pack_binv(h->N, h->K, st->binv64, st->bstr, st->binv_pk32, s);
+  if (e != cudaSuccess) return cuda_err(e, "block-Jacobi packing");
+  h->launches += 3;
   st->ready = true;
   return DGC_OK;
 }
@@ -280,6 +352,20 @@ int upload_ipdg_matrices(dgc_handle_s* h) {
   dense.insert(dense.end(), h->re.M.begin(), h->re.M.end());
   (void)NF;
   CKI(cudaMemcpy(st->dense64, dense.data(), dense.size() * 8, cudaMemcpyHostToDevice));
+  // register-blocked operands: row j of Dr^T, Ds^T (j < Np), row m of LIFT^T and
+  // row j of M, each padded with zeros to NpP columns
+  const int NpP = h->NpP;
+  std::vector<float> ob((size_t)(2 * Np + NF) * NpP, 0.0f), mb((size_t)Np * NpP, 0.0f);
+  for (int j = 0; j < Np; ++j)
+    for (int i = 0; i < Np; ++i) {
+      ob[(size_t)j * NpP + i] = (float)h->re.Drs[(size_t)i * Np + j];
+      ob[(size_t)(Np + j) * NpP + i] = (float)h->re.Dss[(size_t)i * Np + j];
+      mb[(size_t)j * NpP + i] = (float)h->re.M[(size_t)j * Np + i];
+    }
+  for (int m = 0; m < NF; ++m)
+    for (int i = 0; i < Np; ++i) ob[(size_t)(2 * Np + m) * NpP + i] = (float)h->re.Ls[(size_t)i * NF + m];
+  CKI(cudaMemcpy(st->ops_blk32, ob.data(), ob.size() * 4, cudaMemcpyHostToDevice));
+  CKI(cudaMemcpy(st->mass_blk32, mb.data(), mb.size() * 4, cudaMemcpyHostToDevice));
   st->ready = false;
   return DGC_OK;
 }
@@ -305,6 +391,11 @@ int ipdg_init(dgc_handle_s* h) {
   CKI(cudaMalloc(&st->binv32, (size_t)h->K * st->bstr * 4));
   CKI(cudaMemset(st->binv64, 0, (size_t)h->K * st->bstr * 8));
   CKI(cudaMemset(st->binv32, 0, (size_t)h->K * st->bstr * 4));
+  const size_t pk = ((size_t)Np * (Np + 1) / 2 + 3) / 4 * 4;
+  CKI(cudaMalloc(&st->binv_pk32, (size_t)h->K * pk * 4));
+  CKI(cudaMemset(st->binv_pk32, 0, (size_t)h->K * pk * 4));
+  CKI(cudaMalloc(&st->ops_blk32, (size_t)(2 * Np + NF) * h->NpP * 4));
+  CKI(cudaMalloc(&st->mass_blk32, (size_t)Np * h->NpP * 4));
   const size_t n = nvec(h);
   for (int i = 0; i < W_COUNT; ++i) {
     CKI(cudaMalloc(&st->w64[i], n * 8));
@@ -327,6 +418,9 @@ void ipdg_free(dgc_handle_s* h) {
     if (st->chunk[i]) cudaGraphExecDestroy(st->chunk[i]);
   cudaFree(st->binv64);
   cudaFree(st->binv32);
+  cudaFree(st->binv_pk32);
+  cudaFree(st->ops_blk32);
+  cudaFree(st->mass_blk32);
   cudaFree(st->mass64);
   cudaFree(st->mass32);
   cudaFree(st->dense64);
@@ -382,15 +476,25 @@ int cg_iteration(dgc_handle_s* h, int cgi, int slot, int first, cudaStream_t s) 
   p.p_old = wv<R>(h, W_P + (slot + 2) % 3);
   p.qx = wv<R>(h, W_QX);
   p.qy = wv<R>(h, W_QY);
-  if (int rc = launch<R>(h, dgk::IK_GRAD_PCG, p, s)) return rc;
+  // FP32: the register-blocked kernels (ipdg_blk.cuh); FP64: the one-node-per-thread ones
+  auto run = [&](int kind_r, int kind_blk) -> int {
+    if (sizeof(R) == 4) {
+      const cudaError_t e = dgk::ipdg_blk_launch(h->N, kind_blk, p, h->sm_count, s);
+      if (e != cudaSuccess) return cuda_err(e, "ipdg blocked kernel launch");
+      ++h->launches;
+      return DGC_OK;
+    }
+    return launch<R>(h, kind_r, p, s);
+  };
+  if (int rc = run(dgk::IK_GRAD_PCG, dgk::IB_GRAD)) return rc;
   p.du_src = wv<R>(h, W_P + slot);
   p.out = wv<R>(h, W_AP);
-  if (int rc = launch<R>(h, dgk::IK_DIV_SPD_DOT, p, s)) return rc;
+  if (int rc = run(dgk::IK_DIV_SPD_DOT, dgk::IB_DIV)) return rc;
   p.x = wv<R>(h, W_X);
   p.r = wv<R>(h, W_R);
   p.z = wv<R>(h, W_Z);
   p.Ap = wv<R>(h, W_AP);
-  if (int rc = launch<R>(h, dgk::IK_UPDATE, p, s)) return rc;
+  if (int rc = run(dgk::IK_UPDATE, dgk::IB_UPDATE)) return rc;
   dgk::k_cg_check<<<1, 1, 0, s>>>(h->ipdg->cg + cgi, (slot + 1) % 3);
   CKI(cudaGetLastError());
   ++h->launches;

@@ -63,6 +63,10 @@ struct IpdgParams {
   void* z;
   const void* Ap;
   const void* binv;     // [K][BSTR] symmetric block inverses
+  // register-blocked FP32 kernels (ipdg_blk.cuh)
+  const void* mats_blk; // rows Dr^T | Ds^T | LIFT^T (strong form), padded to NpP columns
+  const void* mass_blk; // rows of M, padded to NpP columns
+  const void* binv_pk;  // [K][PK] packed upper triangles of the block inverses
   CgScalars* cg;
   double* dot_out;      // DIV_SPD_DOT / DIV_RESID: accumulated dot product
   int slot;             // iteration slot (i mod 3)
