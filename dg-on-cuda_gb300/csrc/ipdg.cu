@@ -101,6 +101,19 @@ cudaError_t ipdg_blk_launch(int N, int kind, const IpdgParams& p, int sm, cudaSt
   }
 }
 
+template <typename R>
+cudaError_t bc_rhs_launch(int N, int ncells, const IpdgParams& p, const int* cells, const double* g, const double* h,
+                          R* out, cudaStream_t s) {
+  if (ncells == 0) return cudaSuccess;
+#define DGK_BC(n) \
+  case n: ipdg_bc_rhs_kernel<R, n><<<ncells, 64, 0, s>>>(p, cells, g, h, out); return cudaGetLastError();
+  switch (N) {
+    DGK_BC(1) DGK_BC(2) DGK_BC(3) DGK_BC(4) DGK_BC(5) DGK_BC(6) DGK_BC(7) DGK_BC(8)
+    default: return cudaErrorInvalidValue;
+  }
+#undef DGK_BC
+}
+
 cudaError_t pack_binv(int N, int K, const double* binv, int bstr, float* out, cudaStream_t s) {
   auto go = [&](auto kern, int pk) {
     const int64_t n = (int64_t)K * pk;
@@ -220,6 +233,9 @@ struct IpdgState {
   float* binv_pk32 = nullptr;  // [K][PK] packed upper triangles (register-blocked FP32 CG)
   float* ops_blk32 = nullptr;  // rows Dr^T | Ds^T | LIFT^T, strong form, padded to NpP columns
   float* mass_blk32 = nullptr; // rows of M padded to NpP columns
+  uint8_t* bcdir = nullptr;    // per boundary node condition type (dgc_laplace_set_bc_types), or NULL
+  int* bcells = nullptr;       // cells with a boundary face
+  int n_bcells = 0;
   void* mass64 = nullptr;      // padded M in FP64 / FP32
   void* mass32 = nullptr;
   double* dense64 = nullptr;   // row-major Dr | Ds | L | M (FP64) for the block set-up
@@ -263,6 +279,7 @@ dgk::IpdgParams base(const dgc_handle_s* h) {
   p.mats_blk = h->ipdg->ops_blk32;
   p.mass_blk = h->ipdg->mass_blk32;
   p.binv_pk = h->ipdg->binv_pk32;
+  p.bcdir = h->ipdg->bcdir;
   p.status = h->d_status;
   return p;
 }
@@ -296,6 +313,8 @@ int ipdg_build_preconditioner(dgc_handle_s* h, cudaStream_t s) {
   IpdgState* st = h->ipdg;
   if (st->ready) return DGC_OK;
   if (!h->desc.dirichlet) return set_error(DGC_ERR_UNSUPPORTED, "block-Jacobi CG needs Dirichlet boundaries (SPD form)");
+  if (st->bcdir)
+    return set_error(DGC_ERR_UNSUPPORTED, "block-Jacobi CG needs uniform Dirichlet boundaries (clear the per-node types)");
   cudaError_t e = dgk::diag_blocks(h->N, h->K, 1, h->d_geom, reinterpret_cast<const int4*>(h->d_nbr), h->d_tau,
                                    st->dense64, st->dense64 + (size_t)h->Np * h->Np,
                                    st->dense64 + (size_t)2 * h->Np * h->Np,
@@ -394,6 +413,15 @@ int ipdg_init(dgc_handle_s* h) {
   const size_t pk = ((size_t)Np * (Np + 1) / 2 + 3) / 4 * 4;
   CKI(cudaMalloc(&st->binv_pk32, (size_t)h->K * pk * 4));
   CKI(cudaMemset(st->binv_pk32, 0, (size_t)h->K * pk * 4));
+  {
+    std::vector<int> bc;
+    for (int k = 0; k < h->K; ++k)
+      if (h->mesh.nbr[4 * (size_t)k] < 0 || h->mesh.nbr[4 * (size_t)k + 1] < 0 || h->mesh.nbr[4 * (size_t)k + 2] < 0)
+        bc.push_back(k);
+    st->n_bcells = (int)bc.size();
+    CKI(cudaMalloc(&st->bcells, std::max<size_t>(bc.size(), 1) * sizeof(int)));
+    if (!bc.empty()) CKI(cudaMemcpy(st->bcells, bc.data(), bc.size() * sizeof(int), cudaMemcpyHostToDevice));
+  }
   CKI(cudaMalloc(&st->ops_blk32, (size_t)(2 * Np + NF) * h->NpP * 4));
   CKI(cudaMalloc(&st->mass_blk32, (size_t)Np * h->NpP * 4));
   const size_t n = nvec(h);
@@ -421,6 +449,8 @@ void ipdg_free(dgc_handle_s* h) {
   cudaFree(st->binv_pk32);
   cudaFree(st->ops_blk32);
   cudaFree(st->mass_blk32);
+  cudaFree(st->bcdir);
+  cudaFree(st->bcells);
   cudaFree(st->mass64);
   cudaFree(st->mass32);
   cudaFree(st->dense64);
@@ -697,5 +727,40 @@ extern "C" int dgc_block_jacobi(dgc_handle h, double* blocks, void* stream) {
   const int Np = h->Np, bs = h->ipdg->bstr;
   CKI(cudaMemcpy2DAsync(blocks, (size_t)Np * Np * 8, h->ipdg->binv64, (size_t)bs * 8, (size_t)Np * Np * 8, h->K,
                         cudaMemcpyDeviceToDevice, s));
+  return DGC_OK;
+}
+
+extern "C" int dgc_laplace_set_bc_types(dgc_handle h, const uint8_t* flags) {
+  if (int rc = check_laplace(h)) return rc;
+  IpdgState* st = h->ipdg;
+  const size_t nb = (size_t)h->mesh.num_bfaces * h->Nfp;
+  if (!flags) {
+    cudaFree(st->bcdir);
+    st->bcdir = nullptr;
+    return DGC_OK;
+  }
+  if (nb == 0) return DGC_OK;
+  if (!st->bcdir) CKI(cudaMalloc(&st->bcdir, nb));
+  CKI(cudaMemcpy(st->bcdir, flags, nb, cudaMemcpyHostToDevice));
+  return DGC_OK;
+}
+
+extern "C" int dgc_laplace_bc_rhs(dgc_handle h, const double* g, const double* hn, void* out, void* stream) {
+  if (int rc = check_laplace(h)) return rc;
+  if (!out) return set_error(DGC_ERR_ARG, "null output");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  IpdgState* st = h->ipdg;
+  cudaError_t e;
+  if (h->prec == DGC_F64) {
+    dgk::IpdgParams p = base<double>(h);
+    p.mats = h->d_mats64[1];
+    e = dgk::bc_rhs_launch<double>(h->N, st->n_bcells, p, st->bcells, g, hn, static_cast<double*>(out), s);
+  } else {
+    dgk::IpdgParams p = base<float>(h);
+    p.mats = h->d_mats32[1];
+    e = dgk::bc_rhs_launch<float>(h->N, st->n_bcells, p, st->bcells, g, hn, static_cast<float*>(out), s);
+  }
+  if (e != cudaSuccess) return cuda_err(e, "boundary-data kernel");
+  if (st->n_bcells) ++h->launches;
   return DGC_OK;
 }

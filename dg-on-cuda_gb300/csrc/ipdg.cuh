@@ -67,6 +67,7 @@ struct IpdgParams {
   const void* mats_blk; // rows Dr^T | Ds^T | LIFT^T (strong form), padded to NpP columns
   const void* mass_blk; // rows of M, padded to NpP columns
   const void* binv_pk;  // [K][PK] packed upper triangles of the block inverses
+  const uint8_t* bcdir; // per boundary node: 1 Dirichlet, 0 Neumann (NULL: `dirichlet` everywhere)
   CgScalars* cg;
   double* dot_out;      // DIV_SPD_DOT / DIV_RESID: accumulated dot product
   int slot;             // iteration slot (i mod 3)
@@ -186,6 +187,13 @@ struct IpdgTile {
 template <typename R, int N>
 __device__ __forceinline__ int nb_of(const int4& n, int f) { return f == 0 ? n.x : (f == 1 ? n.y : n.z); }
 
+// condition type of node d of boundary face `nb` (< 0): the per-node flags when
+// given (the reference's is_dirichlet(x, y)), else the handle's uniform type
+template <int N>
+__device__ __forceinline__ bool bc_dirichlet(const IpdgParams& p, int nb, int d) {
+  return p.bcdir ? p.bcdir[(size_t)(-1 - nb) * (N + 1) + d] != 0 : p.dirichlet != 0;
+}
+
 // ---------------------------------------------------------------- grad pass
 template <typename R, int N, int MODE>
 __global__ void __launch_bounds__(256) ipdg_grad_kernel(const IpdgParams p) {
@@ -243,7 +251,7 @@ __global__ void __launch_bounds__(256) ipdg_grad_kernel(const IpdgParams p) {
         else up = __ldg(u_in + (size_t)kn * NpP + nd2);
         du = um - up;
       } else {
-        du = p.dirichlet ? (R)2 * um : (R)0;
+        du = bc_dirichlet<N>(p, nb, d) ? (R)2 * um : (R)0;
       }
       const R tl = du * (R)g[5 + f] / (R)2;
       t.F0()[e * NFACE + fm] = (R)g[8 + f] * tl;
@@ -323,7 +331,7 @@ __global__ void __launch_bounds__(256) ipdg_div_kernel(const IpdgParams p) {
         }
         dqn = (qxm - qxp) * nx + (qym - qyp) * ny;
         du = um - up;
-      } else if (p.dirichlet) {
+      } else if (bc_dirichlet<N>(p, nb, d)) {
         dqn = (R)0;
         du = (R)2 * um;
       } else {
@@ -489,6 +497,69 @@ __global__ void __launch_bounds__(256) pcg_start_kernel(const IpdgParams p) {
   if (threadIdx.x == 0) {
     atomicAdd(&p.cg->rz[0], a);
     atomicAdd(&p.cg->rr[0], b);
+  }
+}
+
+// ---------------------------------------------------------------- boundary data
+// apply_inhomogeneous_as_rhs (src/laplace_2d.h:253-348): for each cell with a
+// boundary face (one CTA of 64 threads each) adds to out
+//   Dx qx + Dy qy - LIFT((hq + 2 tau gu) faceJ / 2) / J,
+//   q = -LIFT(n gu faceJ / 2) / J,
+// gu = g[b] at Dirichlet nodes (else 0), hq = h[b] at Neumann nodes (else 0).
+template <typename R, int N>
+__global__ void __launch_bounds__(64) ipdg_bc_rhs_kernel(const IpdgParams p, const int* __restrict__ cells,
+                                                         const double* __restrict__ g, const double* __restrict__ h,
+                                                         R* __restrict__ out) {
+  using O = Order<N>;
+  constexpr int Np = O::Np, NpP = O::NpP, Nfp = O::Nfp, NFACE = O::Nface;
+  constexpr int kD = IpdgConfig<R, N>::kD;
+  __shared__ R tx[NFACE], ty[NFACE], hq[NFACE], qx[Np], qy[Np];
+  const int c = cells[blockIdx.x];
+  const int t = threadIdx.x;
+  const R* G = static_cast<const R*>(p.geom) + (size_t)c * 16;
+  const R* tau = static_cast<const R*>(p.tau) + (size_t)c * 4;
+  const R* DrT = static_cast<const R*>(p.mats);
+  const R* DsT = DrT + kD;
+  const R* LT = DrT + 2 * kD;
+  const int4 n4 = p.nbr[c];
+  for (int m = t; m < NFACE; m += blockDim.x) {
+    const int f = m / Nfp, d = m - f * Nfp;
+    const int nb = f == 0 ? n4.x : (f == 1 ? n4.y : n4.z);
+    R v = 0, w = 0;
+    if (nb < 0) {
+      const size_t b = (size_t)(-1 - nb) * Nfp + d;
+      const bool dir = bc_dirichlet<N>(p, nb, d);
+      v = dir && g ? (R)g[b] : (R)0;
+      w = !dir && h ? (R)h[b] : (R)0;
+    }
+    const R hf = G[5 + f] / (R)2;
+    hq[m] = (w + (R)2 * tau[f] * v) * hf;
+    tx[m] = G[8 + f] * v * hf;
+    ty[m] = G[11 + f] * v * hf;
+  }
+  __syncthreads();
+  const R nJ = G[4];  // -1/J
+  if (t < Np) {
+    R ax = 0, ay = 0;
+    for (int m = 0; m < NFACE; ++m) {
+      ax += LT[m * Np + t] * tx[m];
+      ay += LT[m * Np + t] * ty[m];
+    }
+    qx[t] = nJ * ax;
+    qy[t] = nJ * ay;
+  }
+  __syncthreads();
+  if (t < Np) {
+    R xr = 0, xs = 0, yr = 0, ys = 0, lf = 0;
+    for (int j = 0; j < Np; ++j) {
+      const R dr = DrT[j * Np + t], ds = DsT[j * Np + t];
+      xr += dr * qx[j];
+      xs += ds * qx[j];
+      yr += dr * qy[j];
+      ys += ds * qy[j];
+    }
+    for (int m = 0; m < NFACE; ++m) lf += LT[m * Np + t] * hq[m];
+    out[(size_t)c * NpP + t] += (G[0] * xr + G[2] * xs) + (G[1] * yr + G[3] * ys) + nJ * lf;
   }
 }
 

@@ -103,6 +103,8 @@ def lib():
             L.dgc_laplace_spd_apply.argtypes = [_vp, _vp, _vp, _vp]
             L.dgc_mass_apply.argtypes = [_vp, _vp, _vp, _vp]
             L.dgc_boundary_nodes.argtypes = [_vp, _dp]
+            L.dgc_laplace_set_bc_types.argtypes = [_vp, C.c_void_p]
+            L.dgc_laplace_bc_rhs.argtypes = [_vp, _vp, _vp, _vp, _vp]
             L.dgc_adv1d_create.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(_vp)]
             L.dgc_adv1d_destroy.argtypes = [_vp]
             L.dgc_adv1d_info.argtypes = [_vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
@@ -409,6 +411,22 @@ class Discretization:
     def laplace(self, u, out=None, stream=None):
         out = self.empty_state() if out is None else out
         _check(lib().dgc_laplace_apply(self._h, _ptr(u), _ptr(out), _stream(stream)))
+        return out
+
+    def set_bc_types(self, is_dirichlet=None) -> None:
+        """Per-boundary-node condition types (bool array in boundary_nodes() order); None = uniform."""
+        if is_dirichlet is None:
+            _check(lib().dgc_laplace_set_bc_types(self._h, None))
+            return
+        f = np.ascontiguousarray(is_dirichlet, dtype=np.uint8).reshape(-1)
+        _check(lib().dgc_laplace_set_bc_types(self._h, f.ctypes.data))
+
+    def laplace_bc_rhs(self, g=None, h=None, out=None, stream=None):
+        """out += the boundary-data contribution (apply_inhomogeneous_as_rhs); g, h per boundary node."""
+        out = self.empty_state() if out is None else out
+        kg, pg = self._bdata(g)
+        kh, ph = self._bdata(h)
+        _check(lib().dgc_laplace_bc_rhs(self._h, pg, ph, _ptr(out), _stream(stream)))
         return out
 
     def spd(self, u, out=None, stream=None):

@@ -236,6 +236,22 @@ int dgc_div_apply(dgc_handle h, const void* ux, const void* uy, void* out, const
  * u and out in the handle's precision. */
 int dgc_laplace_apply(dgc_handle h, const void* u, void* out, void* stream);
 
+/* Boundary condition type per boundary face node (replaces the
+ * is_dirichlet(x, y) callback of the reference's boundary objects,
+ * src/laplace_2d.h:179, 233): flags[b] != 0 Dirichlet, 0 Neumann, boundary
+ * nodes in dgc_boundary_nodes order (host array).  NULL returns to the
+ * handle's uniform type (desc.dirichlet).  dgc_pcg_solve needs uniform
+ * Dirichlet boundaries and refuses handles with per-node types. */
+int dgc_laplace_set_bc_types(dgc_handle h, const uint8_t* flags);
+
+/* out += the boundary-data contribution of apply_inhomogeneous_as_rhs
+ * (src/laplace_2d.h:253-348): g[b] = exterior_val(x, y, 0) at Dirichlet nodes,
+ * hn[b] = exterior_grad_n(x, y, 0) at Neumann nodes (FP64 device arrays, one
+ * value per boundary node; NULL = 0); out in the handle's precision.
+ * laplace_2d::operator() with boundary data (same file:121-128) is
+ * dgc_laplace_apply minus this contribution. */
+int dgc_laplace_bc_rhs(dgc_handle h, const double* g, const double* hn, void* out, void* stream);
+
 /* out = S u = -blockdiag(J_k M) A u: the mass-weighted form, symmetric
  * positive definite for Dirichlet problems. */
 int dgc_laplace_spd_apply(dgc_handle h, const void* u, void* out, void* stream);

@@ -881,9 +881,16 @@ static double face_tau(const orc* o, int c, int e, int tau_mode) {
   return N1 * N1 / hm;
 }
 
+/* boundary condition type of boundary node i of face (c, e): the per-node
+ * flags when given (is_dirichlet(x, y) of the reference's BC objects), else
+ * the uniform type */
+static int bc_dir(const orc* o, int dirichlet, const uint8_t* bdir, int c, int e, int i) {
+  return bdir ? bdir[o->nbF[3 * c + e] + i] != 0 : dirichlet;
+}
+
 /* pass 1 for one cell: q = D u - LIFT(n du faceJ / 2) / J; stores du */
-static void lap_pass1_cell(orc* o, int dirichlet, const double* u, int c, double* qx, double* qy,
-                           double* du) {
+static void lap_pass1_cell(orc* o, int dirichlet, const uint8_t* bdir, const double* u, int c, double* qx,
+                           double* qy, double* du) {
   int Np = o->Np, Nfp = o->Nfp;
   double D[ORC_MAX_NP * ORC_MAX_NP], tlx[3 * ORC_MAX_NFP], tly[3 * ORC_MAX_NFP];
   size_t off = (size_t)c * Np;
@@ -896,7 +903,7 @@ static void lap_pass1_cell(orc* o, int dirichlet, const double* u, int c, double
     double nx = o->nx[3 * c + e], ny = o->ny[3 * c + e], fJ = o->faceJ[3 * c + e];
     for (int i = 0; i < Nfp; ++i) {
       double d;
-      if (isb) d = dirichlet ? 2.0 * u[off + o->Fmask[e][i]] : 0.0;
+      if (isb) d = bc_dir(o, dirichlet, bdir, c, e, i) ? 2.0 * u[off + o->Fmask[e][i]] : 0.0;
       else d = u[off + o->Fmask[e][i]] - u[(size_t)nbc * Np + o->Fmask[nbf][Nfp - i - 1]];
       du[(size_t)c * 3 * Nfp + e * Nfp + i] = d;
       tlx[e * Nfp + i] = nx * d * fJ / 2.0;
@@ -908,8 +915,8 @@ static void lap_pass1_cell(orc* o, int dirichlet, const double* u, int c, double
   gemv(Np, 3 * Nfp, o->Ls, -1.0 / cJ, tly, 1.0, qy + off);
 }
 
-static void lap_pass2_cell(orc* o, int dirichlet, int tau_mode, const double* qx, const double* qy,
-                           const double* du, int c, double* out) {
+static void lap_pass2_cell(orc* o, int dirichlet, const uint8_t* bdir, int tau_mode, const double* qx,
+                           const double* qy, const double* du, int c, double* out) {
   int Np = o->Np, Nfp = o->Nfp;
   double D[ORC_MAX_NP * ORC_MAX_NP], tl[3 * ORC_MAX_NFP];
   size_t off = (size_t)c * Np;
@@ -926,7 +933,7 @@ static void lap_pass2_cell(orc* o, int dirichlet, int tau_mode, const double* qx
       double dqN;
       if (isb) {
         double gn = qx[ia] * nx + qy[ia] * ny;
-        dqN = dirichlet ? 0.0 : 2.0 * gn;
+        dqN = bc_dir(o, dirichlet, bdir, c, e, i) ? 0.0 : 2.0 * gn;
       } else {
         size_t ib = (size_t)nbc * Np + o->Fmask[nbf][Nfp - i - 1];
         dqN = (qx[ia] - qx[ib]) * nx + (qy[ia] - qy[ib]) * ny;
@@ -938,8 +945,63 @@ static void lap_pass2_cell(orc* o, int dirichlet, int tau_mode, const double* qx
 }
 
 void orc_laplace_apply(orc* o, int dirichlet, int tau_mode, const double* u, double* out) {
-  for (int c = 0; c < o->K; ++c) lap_pass1_cell(o, dirichlet, u, c, o->qx, o->qy, o->du);
-  for (int c = 0; c < o->K; ++c) lap_pass2_cell(o, dirichlet, tau_mode, o->qx, o->qy, o->du, c, out);
+  for (int c = 0; c < o->K; ++c) lap_pass1_cell(o, dirichlet, NULL, u, c, o->qx, o->qy, o->du);
+  for (int c = 0; c < o->K; ++c) lap_pass2_cell(o, dirichlet, NULL, tau_mode, o->qx, o->qy, o->du, c, out);
+}
+
+/* apply_homogeneous with a condition type per boundary node (laplace_2d.h:130-251) */
+void orc_laplace_apply_bc(orc* o, const uint8_t* bdir, int tau_mode, const double* u, double* out) {
+  for (int c = 0; c < o->K; ++c) lap_pass1_cell(o, 1, bdir, u, c, o->qx, o->qy, o->du);
+  for (int c = 0; c < o->K; ++c) lap_pass2_cell(o, 1, bdir, tau_mode, o->qx, o->qy, o->du, c, out);
+}
+
+/* apply_inhomogeneous_as_rhs (laplace_2d.h:253-348): adds to out, for every
+ * cell with a boundary face, the contribution of the boundary data
+ *   q  = -LIFT(n gu faceJ / 2) / J,  gu = g[b] at Dirichlet nodes, else 0
+ *   out += Dx qx + Dy qy - LIFT((hq + 2 tau gu) faceJ / 2) / J,
+ *          hq = h[b] at Neumann nodes, else 0
+ * with g[b] = exterior_val(x, y, 0) and h[b] = exterior_grad_n(x, y, 0) of
+ * boundary node b; tau as in the homogeneous passes (1 in the reference). */
+void orc_laplace_bc_rhs(orc* o, const uint8_t* bdir, int tau_mode, const double* g, const double* h,
+                        double* out) {
+  int Np = o->Np, Nfp = o->Nfp;
+  double D[ORC_MAX_NP * ORC_MAX_NP], tlx[3 * ORC_MAX_NFP], tly[3 * ORC_MAX_NFP];
+  double qx[ORC_MAX_NP], qy[ORC_MAX_NP], gu[3 * ORC_MAX_NFP];
+  for (int c = 0; c < o->K; ++c) {
+    if (!o->isB[3 * c] && !o->isB[3 * c + 1] && !o->isB[3 * c + 2]) continue;
+    for (int m = 0; m < 3 * Nfp; ++m) { tlx[m] = 0.0; tly[m] = 0.0; gu[m] = 0.0; }
+    for (int i = 0; i < Np; ++i) { qx[i] = 0.0; qy[i] = 0.0; }  /* gemv reads y even with beta = 0 */
+    for (int e = 0; e < 3; ++e) {
+      if (!o->isB[3 * c + e]) continue;
+      double nx = o->nx[3 * c + e], ny = o->ny[3 * c + e], fJ = o->faceJ[3 * c + e];
+      for (int i = 0; i < Nfp; ++i) {
+        int b = o->nbF[3 * c + e] + i;
+        double v = bc_dir(o, 1, bdir, c, e, i) && g ? g[b] : 0.0;
+        gu[e * Nfp + i] = v;
+        tlx[e * Nfp + i] = nx * v * fJ / 2.0;
+        tly[e * Nfp + i] = ny * v * fJ / 2.0;
+      }
+    }
+    double cJ = o->J[c];
+    gemv(Np, 3 * Nfp, o->Ls, -1.0 / cJ, tlx, 0.0, qx);
+    gemv(Np, 3 * Nfp, o->Ls, -1.0 / cJ, tly, 0.0, qy);
+    size_t off = (size_t)c * Np;
+    phys_matrix(o, o->Drs, o->Dss, c, 0, D);
+    gemv(Np, Np, D, 1.0, qx, 1.0, out + off);
+    phys_matrix(o, o->Drs, o->Dss, c, 1, D);
+    gemv(Np, Np, D, 1.0, qy, 1.0, out + off);
+    for (int m = 0; m < 3 * Nfp; ++m) tlx[m] = 0.0;
+    for (int e = 0; e < 3; ++e) {
+      if (!o->isB[3 * c + e]) continue;
+      double fJ = o->faceJ[3 * c + e], tau = face_tau(o, c, e, tau_mode);
+      for (int i = 0; i < Nfp; ++i) {
+        int b = o->nbF[3 * c + e] + i;
+        double hq = !bc_dir(o, 1, bdir, c, e, i) && h ? h[b] : 0.0;
+        tlx[e * Nfp + i] = (hq + 2.0 * tau * gu[e * Nfp + i]) * fJ / 2.0;
+      }
+    }
+    gemv(Np, 3 * Nfp, o->Ls, -1.0 / cJ, tlx, 1.0, out + off);
+  }
 }
 
 /* out = -J_k M (A u)_k : the mass-weighted, symmetric positive definite form */
@@ -974,10 +1036,10 @@ void orc_spd_diag_blocks(orc* o, int tau_mode, double* blocks) {
     size_t off = (size_t)c * Np;
     for (int j = 0; j < Np; ++j) {
       u[off + j] = 1.0;
-      lap_pass1_cell(o, 1, u, c, qx, qy, du);
+      lap_pass1_cell(o, 1, NULL, u, c, qx, qy, du);
       for (int e = 0; e < 3; ++e)
-        if (!o->isB[3 * c + e]) lap_pass1_cell(o, 1, u, o->nbC[3 * c + e], qx, qy, du);
-      lap_pass2_cell(o, 1, tau_mode, qx, qy, du, c, out);
+        if (!o->isB[3 * c + e]) lap_pass1_cell(o, 1, NULL, u, o->nbC[3 * c + e], qx, qy, du);
+      lap_pass2_cell(o, 1, NULL, tau_mode, qx, qy, du, c, out);
       double col[ORC_MAX_NP];
       gemv(Np, Np, o->M, -o->J[c], out + off, 0.0, col);
       for (int i = 0; i < Np; ++i) blocks[(size_t)c * Np * Np + (size_t)i * Np + j] = col[i];

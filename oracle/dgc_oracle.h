@@ -85,6 +85,11 @@ void orc_exact(orc* o, const orc_problem* p, double t, double* q);
  * or all Neumann (dirichlet=0); tau_mode 0 = reference tau = 1, tau_mode 1 = per-face
  * tau = (N+1)^2 / h_f with h_f the smaller altitude onto the face. */
 void orc_laplace_apply(orc* o, int dirichlet, int tau_mode, const double* u, double* out);
+/* laplace_2d with a condition type per boundary node (bdir[b] != 0: Dirichlet)
+ * and the boundary-data contribution apply_inhomogeneous_as_rhs adds */
+void orc_laplace_apply_bc(orc* o, const uint8_t* bdir, int tau_mode, const double* u, double* out);
+void orc_laplace_bc_rhs(orc* o, const uint8_t* bdir, int tau_mode, const double* g, const double* h,
+                        double* out);
 /* SPD form S u = -blockdiag(J_k M) A u, and its diagonal blocks (K x Np x Np) */
 void orc_spd_apply(orc* o, int tau_mode, const double* u, double* out);
 void orc_spd_diag_blocks(orc* o, int tau_mode, double* blocks);

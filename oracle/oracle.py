@@ -75,6 +75,8 @@ def lib():
             L.orc_spd_apply.argtypes = [C.c_void_p, C.c_int, _dp, _dp]
             L.orc_spd_diag_blocks.argtypes = [C.c_void_p, C.c_int, _dp]
             L.orc_mass_apply.argtypes = [C.c_void_p, _dp, _dp]
+            L.orc_laplace_apply_bc.argtypes = [C.c_void_p, C.c_void_p, C.c_int, _dp, _dp]
+            L.orc_laplace_bc_rhs.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, _dp]
             L.orc_grad.argtypes = [C.c_void_p, _dp, C.c_void_p, C.c_double, _dp, _dp]
             L.orc_div.argtypes = [C.c_void_p, _dp, _dp, C.c_void_p, C.c_void_p, C.c_double, _dp]
             L.orc_pcg.restype = C.c_int
@@ -210,6 +212,24 @@ class Oracle:
         u = np.ascontiguousarray(u, dtype=np.float64).reshape(-1)
         out = np.zeros_like(u)
         lib().orc_laplace_apply(self._h, int(dirichlet), tau_mode, u, out)
+        return out
+
+    def laplace_bc(self, u, is_dirichlet, tau_mode: int = 0) -> np.ndarray:
+        """apply_homogeneous with a condition type per boundary node (bool array)."""
+        u = np.ascontiguousarray(u, dtype=np.float64).reshape(-1)
+        f = np.ascontiguousarray(is_dirichlet, dtype=np.uint8).reshape(-1)
+        out = np.zeros_like(u)
+        lib().orc_laplace_apply_bc(self._h, f.ctypes.data, tau_mode, u, out)
+        return out
+
+    def laplace_bc_rhs(self, is_dirichlet, g=None, h=None, tau_mode: int = 0, out=None) -> np.ndarray:
+        """apply_inhomogeneous_as_rhs: adds the boundary-data contribution to out
+        (zeros when not given); g, h = exterior_val(x, y, 0), exterior_grad_n(x, y, 0)."""
+        out = np.zeros(self.K * self.Np) if out is None else np.array(out, dtype=np.float64).reshape(-1)
+        f = np.ascontiguousarray(is_dirichlet, dtype=np.uint8).reshape(-1)
+        g, h = self._opt(g), self._opt(h)
+        lib().orc_laplace_bc_rhs(self._h, f.ctypes.data, tau_mode, None if g is None else g.ctypes.data,
+                                 None if h is None else h.ctypes.data, out)
         return out
 
     @staticmethod

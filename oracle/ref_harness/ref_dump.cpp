@@ -55,6 +55,13 @@ struct dirichlet_all {
   double exterior_grad_n(double, double, double g) const { return g; }
 };
 
+// laplace_2d boundary object with both condition types and nonzero data
+struct mixed_bc {
+  bool is_dirichlet(double x, double y) const { return x + 0.3 * y < 0.2; }
+  double exterior_val(double x, double y, double v) const { return 2.0 * std::sin(x + y) - v; }
+  double exterior_grad_n(double x, double y, double gn) const { return 2.0 * std::cos(x * y) - gn; }
+};
+
 // boundary objects of the form u+ = g(x, y) + sign u- for grad_2d / div_2d
 struct scalar_bc {
   double sign;
@@ -233,6 +240,20 @@ int main(int argc, char** argv) {
     for (int i = 0; i < n; ++i) u[i] = std::sin(1.3 * i + 0.2) + 0.1 * std::cos(0.7 * i);
     lap(u.begin(), dirichlet_all());
     putv("lap2_out", u);
+    // mixed condition types with boundary data: the homogeneous part, the data
+    // contribution alone, and operator() (both)
+    std::vector<double> lu(n);
+    for (int i = 0; i < n; ++i) lu[i] = std::cos(0.8 * i + 0.5) - 0.2 * std::sin(1.9 * i);
+    putv("lapm_u", lu);
+    std::vector<double> a(lu);
+    lap.apply_homogeneous(a.begin(), mixed_bc());
+    putv("lapm_hom", a);
+    std::vector<double> z(n, 0.0);
+    lap.apply_inhomogeneous_as_rhs(z.begin(), mixed_bc());
+    putv("lapm_rhs", z);
+    std::vector<double> b(lu);
+    lap(b.begin(), mixed_bc());
+    putv("lapm_full", b);
   }
 
   // grad_2d and div_2d (weak form, central fluxes) with boundary data

@@ -2,9 +2,11 @@
 block-Jacobi PCG solvers, through the C ABI.
 
 FP64 applies: the reference's own laplace_2d outputs (tests/golden/, tau = 1,
-homogeneous Dirichlet) and the oracle (scaled tau, Neumann) at 1e-12 relative.
-FP32 applies: the oracle at 2e-5.  Solvers: both methods reach the requested
-true FP64 residual and agree with the oracle's FP64 PCG solution.
+homogeneous Dirichlet; mixed Dirichlet / Neumann node types with boundary data
+through apply_homogeneous, apply_inhomogeneous_as_rhs and operator()) and the
+oracle (scaled tau, Neumann, mixed types) at 1e-12 relative.  FP32 applies: the
+oracle at 2e-5.  Solvers: both methods reach the requested true FP64 residual
+and agree with the oracle's FP64 PCG solution.
 """
 import os
 
@@ -170,3 +172,44 @@ def test_mixed_ir_converges_at_scale():
     ex = (np.sin(np.pi * x) * np.sin(np.pi * y)).reshape(-1)
     assert relerr(D.download(xs).reshape(-1), ex) < 1e-6
     D.check()
+
+
+def mixed_bc(D):
+    """The reference harness's mixed_bc at the handle's boundary nodes (Dirichlet where
+    x + 0.3 y < 0.2; exterior_val(x, y, 0) = 2 sin(x + y), exterior_grad_n(x, y, 0) = 2 cos(x y))."""
+    b = D.boundary_nodes()
+    bx, by = b[:, 0], b[:, 1]
+    return bx + 0.3 * by < 0.2, 2 * np.sin(bx + by), 2 * np.cos(bx * by)
+
+
+@pytest.mark.parametrize("case", [f"{m}_N{n}" for m in ("jit4", "coarse") for n in range(1, 7)] +
+                         ["cells4_N2", "fine_N1"])
+def test_laplace_mixed_conditions_and_boundary_data_match_reference(case):
+    d = np.load(os.path.join(GOLDEN, f"ref_{case}.npz"))
+    N = int(case.split("_N")[1])
+    D = dg.Discretization(golden_mesh(d), "laplace", N, dg.F64, tau=dg.TAU_ONE, dirichlet=True)
+    isd, g, h = mixed_bc(D)
+    D.set_bc_types(isd)
+    hom = D.download(D.laplace(D.upload(d["lapm_u"])))
+    assert relerr(hom, d["lapm_hom"]) < 1e-12
+    rhs = D.download(D.laplace_bc_rhs(g, h))
+    assert relerr(rhs, d["lapm_rhs"]) < 1e-12
+    assert relerr(hom - rhs, d["lapm_full"]) < 1e-12      # laplace_2d::operator()
+    with pytest.raises(dg.DgcError):                         # CG needs uniform Dirichlet
+        D.pcg(D.upload(d["lapm_u"]))
+    D.set_bc_types(None)
+    D.check()
+
+
+@pytest.mark.parametrize("N", (1, 3, 4, 6, 8))
+def test_laplace_mixed_conditions_match_oracle(N):
+    m = meshes.jittered_square(6, 70 + N)
+    o = oracle.Oracle(m.xy, m.cells, N)
+    rng = np.random.default_rng(N)
+    u = rng.standard_normal(o.K * o.Np)
+    for prec, tol in ((dg.F64, 1e-12), (dg.F32, 2e-5)):
+        D = dg.Discretization(m, "laplace", N, prec, tau=dg.TAU_SCALED, dirichlet=True)
+        isd, g, h = mixed_bc(D)
+        D.set_bc_types(isd)
+        assert relerr(D.download(D.laplace(D.upload(u))), o.laplace_bc(u, isd, tau_mode=1)) < tol
+        assert relerr(D.download(D.laplace_bc_rhs(g, h)), o.laplace_bc_rhs(isd, g, h, tau_mode=1)) < tol

@@ -113,6 +113,25 @@ def test_laplace_apply(golden):
     assert relerr(out, d["lap2_out"]) < 1e-12
 
 
+def mixed_bc(bx, by):
+    """The reference harness's mixed_bc object at boundary nodes: Dirichlet where
+    x + 0.3 y < 0.2; exterior_val(x, y, 0) = 2 sin(x + y), exterior_grad_n(x, y, 0) = 2 cos(x y)."""
+    return bx + 0.3 * by < 0.2, 2 * np.sin(bx + by), 2 * np.cos(bx * by)
+
+
+def test_laplace_mixed_conditions_and_boundary_data(golden):
+    N, d, o = golden
+    a = o.arrays()
+    isd, g, h = mixed_bc(a["bx"], a["by"])
+    assert 0 < isd.sum() < isd.size      # both condition types present
+    hom = o.laplace_bc(d["lapm_u"], isd)
+    assert relerr(hom, d["lapm_hom"]) < 1e-12
+    rhs = o.laplace_bc_rhs(isd, g, h)
+    assert relerr(rhs, d["lapm_rhs"]) < 1e-12
+    # operator() = apply_homogeneous - (the data contribution) (laplace_2d.h:121-128)
+    assert relerr(hom - rhs, d["lapm_full"]) < 1e-12
+
+
 def boundary_data(o):
     """The reference harness's boundary functions at the oracle's boundary nodes:
     grad / div exterior values 2 g - u with g = sin x cos y (and x y for div)."""
