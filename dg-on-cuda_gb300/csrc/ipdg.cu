@@ -114,6 +114,21 @@ cudaError_t bc_rhs_launch(int N, int ncells, const IpdgParams& p, const int* cel
 #undef DGK_BC
 }
 
+// floats per packed block (IpdgBlk<N>::PK) for the allocation on the host
+int packed_stride(int N) {
+  switch (N) {
+    case 1: return IpdgBlk<1>::PK;
+    case 2: return IpdgBlk<2>::PK;
+    case 3: return IpdgBlk<3>::PK;
+    case 4: return IpdgBlk<4>::PK;
+    case 5: return IpdgBlk<5>::PK;
+    case 6: return IpdgBlk<6>::PK;
+    case 7: return IpdgBlk<7>::PK;
+    case 8: return IpdgBlk<8>::PK;
+    default: return 0;
+  }
+}
+
 cudaError_t pack_binv(int N, int K, const double* binv, int bstr, float* out, cudaStream_t s) {
   auto go = [&](auto kern, int pk) {
     const int64_t n = (int64_t)K * pk;
@@ -410,7 +425,7 @@ int ipdg_init(dgc_handle_s* h) {
   CKI(cudaMalloc(&st->binv32, (size_t)h->K * st->bstr * 4));
   CKI(cudaMemset(st->binv64, 0, (size_t)h->K * st->bstr * 8));
   CKI(cudaMemset(st->binv32, 0, (size_t)h->K * st->bstr * 4));
-  const size_t pk = ((size_t)Np * (Np + 1) / 2 + 3) / 4 * 4;
+  const size_t pk = (size_t)dgk::packed_stride(h->N);
   CKI(cudaMalloc(&st->binv_pk32, (size_t)h->K * pk * 4));
   CKI(cudaMemset(st->binv_pk32, 0, (size_t)h->K * pk * 4));
   {

@@ -29,7 +29,14 @@ struct IpdgBlk {
   static constexpr int KB = 2 * Np + NFACE;  // operator rows: Dr^T | Ds^T | LIFT^T
   static constexpr uint32_t kOps = KB * NpP * 4;
   static constexpr uint32_t kMass = Np * NpP * 4;
-  static constexpr int PK = (Np * (Np + 1) / 2 + 3) / 4 * 4;  // packed symmetric block, padded
+  // packed symmetric block padded to a multiple of 4 floats with PK / 4 odd, so
+  // the blocks of the 8 elements a warp covers start in different bank groups
+  static constexpr int PK0 = (Np * (Np + 1) / 2 + 3) / 4 * 4;
+  static constexpr int PK = (PK0 / 4) % 2 == 0 ? PK0 + 4 : PK0;
+  // the 4-node groups of an element sit in one warp: column values are taken
+  // from the owning lane by shuffle instead of (bank-conflicting) shared loads
+  static constexpr bool kShfl = (32 % NG) == 0;
+  static constexpr int FSG = 2 * FSTR + 1, FSD = FSTR + 1;  // odd flux-row strides (grad: x | y rows)
   static constexpr uint32_t kF = TE * NpP * 4;                // one field tile
   static constexpr uint32_t kG = TE * 16 * 4, kN = TE * 16, kT = TE * 4 * 4;
   // grad: buffers hold z | p_old | geometry | neighbours
@@ -37,13 +44,13 @@ struct IpdgBlk {
   static constexpr uint32_t oBar = 0, oOps = 32;
   static constexpr uint32_t oBufG = oOps + kOps;
   static constexpr uint32_t oFluxG = oBufG + 2 * kBufG;
-  static constexpr uint32_t kSmemGrad = oFluxG + TE * 2 * FSTR * 4;
+  static constexpr uint32_t kSmemGrad = oFluxG + TE * FSG * 4;
   // div: buffers hold qx | qy | p | geometry | neighbours | tau
   static constexpr uint32_t kBufD = 3 * kF + kG + kN + kT;
   static constexpr uint32_t oMassD = oOps + kOps;
   static constexpr uint32_t oBufD = oMassD + kMass;
   static constexpr uint32_t oFluxD = oBufD + 2 * kBufD;
-  static constexpr uint32_t oWD = oFluxD + TE * FSTR * 4;
+  static constexpr uint32_t oWD = (oFluxD + TE * FSD * 4 + 15) / 16 * 16;  // float4 stores
   static constexpr uint32_t kSmemDiv = oWD + kF + 16 * 8;
   // update: buffers hold x | r | p | Ap | packed Binv (all bulk-copied)
   static constexpr uint32_t kBufU = 4 * kF + TE * PK * 4;
@@ -52,6 +59,12 @@ struct IpdgBlk {
   static constexpr uint32_t oBufU = oTabU + kTabU;
   static constexpr uint32_t kSmemUpd = oBufU + 2 * kBufU + 16 * 8;
   static_assert(NpP % 4 == 0 && kOps % 16 == 0 && kMass % 16 == 0, "16-byte rows");
+  // every region read or written with 16-byte accesses or bulk copies starts on 16 bytes
+  static_assert(oBufG % 16 == 0 && kBufG % 16 == 0 && oFluxG % 16 == 0, "grad layout alignment");
+  static_assert(oMassD % 16 == 0 && oBufD % 16 == 0 && kBufD % 16 == 0 && oWD % 16 == 0 && (oWD + kF) % 16 == 0,
+                "div layout alignment");
+  static_assert(oBufU % 16 == 0 && kBufU % 16 == 0 && (oBufU + 2 * kBufU) % 16 == 0 && PK % 4 == 0,
+                "update layout alignment");
 };
 
 // packed index of (i, j) in the upper triangle stored row by row
@@ -67,13 +80,21 @@ __device__ __forceinline__ float f4_at(const float4& v, int i) {
   return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
 }
 
+// node j of an element whose NG lanes (NG | 32) each hold 4 consecutive nodes
+// as v: read from the owning lane.  All 32 lanes must take part.
+template <int NG>
+__device__ __forceinline__ float col_shfl(const float4& v, int j) {
+  const int src = ((int)(threadIdx.x & 31) & ~(NG - 1)) + (j >> 2);
+  return __shfl_sync(0xffffffffu, f4_at(v, j & 3), src);
+}
+
 // ---------------------------------------------------------------- grad pass
 // p = z + beta p_old (written), qx, qy = grad p (strong form, jumps lifted)
 template <int N>
 __global__ void __launch_bounds__(256, 4) ipdg_grad_blk_kernel(const IpdgParams p) {
   using B = IpdgBlk<N>;
   constexpr int Np = B::Np, NpP = B::NpP, Nfp = B::Nfp, NFACE = B::NFACE, NG = B::NG, TE = B::TE;
-  constexpr int FSTR = B::FSTR;
+  constexpr int FSTR = B::FSTR, FS = B::FSG;
   extern __shared__ __align__(128) unsigned char smem[];
   if (p.cg->done) return;
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem + B::oBar);
@@ -118,7 +139,7 @@ __global__ void __launch_bounds__(256, 4) ipdg_grad_blk_kernel(const IpdgParams 
     fence_barrier_init();
   }
   // padding columns of the flux rows stay zero
-  for (int x = tid; x < TE * 2 * FSTR; x += 256) sF[x] = 0.0f;
+  for (int x = tid; x < TE * FS; x += 256) sF[x] = 0.0f;
   __syncthreads();
   if (tid == 0) {
     mbar_arrive_expect_tx(&bar[2], B::kOps);
@@ -187,21 +208,42 @@ __global__ void __launch_bounds__(256, 4) ipdg_grad_blk_kernel(const IpdgParams 
         const float* g = sG + e * 16;
         const float du = sU[e * NpP + fmask<N>(f, d)] - fmaf(beta, vp[q], vz[q]);
         const float tl = du * g[5 + f] * 0.5f * g[4];  // g[4] = -1/J
-        sF[(e * 2) * FSTR + fm] = g[8 + f] * tl;
-        sF[(e * 2 + 1) * FSTR + fm] = g[11 + f] * tl;
+        sF[e * FS + fm] = g[8 + f] * tl;
+        sF[e * FS + FSTR + fm] = g[11 + f] * tl;
       }
     }
     __syncthreads();
-    if (slot < ne) {
+    // with kShfl every thread has a slot (TE NG = 256) and takes part in the
+    // shuffles; lanes past the tile compute on stale values and store nothing
+    if (B::kShfl || slot < ne) {
       const float* ue = sU + slot * NpP;
+      const float4 pown = reinterpret_cast<const float4*>(sU)[slot * NG + grp];  // this thread's 4 nodes of p
       float4 ur = make_float4(0.f, 0.f, 0.f, 0.f), us = ur, lx = ur, ly = ur;
+      if constexpr (B::kShfl) {
+        // nodes 4 jg .. 4 jg + 3 come from lane jg of the element's group; the
+        // outer loop stays rolled to bound register pressure
+        const int base = (int)(threadIdx.x & 31) & ~(NG - 1);
+#pragma unroll 1
+        for (int jg = 0; jg < NG; ++jg) {
 #pragma unroll
-      for (int j = 0; j < Np; ++j) {
-        const float v = ue[j];
-        ur = f4_fma(ops4[j * NG + grp], v, ur);
-        us = f4_fma(ops4[(Np + j) * NG + grp], v, us);
+          for (int c = 0; c < 4; ++c) {
+            const float v = __shfl_sync(0xffffffffu, f4_at(pown, c), base + jg);
+            const int j = 4 * jg + c;
+            if (j < Np) {
+              ur = f4_fma(ops4[j * NG + grp], v, ur);
+              us = f4_fma(ops4[(Np + j) * NG + grp], v, us);
+            }
+          }
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < Np; ++j) {
+          const float v = ue[j];
+          ur = f4_fma(ops4[j * NG + grp], v, ur);
+          us = f4_fma(ops4[(Np + j) * NG + grp], v, us);
+        }
       }
-      const float* fx = sF + (slot * 2) * FSTR;
+      const float* fx = sF + slot * FS;
       const float* fy = fx + FSTR;
 #pragma unroll
       for (int m = 0; m < NFACE; ++m) {
@@ -220,9 +262,11 @@ __global__ void __launch_bounds__(256, 4) ipdg_grad_blk_kernel(const IpdgParams 
       qy.y = ry * ur.y + sy * us.y + ly.y;
       qy.z = ry * ur.z + sy * us.z + ly.z;
       qy.w = ry * ur.w + sy * us.w + ly.w;
-      const size_t o = (size_t)(k0 + slot) * NpP;
-      reinterpret_cast<float4*>(qxo + o)[grp] = qx;  // padding columns of the operators are zero
-      reinterpret_cast<float4*>(qyo + o)[grp] = qy;
+      if (slot < ne) {
+        const size_t o = (size_t)(k0 + slot) * NpP;
+        reinterpret_cast<float4*>(qxo + o)[grp] = qx;  // padding columns of the operators are zero
+        reinterpret_cast<float4*>(qyo + o)[grp] = qy;
+      }
     }
     __syncthreads();
   }
@@ -234,7 +278,7 @@ template <int N>
 __global__ void __launch_bounds__(256, 4) ipdg_div_blk_kernel(const IpdgParams p) {
   using B = IpdgBlk<N>;
   constexpr int Np = B::Np, NpP = B::NpP, Nfp = B::Nfp, NFACE = B::NFACE, NG = B::NG, TE = B::TE;
-  constexpr int FSTR = B::FSTR;
+  constexpr int FS = B::FSD;
   extern __shared__ __align__(128) unsigned char smem[];
   if (p.cg->done) return;
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem + B::oBar);
@@ -284,7 +328,7 @@ __global__ void __launch_bounds__(256, 4) ipdg_div_blk_kernel(const IpdgParams p
     mbar_init(&bar[2], 1);
     fence_barrier_init();
   }
-  for (int x = tid; x < TE * FSTR; x += 256) sF[x] = 0.0f;
+  for (int x = tid; x < TE * FS; x += 256) sF[x] = 0.0f;
   __syncthreads();
   if (tid == 0) {
     mbar_arrive_expect_tx(&bar[2], B::kOps + B::kMass);
@@ -303,6 +347,23 @@ __global__ void __launch_bounds__(256, 4) ipdg_div_blk_kernel(const IpdgParams p
     if (tid == 0 && nxt < ntiles) issue(nxt, b ^ 1);
     if (!__syncthreads_and(mbar_wait(&bar[b], ph[b], p.status))) return;
     ph[b] ^= 1;
+    // S p = -J M (A p): rows of the symmetric mass matrix cover the thread's 4
+    // nodes; A p of node j from its owning lane (kShfl) or from shared memory
+    auto mass_epilogue = [&](const float4& au, const float* we = nullptr) {
+      float4 sm = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+      for (int j = 0; j < Np; ++j) sm = f4_fma(mass4[j * NG + grp], we ? we[j] : col_shfl<NG>(au, j), sm);
+      if (slot < ne) {
+        const float mJ = bufG(b)[slot * 16 + 14];  // -J
+        sm.x *= mJ;
+        sm.y *= mJ;
+        sm.z *= mJ;
+        sm.w *= mJ;
+        reinterpret_cast<float4*>(out + (size_t)(k0 + slot) * NpP)[grp] = sm;
+        const float4 pu = reinterpret_cast<const float4*>(bufU(b) + slot * NpP)[grp];
+        dot += (double)pu.x * sm.x + (double)pu.y * sm.y + (double)pu.z * sm.z + (double)pu.w * sm.w;
+      }
+    };
     const float* sX = bufX(b);
     const float* sY = bufY(b);
     const float* sU = bufU(b);
@@ -361,24 +422,27 @@ __global__ void __launch_bounds__(256, 4) ipdg_div_blk_kernel(const IpdgParams p
           dqn = 2.0f * (qxm * nx + qym * ny);
           du = 0.0f;
         }
-        sF[e * FSTR + fm] = (dqn + 2.0f * sT[e * 4 + f] * du) * g[5 + f] * 0.5f * g[4];  // g[4] = -1/J
+        sF[e * FS + fm] = (dqn + 2.0f * sT[e * 4 + f] * du) * g[5 + f] * 0.5f * g[4];  // g[4] = -1/J
       }
     }
     __syncthreads();
-    if (slot < ne) {
+    if (B::kShfl || slot < ne) {  // see the grad pass for the kShfl lanes
       const float* xe = sX + slot * NpP;
       const float* ye = sY + slot * NpP;
+      const int l = slot * NG + grp;
+      const float4 x4 = reinterpret_cast<const float4*>(sX)[l], y4 = reinterpret_cast<const float4*>(sY)[l];
       float4 xr = make_float4(0.f, 0.f, 0.f, 0.f), xs = xr, yr = xr, ys = xr, lf = xr;
 #pragma unroll
       for (int j = 0; j < Np; ++j) {
         const float4 dr = ops4[j * NG + grp], ds = ops4[(Np + j) * NG + grp];
-        const float vx = xe[j], vy = ye[j];
+        const float vx = B::kShfl ? col_shfl<NG>(x4, j) : xe[j];
+        const float vy = B::kShfl ? col_shfl<NG>(y4, j) : ye[j];
         xr = f4_fma(dr, vx, xr);
         xs = f4_fma(ds, vx, xs);
         yr = f4_fma(dr, vy, yr);
         ys = f4_fma(ds, vy, ys);
       }
-      const float* fe = sF + slot * FSTR;
+      const float* fe = sF + slot * FS;
 #pragma unroll
       for (int m = 0; m < NFACE; ++m) lf = f4_fma(ops4[(2 * Np + m) * NG + grp], fe[m], lf);
       const float* g = sG + slot * 16;
@@ -388,23 +452,20 @@ __global__ void __launch_bounds__(256, 4) ipdg_div_blk_kernel(const IpdgParams p
       au.y = (rx * xr.y + sx * xs.y) + (ry * yr.y + sy * ys.y) + lf.y;
       au.z = (rx * xr.z + sx * xs.z) + (ry * yr.z + sy * ys.z) + lf.z;
       au.w = (rx * xr.w + sx * xs.w) + (ry * yr.w + sy * ys.w) + lf.w;
-      reinterpret_cast<float4*>(sW + slot * NpP)[grp] = au;
+      if constexpr (B::kShfl) {
+        mass_epilogue(au);
+      } else {
+        reinterpret_cast<float4*>(sW + slot * NpP)[grp] = au;
+      }
     }
-    __syncthreads();
-    if (slot < ne) {
-      // S p = -J M (A p): rows of the symmetric mass matrix cover the thread's 4 nodes
-      const float* we = sW + slot * NpP;
-      float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-      for (int j = 0; j < Np; ++j) s = f4_fma(mass4[j * NG + grp], we[j], s);
-      const float mJ = sG[slot * 16 + 14];  // -J
-      s.x *= mJ;
-      s.y *= mJ;
-      s.z *= mJ;
-      s.w *= mJ;
-      reinterpret_cast<float4*>(out + (size_t)(k0 + slot) * NpP)[grp] = s;
-      const float4 pu = reinterpret_cast<const float4*>(sU + slot * NpP)[grp];
-      dot += (double)pu.x * s.x + (double)pu.y * s.y + (double)pu.z * s.z + (double)pu.w * s.w;
+    if constexpr (!B::kShfl) {
+      __syncthreads();
+      if (slot < ne) {
+        const float* we = sW + slot * NpP;
+        float4 au;
+        au.x = au.y = au.z = au.w = 0.0f;  // unused: the mass product reads we[]
+        mass_epilogue(au, we);
+      }
     }
     __syncthreads();
   }
