@@ -163,8 +163,17 @@ cudaError_t ipdg_launch(int N, int kind, const IpdgParams& p, int sm, cudaStream
   }
 }
 
+// blocks[k] += shift J_k M (the diagonal blocks of S + shift J M)
+__global__ void k_block_shift(int K, int Np, int bstr, const double* __restrict__ geom, const double* __restrict__ M,
+                              double shift, double* __restrict__ blocks) {
+  const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (g >= (int64_t)K * Np * Np) return;
+  const int k = (int)(g / (Np * Np)), q = (int)(g % (Np * Np));
+  blocks[(size_t)k * bstr + q] += shift * geom[(size_t)k * 16 + 4] * M[q];  // geom slot 4: J
+}
+
 template <int N>
-cudaError_t diag_blocks_n(int K, int dirichlet, const double* geom, const int4* nbr, const double* tau,
+cudaError_t diag_blocks_n(int K, int dirichlet, double shift, const double* geom, const int4* nbr, const double* tau,
                           const double* Dr, const double* Ds, const double* L, const double* M, double* blocks,
                           float* blocks32, int bstr, int* status, cudaStream_t s) {
   using O = Order<N>;
@@ -173,15 +182,21 @@ cudaError_t diag_blocks_n(int K, int dirichlet, const double* geom, const int4* 
                                                                          M, blocks, bstr);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
+  if (shift != 0.0) {
+    const int64_t m = n * O::Np;
+    k_block_shift<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(K, O::Np, bstr, geom, M, shift, blocks);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
   block_invert_kernel<N><<<K, 128, 0, s>>>(K, blocks, blocks32, bstr, status);
   return cudaGetLastError();
 }
 
-cudaError_t diag_blocks(int N, int K, int dirichlet, const double* geom, const int4* nbr, const double* tau,
-                        const double* Dr, const double* Ds, const double* L, const double* M, double* blocks,
-                        float* blocks32, int bstr, int* status, cudaStream_t s) {
+cudaError_t diag_blocks(int N, int K, int dirichlet, double shift, const double* geom, const int4* nbr,
+                        const double* tau, const double* Dr, const double* Ds, const double* L, const double* M,
+                        double* blocks, float* blocks32, int bstr, int* status, cudaStream_t s) {
 #define DGK_DB(n) \
-  case n: return diag_blocks_n<n>(K, dirichlet, geom, nbr, tau, Dr, Ds, L, M, blocks, blocks32, bstr, status, s);
+  case n:          \
+    return diag_blocks_n<n>(K, dirichlet, shift, geom, nbr, tau, Dr, Ds, L, M, blocks, blocks32, bstr, status, s);
   switch (N) {
     DGK_DB(1) DGK_DB(2) DGK_DB(3) DGK_DB(4) DGK_DB(5) DGK_DB(6) DGK_DB(7) DGK_DB(8)
     default: return cudaErrorInvalidValue;
@@ -190,6 +205,21 @@ cudaError_t diag_blocks(int N, int K, int dirichlet, const double* geom, const i
 }
 
 // ---------------------------------------------------------------- vector kernels
+// sum of x over valid nodes (padding excluded) into *out
+__global__ void k_valid_sum(size_t n, int NpP, int Np, const double* __restrict__ x, double* out) {
+  __shared__ double red[16];
+  double s = 0.0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    if ((int)(i % NpP) < Np) s += x[i];
+  s = block_sum(s, red);
+  if (threadIdx.x == 0) atomicAdd(out, s);
+}
+// x -= *c / count on valid nodes (c read on the device)
+__global__ void k_sub_mean(size_t n, int NpP, int Np, const double* __restrict__ c, double count, double* x) {
+  const double m = *c / count;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    if ((int)(i % NpP) < Np) x[i] -= m;
+}
 __global__ void k_r64_to_r32(size_t n, const double* __restrict__ r, double scale, float* __restrict__ out) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
     out[i] = (float)(r[i] * scale);
@@ -249,6 +279,8 @@ struct IpdgState {
   float* ops_blk32 = nullptr;  // rows Dr^T | Ds^T | LIFT^T, strong form, padded to NpP columns
   float* mass_blk32 = nullptr; // rows of M padded to NpP columns
   uint8_t* bcdir = nullptr;    // per boundary node condition type (dgc_laplace_set_bc_types), or NULL
+  double shift = 0.0;          // S = -J M (A - shift I) (dgc_laplace_set_shift)
+  double* bproj = nullptr;     // projected right-hand side of a singular (all-Neumann) solve
   int* bcells = nullptr;       // cells with a boundary face
   int n_bcells = 0;
   void* mass64 = nullptr;      // padded M in FP64 / FP32
@@ -295,6 +327,7 @@ dgk::IpdgParams base(const dgc_handle_s* h) {
   p.mass_blk = h->ipdg->mass_blk32;
   p.binv_pk = h->ipdg->binv_pk32;
   p.bcdir = h->ipdg->bcdir;
+  p.shift = h->ipdg->shift;
   p.status = h->d_status;
   return p;
 }
@@ -327,10 +360,10 @@ enum { W_X = 0, W_R = 1, W_Z = 2, W_P = 3, W_AP = 6, W_QX = 7, W_QY = 8, W_T = 9
 int ipdg_build_preconditioner(dgc_handle_s* h, cudaStream_t s) {
   IpdgState* st = h->ipdg;
   if (st->ready) return DGC_OK;
-  if (!h->desc.dirichlet) return set_error(DGC_ERR_UNSUPPORTED, "block-Jacobi CG needs Dirichlet boundaries (SPD form)");
   if (st->bcdir)
-    return set_error(DGC_ERR_UNSUPPORTED, "block-Jacobi CG needs uniform Dirichlet boundaries (clear the per-node types)");
-  cudaError_t e = dgk::diag_blocks(h->N, h->K, 1, h->d_geom, reinterpret_cast<const int4*>(h->d_nbr), h->d_tau,
+    return set_error(DGC_ERR_UNSUPPORTED, "block-Jacobi CG needs uniform boundary types (clear the per-node types)");
+  cudaError_t e = dgk::diag_blocks(h->N, h->K, h->desc.dirichlet, st->shift, h->d_geom,
+                                   reinterpret_cast<const int4*>(h->d_nbr), h->d_tau,
                                    st->dense64, st->dense64 + (size_t)h->Np * h->Np,
                                    st->dense64 + (size_t)2 * h->Np * h->Np,
                                    st->dense64 + (size_t)2 * h->Np * h->Np + (size_t)h->Np * 3 * h->Nfp,
@@ -466,6 +499,7 @@ void ipdg_free(dgc_handle_s* h) {
   cudaFree(st->mass_blk32);
   cudaFree(st->bcdir);
   cudaFree(st->bcells);
+  cudaFree(st->bproj);
   cudaFree(st->mass64);
   cudaFree(st->mass32);
   cudaFree(st->dense64);
@@ -664,6 +698,21 @@ extern "C" int dgc_pcg_solve(dgc_handle h, const double* b, double* x, const dgc
   const auto t0 = std::chrono::steady_clock::now();
   const size_t n = nvec(h);
   dgc_solve_stats S{};
+  // all-Neumann without shift: S is singular with the constants as null space;
+  // solve with the right-hand side projected onto its range (zero sum over the
+  // valid nodes) and return the solution with zero mean
+  const bool singular = !h->desc.dirichlet && st->shift == 0.0;
+  const double count = (double)h->K * h->Np;
+  if (singular) {
+    if (!st->bproj) CKI(cudaMalloc(&st->bproj, n * 8));
+    CKI(cudaMemcpyAsync(st->bproj, b, n * 8, cudaMemcpyDeviceToDevice, s));
+    CKI(cudaMemsetAsync(st->dots, 0, 8, s));
+    dgk::k_valid_sum<<<grid_for(h, n), 256, 0, s>>>(n, h->NpP, h->Np, b, st->dots);
+    dgk::k_sub_mean<<<grid_for(h, n), 256, 0, s>>>(n, h->NpP, h->Np, st->dots, count, st->bproj);
+    CKI(cudaGetLastError());
+    h->launches += 2;
+    b = st->bproj;
+  }
   // ||b||^2
   CKI(cudaMemsetAsync(st->dots, 0, 8, s));
   dgk::k_dot<double><<<grid_for(h, n), 256, 0, s>>>(n, b, b, st->dots);
@@ -713,6 +762,14 @@ extern "C" int dgc_pcg_solve(dgc_handle h, const double* b, double* x, const dgc
   S.outer_iterations = outer;
   S.iterations = S.inner_iterations;
   CKI(cudaStreamSynchronize(s));
+  if (singular) {  // the null-space component of x: zero mean
+    CKI(cudaMemsetAsync(st->dots, 0, 8, s));
+    dgk::k_valid_sum<<<grid_for(h, n), 256, 0, s>>>(n, h->NpP, h->Np, x, st->dots);
+    dgk::k_sub_mean<<<grid_for(h, n), 256, 0, s>>>(n, h->NpP, h->Np, st->dots, count, x);
+    CKI(cudaGetLastError());
+    CKI(cudaStreamSynchronize(s));
+    h->launches += 2;
+  }
   S.final_relres = bb > 0.0 ? std::sqrt(rr / bb) : 0.0;
   S.converged = rr <= tol2 ? 1 : 0;
   S.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -777,5 +834,16 @@ extern "C" int dgc_laplace_bc_rhs(dgc_handle h, const double* g, const double* h
   }
   if (e != cudaSuccess) return cuda_err(e, "boundary-data kernel");
   if (st->n_bcells) ++h->launches;
+  return DGC_OK;
+}
+
+extern "C" int dgc_laplace_set_shift(dgc_handle h, double shift) {
+  if (int rc = check_laplace(h)) return rc;
+  if (!(shift >= 0.0)) return set_error(DGC_ERR_ARG, "shift must be >= 0");
+  IpdgState* st = h->ipdg;
+  if (st->shift != shift) {
+    st->shift = shift;
+    st->ready = false;  // the block-Jacobi blocks depend on the shift
+  }
   return DGC_OK;
 }

@@ -68,6 +68,7 @@ struct IpdgParams {
   const void* mass_blk; // rows of M, padded to NpP columns
   const void* binv_pk;  // [K][PK] packed upper triangles of the block inverses
   const uint8_t* bcdir; // per boundary node: 1 Dirichlet, 0 Neumann (NULL: `dirichlet` everywhere)
+  double shift;         // SPD modes: S = -J M (A - shift I) (Helmholtz-type operators; 0 = laplace)
   CgScalars* cg;
   double* dot_out;      // DIV_SPD_DOT / DIV_RESID: accumulated dot product
   int slot;             // iteration slot (i mod 3)
@@ -369,7 +370,7 @@ __global__ void __launch_bounds__(256) ipdg_div_kernel(const IpdgParams p) {
       if (act) static_cast<R*>(p.out)[(size_t)(k0 + e) * NpP + i] = au;
     } else {
       // S u = -J M (A u): the mass matrix mixes the element's nodes
-      if (act) t.W()[e * NpP + i] = au;
+      if (act) t.W()[e * NpP + i] = au - (R)p.shift * t.Cc()[e * NpP + i];  // (A - shift I) u
       __syncthreads();
       if (act) {
         const R* we = t.W() + e * NpP;

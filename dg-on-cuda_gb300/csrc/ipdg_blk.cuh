@@ -452,6 +452,14 @@ __global__ void __launch_bounds__(256, 4) ipdg_div_blk_kernel(const IpdgParams p
       au.y = (rx * xr.y + sx * xs.y) + (ry * yr.y + sy * ys.y) + lf.y;
       au.z = (rx * xr.z + sx * xs.z) + (ry * yr.z + sy * ys.z) + lf.z;
       au.w = (rx * xr.w + sx * xs.w) + (ry * yr.w + sy * ys.w) + lf.w;
+      {  // (A - shift I) p
+        const float sh = (float)p.shift;
+        const float4 u4 = reinterpret_cast<const float4*>(bufU(b))[l];
+        au.x -= sh * u4.x;
+        au.y -= sh * u4.y;
+        au.z -= sh * u4.z;
+        au.w -= sh * u4.w;
+      }
       if constexpr (B::kShfl) {
         mass_epilogue(au);
       } else {

@@ -104,6 +104,7 @@ def lib():
             L.dgc_mass_apply.argtypes = [_vp, _vp, _vp, _vp]
             L.dgc_boundary_nodes.argtypes = [_vp, _dp]
             L.dgc_laplace_set_bc_types.argtypes = [_vp, C.c_void_p]
+            L.dgc_laplace_set_shift.argtypes = [_vp, C.c_double]
             L.dgc_laplace_bc_rhs.argtypes = [_vp, _vp, _vp, _vp, _vp]
             L.dgc_adv1d_create.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(_vp)]
             L.dgc_adv1d_destroy.argtypes = [_vp]
@@ -412,6 +413,10 @@ class Discretization:
         out = self.empty_state() if out is None else out
         _check(lib().dgc_laplace_apply(self._h, _ptr(u), _ptr(out), _stream(stream)))
         return out
+
+    def set_shift(self, shift: float) -> None:
+        """SPD form S = -J M (A - shift I) for spd(), pcg() and the block-Jacobi blocks."""
+        _check(lib().dgc_laplace_set_shift(self._h, shift))
 
     def set_bc_types(self, is_dirichlet=None) -> None:
         """Per-boundary-node condition types (bool array in boundary_nodes() order); None = uniform."""

@@ -236,6 +236,13 @@ int dgc_div_apply(dgc_handle h, const void* ux, const void* uy, void* out, const
  * u and out in the handle's precision. */
 int dgc_laplace_apply(dgc_handle h, const void* u, void* out, void* stream);
 
+/* Shift of the SPD form: S = -blockdiag(J_k M) (A - shift I) = S_0 + shift J M
+ * for the Helmholtz-type systems (A - shift I) u = f of implicit diffusion
+ * steps (examples/stokes_2d/stokes_2d.h:464-481 assembles A - 1.5/dt I).
+ * Used by dgc_laplace_spd_apply, dgc_pcg_solve and the block-Jacobi blocks
+ * (rebuilt when the shift changes); shift >= 0, default 0. */
+int dgc_laplace_set_shift(dgc_handle h, double shift);
+
 /* Boundary condition type per boundary face node (replaces the
  * is_dirichlet(x, y) callback of the reference's boundary objects,
  * src/laplace_2d.h:179, 233): flags[b] != 0 Dirichlet, 0 Neumann, boundary
@@ -284,7 +291,9 @@ typedef struct dgc_solve_stats {
 } dgc_solve_stats;
 
 /* Solve S x = b with block-Jacobi preconditioned CG (b, x FP64 device
- * vectors, native layout; x holds the initial guess).  No reference
+ * vectors, native layout; x holds the initial guess).  All-Neumann handles
+ * without shift have the constants as null space: b is projected onto the
+ * range (zero sum over the valid nodes) and x returned with zero mean.  No reference
  * counterpart: the reference assembles the matrix column by column and calls
  * cuSOLVER-Sp QR (examples/poisson_2d/main.cpp:130-223).  Returns
  * DGC_ERR_NOT_CONVERGED (with stats filled) if the tolerance is not met. */

@@ -213,3 +213,56 @@ def test_laplace_mixed_conditions_match_oracle(N):
         D.set_bc_types(isd)
         assert relerr(D.download(D.laplace(D.upload(u))), o.laplace_bc(u, isd, tau_mode=1)) < tol
         assert relerr(D.download(D.laplace_bc_rhs(g, h)), o.laplace_bc_rhs(isd, g, h, tau_mode=1)) < tol
+
+
+def dense_spd(D):
+    """S (FP64, through dgc_laplace_spd_apply) as a dense matrix over the valid nodes."""
+    K, Np, NpP = D.K, D.Np, D.NpP
+    idx = [k * NpP + i for k in range(K) for i in range(Np)]
+    cols = []
+    for j in idx:
+        e = torch.zeros(D.state_len, dtype=torch.float64, device="cuda")
+        e[j] = 1.0
+        cols.append(D.spd(e).cpu().numpy()[idx])
+    return np.stack(cols, 1), idx
+
+
+def test_shifted_spd_form_and_helmholtz_solve():
+    m = meshes.jittered_square(4, 12)
+    D = dg.Discretization(m, "laplace", 3, dg.F64, tau=dg.TAU_SCALED, dirichlet=True)
+    u = torch.from_numpy(np.random.default_rng(0).standard_normal(D.state_len)).cuda()
+    s0 = D.spd(u).cpu().numpy()
+    mu = D.mass(u).cpu().numpy()
+    gamma = 37.5
+    D.set_shift(gamma)
+    assert relerr(D.spd(u).cpu().numpy(), s0 + gamma * mu) < 1e-12
+    S, idx = dense_spd(D)
+    assert np.allclose(S, S.T, atol=1e-10 * np.abs(S).max())
+    b = D.mass(u)
+    x, st = D.pcg(b, rtol=1e-12)
+    xd = np.linalg.solve(S, b.cpu().numpy()[idx])
+    assert st["converged"] and relerr(x.cpu().numpy()[idx], xd) < 1e-9
+    xm, stm = D.pcg(b, mode=dg.SOLVE_MIXED_IR, rtol=1e-11)
+    assert stm["converged"] and relerr(xm.cpu().numpy()[idx], xd) < 1e-8
+    D.set_shift(0.0)
+    assert relerr(D.spd(u).cpu().numpy(), s0) < 1e-15
+
+
+def test_all_neumann_pcg_solves_the_consistent_system():
+    m = meshes.jittered_square(4, 13)
+    D = dg.Discretization(m, "laplace", 2, dg.F64, tau=dg.TAU_SCALED, dirichlet=False)
+    S, idx = dense_spd(D)
+    w = np.linalg.eigvalsh(0.5 * (S + S.T))
+    assert abs(w[0]) < 1e-8 * w[-1] and w[1] > 1e-8 * w[-1]     # one-dimensional null space
+    rng = np.random.default_rng(1)
+    bv = np.zeros(D.state_len)
+    bv[idx] = rng.standard_normal(len(idx))
+    b = torch.from_numpy(bv).cuda()
+    for mode in (dg.SOLVE_FP64_PCG, dg.SOLVE_MIXED_IR):
+        x, st = D.pcg(b, mode=mode, rtol=1e-10)
+        assert st["converged"]
+        xs = x.cpu().numpy()[idx]
+        bp = bv[idx] - bv[idx].mean()
+        ref = np.linalg.lstsq(S, bp, rcond=None)[0]
+        assert abs(xs.mean()) < 1e-10 * np.abs(xs).max()
+        assert relerr(xs, ref - ref.mean()) < 1e-7
