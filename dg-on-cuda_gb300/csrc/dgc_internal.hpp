@@ -57,6 +57,8 @@ void ipdg_operators_changed(dgc_handle_s* h);
 // block-Jacobi inverse of the SPD laplace form (built once), and z = Binv r (FP64)
 int ipdg_build_preconditioner(dgc_handle_s* h, cudaStream_t s);
 int ipdg_block_jacobi_apply(dgc_handle_s* h, const double* r, double* z, cudaStream_t s);
+// device list of the cells with a boundary face (laplace handles)
+int ipdg_boundary_cells(const dgc_handle_s* h, const int** cells, int* n);
 // out = S u with the FP32 kernels (any laplace handle; one field, native layout)
 int ipdg_spd_apply_f32(dgc_handle_s* h, const float* u, float* out, cudaStream_t s);
 // stage-kernel parameters of a handle (geometry, operators, physics; no buffers)

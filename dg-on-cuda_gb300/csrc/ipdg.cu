@@ -114,6 +114,18 @@ cudaError_t bc_rhs_launch(int N, int ncells, const IpdgParams& p, const int* cel
 #undef DGK_BC
 }
 
+template <typename R>
+cudaError_t bc_jump_launch(int N, int ncells, const IpdgParams& p, const int* cells, R* out, cudaStream_t s) {
+  if (ncells == 0) return cudaSuccess;
+#define DGK_BJ(n) \
+  case n: ipdg_bc_jump_kernel<R, n><<<ncells, 64, 0, s>>>(p, cells, out); return cudaGetLastError();
+  switch (N) {
+    DGK_BJ(1) DGK_BJ(2) DGK_BJ(3) DGK_BJ(4) DGK_BJ(5) DGK_BJ(6) DGK_BJ(7) DGK_BJ(8)
+    default: return cudaErrorInvalidValue;
+  }
+#undef DGK_BJ
+}
+
 // floats per packed block (IpdgBlk<N>::PK) for the allocation on the host
 int packed_stride(int N) {
   switch (N) {
@@ -283,6 +295,10 @@ struct IpdgState {
   double* bproj = nullptr;     // projected right-hand side of a singular (all-Neumann) solve
   int* bcells = nullptr;       // cells with a boundary face
   int n_bcells = 0;
+  int* jcells = nullptr;       // boundary cells and their face neighbours (ipdg_bc_jump_kernel)
+  int n_jcells = 0;
+  int bc_data_mode = DGC_BC_DATA_REFERENCE;
+  void* qd = nullptr;          // lifted Dirichlet data q_d, 2 x K x NpP in the handle's precision
   void* mass64 = nullptr;      // padded M in FP64 / FP32
   void* mass32 = nullptr;
   double* dense64 = nullptr;   // row-major Dr | Ds | L | M (FP64) for the block set-up
@@ -469,6 +485,20 @@ int ipdg_init(dgc_handle_s* h) {
     st->n_bcells = (int)bc.size();
     CKI(cudaMalloc(&st->bcells, std::max<size_t>(bc.size(), 1) * sizeof(int)));
     if (!bc.empty()) CKI(cudaMemcpy(st->bcells, bc.data(), bc.size() * sizeof(int), cudaMemcpyHostToDevice));
+    std::vector<char> mark(h->K, 0);
+    for (int k : bc) {
+      mark[k] = 1;
+      for (int f = 0; f < 3; ++f) {
+        const int nb = h->mesh.nbr[4 * (size_t)k + f];
+        if (nb >= 0) mark[nb >> 2] = 1;
+      }
+    }
+    std::vector<int> jc;
+    for (int k = 0; k < h->K; ++k)
+      if (mark[k]) jc.push_back(k);
+    st->n_jcells = (int)jc.size();
+    CKI(cudaMalloc(&st->jcells, std::max<size_t>(jc.size(), 1) * sizeof(int)));
+    if (!jc.empty()) CKI(cudaMemcpy(st->jcells, jc.data(), jc.size() * sizeof(int), cudaMemcpyHostToDevice));
   }
   CKI(cudaMalloc(&st->ops_blk32, (size_t)(2 * Np + NF) * h->NpP * 4));
   CKI(cudaMalloc(&st->mass_blk32, (size_t)Np * h->NpP * 4));
@@ -499,6 +529,8 @@ void ipdg_free(dgc_handle_s* h) {
   cudaFree(st->mass_blk32);
   cudaFree(st->bcdir);
   cudaFree(st->bcells);
+  cudaFree(st->jcells);
+  cudaFree(st->qd);
   cudaFree(st->bproj);
   cudaFree(st->mass64);
   cudaFree(st->mass32);
@@ -513,6 +545,13 @@ void ipdg_free(dgc_handle_s* h) {
   cudaFreeHost(st->h_dots);
   delete st;
   h->ipdg = nullptr;
+}
+
+int ipdg_boundary_cells(const dgc_handle_s* h, const int** cells, int* n) {
+  if (!h->ipdg) return set_error(DGC_ERR_UNSUPPORTED, "not a laplace handle");
+  *cells = h->ipdg->bcells;
+  *n = h->ipdg->n_bcells;
+  return DGC_OK;
 }
 
 void ipdg_operators_changed(dgc_handle_s* h) {
@@ -822,18 +861,39 @@ extern "C" int dgc_laplace_bc_rhs(dgc_handle h, const double* g, const double* h
   if (!out) return set_error(DGC_ERR_ARG, "null output");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   IpdgState* st = h->ipdg;
-  cudaError_t e;
-  if (h->prec == DGC_F64) {
-    dgk::IpdgParams p = base<double>(h);
-    p.mats = h->d_mats64[1];
-    e = dgk::bc_rhs_launch<double>(h->N, st->n_bcells, p, st->bcells, g, hn, static_cast<double*>(out), s);
-  } else {
-    dgk::IpdgParams p = base<float>(h);
-    p.mats = h->d_mats32[1];
-    e = dgk::bc_rhs_launch<float>(h->N, st->n_bcells, p, st->bcells, g, hn, static_cast<float*>(out), s);
+  const bool jump = st->bc_data_mode == DGC_BC_DATA_CONSISTENT && g && st->n_bcells;
+  const size_t n = nvec(h), esz = h->prec == DGC_F64 ? 8 : 4;
+  if (jump && !st->qd) {  // zero off the boundary cells for good: only those are ever written
+    CKI(cudaMalloc(&st->qd, 2 * n * esz));
+    CKI(cudaMemset(st->qd, 0, 2 * n * esz));
   }
+  cudaError_t e;
+  auto run = [&](auto zero, void* const* mats) {
+    using R = decltype(zero);
+    dgk::IpdgParams p = base<R>(h);
+    p.mats = mats[1];
+    if (jump) {
+      p.qx = st->qd;
+      p.qy = static_cast<char*>(st->qd) + n * esz;
+    }
+    e = dgk::bc_rhs_launch<R>(h->N, st->n_bcells, p, st->bcells, g, hn, static_cast<R*>(out), s);
+    if (e == cudaSuccess && jump) e = dgk::bc_jump_launch<R>(h->N, st->n_jcells, p, st->jcells, static_cast<R*>(out), s);
+  };
+  if (h->prec == DGC_F64)
+    run(0.0, h->d_mats64);
+  else
+    run(0.0f, h->d_mats32);
   if (e != cudaSuccess) return cuda_err(e, "boundary-data kernel");
   if (st->n_bcells) ++h->launches;
+  if (jump && st->n_jcells) ++h->launches;
+  return DGC_OK;
+}
+
+extern "C" int dgc_laplace_set_bc_data_mode(dgc_handle h, int mode) {
+  if (int rc = check_laplace(h)) return rc;
+  if (mode != DGC_BC_DATA_REFERENCE && mode != DGC_BC_DATA_CONSISTENT)
+    return set_error(DGC_ERR_ARG, "unknown boundary-data mode");
+  h->ipdg->bc_data_mode = mode;
   return DGC_OK;
 }
 

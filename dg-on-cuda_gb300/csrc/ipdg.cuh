@@ -548,6 +548,10 @@ __global__ void __launch_bounds__(64) ipdg_bc_rhs_kernel(const IpdgParams p, con
     }
     qx[t] = nJ * ax;
     qy[t] = nJ * ay;
+    if (p.qx) {  // kept for ipdg_bc_jump_kernel
+      static_cast<R*>(p.qx)[(size_t)c * NpP + t] = nJ * ax;
+      static_cast<R*>(p.qy)[(size_t)c * NpP + t] = nJ * ay;
+    }
   }
   __syncthreads();
   if (t < Np) {
@@ -561,6 +565,51 @@ __global__ void __launch_bounds__(64) ipdg_bc_rhs_kernel(const IpdgParams p, con
     }
     for (int m = 0; m < NFACE; ++m) lf += LT[m * Np + t] * hq[m];
     out[(size_t)c * NpP + t] += (G[0] * xr + G[2] * xs) + (G[1] * yr + G[3] * ys) + nJ * lf;
+  }
+}
+
+// The jumps of the lifted Dirichlet data q_d that apply_inhomogeneous_as_rhs
+// leaves out (its second pass adds only boundary-face terms, laplace_2d.h:
+// 302-347, where apply_homogeneous's dqN also holds the jumps of q across
+// interior faces and 2 q.n on Neumann faces, :222-242).  q_d as stored by
+// ipdg_bc_rhs_kernel in p.qx / p.qy (zero off the boundary cells); on each
+// listed cell (a boundary cell or a face neighbour of one), one CTA of 64
+// threads adds
+//   -LIFT(dqN faceJ / 2) / J,  dqN = (q_d(c) - q_d(nb)).n on interior faces,
+//   2 q_d(c).n on Neumann faces, 0 on Dirichlet faces.
+template <typename R, int N>
+__global__ void __launch_bounds__(64) ipdg_bc_jump_kernel(const IpdgParams p, const int* __restrict__ cells,
+                                                          R* __restrict__ out) {
+  using O = Order<N>;
+  constexpr int Np = O::Np, NpP = O::NpP, Nfp = O::Nfp, NFACE = O::Nface;
+  constexpr int kD = IpdgConfig<R, N>::kD;
+  __shared__ R tl[NFACE];
+  const int c = cells[blockIdx.x];
+  const int t = threadIdx.x;
+  const R* G = static_cast<const R*>(p.geom) + (size_t)c * 16;
+  const R* LT = static_cast<const R*>(p.mats) + 2 * kD;
+  const R* qx = static_cast<const R*>(p.qx);
+  const R* qy = static_cast<const R*>(p.qy);
+  const int4 n4 = p.nbr[c];
+  for (int m = t; m < NFACE; m += blockDim.x) {
+    const int f = m / Nfp, d = m - f * Nfp;
+    const int nb = f == 0 ? n4.x : (f == 1 ? n4.y : n4.z);
+    const size_t ia = (size_t)c * NpP + fmask<N>(f, d);
+    const R nx = G[8 + f], ny = G[11 + f];
+    R dqn;
+    if (nb >= 0) {
+      const size_t ib = (size_t)(nb >> 2) * NpP + fmask<N>(nb & 3, Nfp - 1 - d);
+      dqn = (qx[ia] - qx[ib]) * nx + (qy[ia] - qy[ib]) * ny;
+    } else {
+      dqn = bc_dirichlet<N>(p, nb, d) ? (R)0 : (R)2 * (qx[ia] * nx + qy[ia] * ny);
+    }
+    tl[m] = dqn * (G[5 + f] / (R)2);
+  }
+  __syncthreads();
+  if (t < Np) {
+    R lf = 0;
+    for (int m = 0; m < NFACE; ++m) lf += LT[m * Np + t] * tl[m];
+    out[(size_t)c * NpP + t] += G[4] * lf;  // G[4] = -1/J
   }
 }
 

@@ -62,6 +62,7 @@ class SolveStats(C.Structure):
 
 
 SOLVE_FP64_PCG, SOLVE_MIXED_IR = 0, 1
+BC_DATA_REFERENCE, BC_DATA_CONSISTENT = 0, 1
 ERR_NOT_CONVERGED = -6
 
 _lock = threading.Lock()
@@ -106,6 +107,13 @@ def lib():
             L.dgc_laplace_set_bc_types.argtypes = [_vp, C.c_void_p]
             L.dgc_laplace_set_shift.argtypes = [_vp, C.c_double]
             L.dgc_laplace_bc_rhs.argtypes = [_vp, _vp, _vp, _vp, _vp]
+            L.dgc_laplace_set_bc_data_mode.argtypes = [_vp, C.c_int]
+            L.dgc_stokes_create.argtypes = [C.c_int, _dp, C.c_int, _ip, C.c_int, C.POINTER(_vp)]
+            L.dgc_stokes_destroy.argtypes = [_vp]
+            L.dgc_stokes_handles.argtypes = [_vp, C.POINTER(_vp), C.POINTER(_vp)]
+            L.dgc_stokes_set_solver.argtypes = [_vp, C.POINTER(SolveOpts)]
+            L.dgc_stokes_step.argtypes = [_vp, _vp, _vp, _vp, _vp, C.c_double, C.c_void_p, _vp, _vp, _vp,
+                                          C.POINTER(SolveStats), _vp]
             L.dgc_adv1d_create.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(_vp)]
             L.dgc_adv1d_destroy.argtypes = [_vp]
             L.dgc_adv1d_info.argtypes = [_vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
@@ -245,14 +253,29 @@ class Discretization:
         self.state_len = info.state_len
         self.precision = precision
 
+    @classmethod
+    def _borrow(cls, h, owner):
+        """View of a handle owned by another object (kept alive through owner)."""
+        self = cls.__new__(cls)
+        self._h = _vp(h)
+        self._owner = owner
+        info = Info()
+        _check(lib().dgc_get_info(self._h, C.byref(info)))
+        self.info = info
+        self.K, self.N, self.Np, self.NpP = info.num_cells, info.order, info.np, info.np_padded
+        self.Nfp, self.Nf = info.nfp, info.num_fields
+        self.state_len = info.state_len
+        self.precision = F64
+        return self
+
     def __del__(self):
         h = getattr(self, "_h", None)
-        if h is not None and h.value:
+        if h is not None and h.value and getattr(self, "_owner", None) is None:
             try:
                 lib().dgc_destroy(h)
             except Exception:
                 pass
-            self._h = None
+        self._h = None
 
     # ---------------------------------------------------------------- host-side info
     @property
@@ -417,6 +440,11 @@ class Discretization:
     def set_shift(self, shift: float) -> None:
         """SPD form S = -J M (A - shift I) for spd(), pcg() and the block-Jacobi blocks."""
         _check(lib().dgc_laplace_set_shift(self._h, shift))
+
+    def set_bc_data_mode(self, mode: int) -> None:
+        """BC_DATA_REFERENCE (apply_inhomogeneous_as_rhs as the reference forms it)
+        or BC_DATA_CONSISTENT (plus the jumps of the lifted Dirichlet data)."""
+        _check(lib().dgc_laplace_set_bc_data_mode(self._h, mode))
 
     def set_bc_types(self, is_dirichlet=None) -> None:
         """Per-boundary-node condition types (bool array in boundary_nodes() order); None = uniform."""

@@ -259,6 +259,20 @@ int dgc_laplace_set_bc_types(dgc_handle h, const uint8_t* flags);
  * dgc_laplace_apply minus this contribution. */
 int dgc_laplace_bc_rhs(dgc_handle h, const double* g, const double* hn, void* out, void* stream);
 
+/* What dgc_laplace_bc_rhs adds for Dirichlet data.  REFERENCE (default):
+ * exactly apply_inhomogeneous_as_rhs, whose second pass adds the lifted data
+ * q_d = -LIFT(n g faceJ / 2) / J only through boundary-face terms
+ * (src/laplace_2d.h:302-347).  CONSISTENT: also the jumps of q_d across
+ * interior faces and 2 q_d.n on Neumann faces, which apply_homogeneous has for
+ * the same lift (same file:222-242); dgc_laplace_apply(u) minus this term is
+ * then the affine operator of the scheme, exact on polynomials of degree <= N
+ * with their own boundary data.  The two differ only for non-zero Dirichlet
+ * data (the examples' Poisson problem has none; the Stokes example's
+ * velocity solves do), and one extra launch over the boundary cells and their
+ * neighbours. */
+typedef enum dgc_bc_data_mode { DGC_BC_DATA_REFERENCE = 0, DGC_BC_DATA_CONSISTENT = 1 } dgc_bc_data_mode;
+int dgc_laplace_set_bc_data_mode(dgc_handle h, int mode);
+
 /* out = S u = -blockdiag(J_k M) A u: the mass-weighted form, symmetric
  * positive definite for Dirichlet problems. */
 int dgc_laplace_spd_apply(dgc_handle h, const void* u, void* out, void* stream);
@@ -383,6 +397,50 @@ int dgc_adv1d_rhs(dgc_adv1d a, const void* q, double t, void* out, void* stream)
  * the operator and 8 axpy calls).  work: 3 state vectors of scratch. */
 int dgc_adv1d_rk4_step(dgc_adv1d a, void* q, double t, double dt, void* const* work, void* stream);
 int64_t dgc_adv1d_launch_count(dgc_adv1d a);
+
+/* ---- the Stokes example's dual-splitting step (examples/stokes_2d) ---------
+ * u_t = lap u - grad p, div u = 0 advanced by BDF2 dual splitting (Fehn et al.
+ * 2017): u~ = (4 u^n - u^(n-1)) / 3; A_N p = 1.5/dt div u~ + Neumann data;
+ * u~ -= 2 dt / 3 grad p; (A_D - 1.5/dt I) u^(n+1) = -1.5/dt u~ + Dirichlet
+ * data, with the laplace_2d operator (tau = 1) on the pressure (all Neumann)
+ * and the velocity (all Dirichlet).  Velocity and pressure are FP64 device
+ * vectors in the native layout of a laplace handle (K x NpP).  The velocity
+ * handle takes its Dirichlet data as the reference does (dgc_laplace_set_
+ * bc_data_mode REFERENCE); with that term the example's scheme does not
+ * converge to its analytic solution, with CONSISTENT on the velocity handle
+ * (dgc_stokes_handles) it does. */
+typedef struct dgc_stokes_s* dgc_stokes;
+/* Boundary data, FP64 device arrays over the boundary face nodes in
+ * dgc_boundary_nodes order (the reference's boundary objects evaluated there). */
+typedef struct dgc_stokes_bc {
+  const double* ut_x;   /* u_tilde_bc::exterior_val(x, y, 0): 2 (4 g(t^n) - g(t^(n-1))) / 3 */
+  const double* ut_y;
+  const double* dgdt_x; /* the dgdt term of pressure_bc's hp at t^(n+1) (stokes_2d.h:245-248; the
+                           example's lamda g e^(-lamda t), i.e. -dg/dt) */
+  const double* dgdt_y;
+  const double* g_x;    /* u_x_bc / u_y_bc::exterior_val(x, y, 0): 2 g(t^(n+1)) */
+  const double* g_y;
+} dgc_stokes_bc;
+/* Replaces stokes_2d(mesh, order) (examples/stokes_2d/stokes_2d.h:265-276):
+ * two laplace handles on the mesh plus workspace.  order in [1, 8]. */
+int dgc_stokes_create(int num_vertices, const double* vertex_xy, int num_cells, const int32_t* cells, int order,
+                      dgc_stokes* out);
+int dgc_stokes_destroy(dgc_stokes s);
+/* The velocity (Dirichlet) and pressure (Neumann) laplace handles, owned by s:
+ * node coordinates, layout conversion and boundary nodes come from them. */
+int dgc_stokes_handles(dgc_stokes s, dgc_handle* velocity, dgc_handle* pressure);
+/* Solver of the pressure and viscous systems (default: mixed refinement,
+ * rtol 1e-12, maxit 200000). */
+int dgc_stokes_set_solver(dgc_stokes s, const dgc_solve_opts* opts);
+/* One step t^n -> t^(n+1) = t^n + dt (advance_timestep, stokes_2d.h:393-423):
+ * u_prev = u^(n-1), u = u^n; writes u^(n+1) to ux_out / uy_out (which may
+ * alias u_prev, not u) and, when p_out is non-NULL, the zero-mean pressure.
+ * stats sums the three solves (final_relres: the largest).  The reference
+ * solves with a host sparse LU; here both systems run block-Jacobi PCG to
+ * the solver's rtol. */
+int dgc_stokes_step(dgc_stokes s, const double* ux_prev, const double* uy_prev, const double* ux, const double* uy,
+                    double dt, const dgc_stokes_bc* bc, double* ux_out, double* uy_out, double* p_out,
+                    dgc_solve_stats* stats, void* stream);
 
 /* ---- files ------------------------------------------------------------------ */
 

@@ -1004,6 +1004,62 @@ void orc_laplace_bc_rhs(orc* o, const uint8_t* bdir, int tau_mode, const double*
   }
 }
 
+/* The part of the boundary-data contribution that apply_inhomogeneous_as_rhs
+ * (laplace_2d.h:253-348) leaves out.  Its first pass lifts the Dirichlet data
+ * into q_d on the boundary cells, but its second pass adds only their
+ * boundary-face terms; the affine operator of the scheme also has the jumps of
+ * q_d (apply_homogeneous's dqN, laplace_2d.h:222-242):
+ *   out += -LIFT(dqN faceJ / 2) / J on every cell,
+ *   dqN = (q_d(c) - q_d(nb)).n on interior faces, 2 q_d(c).n on Neumann
+ *   boundary faces, 0 on Dirichlet faces (q_d = 0 off the boundary cells).
+ * With it, laplace_apply(u) - bc_rhs - bc_jump is exact on polynomials of
+ * degree <= N with their own boundary data; without it (the reference) it is
+ * not, for non-zero Dirichlet data. */
+void orc_laplace_bc_jump(orc* o, const uint8_t* bdir, const double* g, double* out) {
+  int Np = o->Np, Nfp = o->Nfp;
+  double tlx[3 * ORC_MAX_NFP], tly[3 * ORC_MAX_NFP], tl[3 * ORC_MAX_NFP];
+  size_t n = (size_t)o->K * Np;
+  for (size_t i = 0; i < n; ++i) { o->qx[i] = 0.0; o->qy[i] = 0.0; }
+  if (!g) return;
+  for (int c = 0; c < o->K; ++c) {
+    if (!o->isB[3 * c] && !o->isB[3 * c + 1] && !o->isB[3 * c + 2]) continue;
+    for (int m = 0; m < 3 * Nfp; ++m) { tlx[m] = 0.0; tly[m] = 0.0; }
+    for (int e = 0; e < 3; ++e) {
+      if (!o->isB[3 * c + e]) continue;
+      double nx = o->nx[3 * c + e], ny = o->ny[3 * c + e], fJ = o->faceJ[3 * c + e];
+      for (int i = 0; i < Nfp; ++i) {
+        double v = bc_dir(o, 1, bdir, c, e, i) ? g[o->nbF[3 * c + e] + i] : 0.0;
+        tlx[e * Nfp + i] = nx * v * fJ / 2.0;
+        tly[e * Nfp + i] = ny * v * fJ / 2.0;
+      }
+    }
+    size_t off = (size_t)c * Np;
+    gemv(Np, 3 * Nfp, o->Ls, -1.0 / o->J[c], tlx, 0.0, o->qx + off);
+    gemv(Np, 3 * Nfp, o->Ls, -1.0 / o->J[c], tly, 0.0, o->qy + off);
+  }
+  for (int c = 0; c < o->K; ++c) {
+    size_t off = (size_t)c * Np;
+    int any = 0;
+    for (int e = 0; e < 3; ++e) {
+      int isb = o->isB[3 * c + e], nbc = o->nbC[3 * c + e], nbf = o->nbF[3 * c + e];
+      double nx = o->nx[3 * c + e], ny = o->ny[3 * c + e], fJ = o->faceJ[3 * c + e];
+      for (int i = 0; i < Nfp; ++i) {
+        size_t ia = off + o->Fmask[e][i];
+        double dqN;
+        if (isb) {
+          dqN = bc_dir(o, 1, bdir, c, e, i) ? 0.0 : 2.0 * (o->qx[ia] * nx + o->qy[ia] * ny);
+        } else {
+          size_t ib = (size_t)nbc * Np + o->Fmask[nbf][Nfp - i - 1];
+          dqN = (o->qx[ia] - o->qx[ib]) * nx + (o->qy[ia] - o->qy[ib]) * ny;
+        }
+        tl[e * Nfp + i] = dqN * fJ / 2.0;
+        any |= dqN != 0.0;
+      }
+    }
+    if (any) gemv(Np, 3 * Nfp, o->Ls, -1.0 / o->J[c], tl, 1.0, out + off);
+  }
+}
+
 /* out = -J_k M (A u)_k : the mass-weighted, symmetric positive definite form */
 void orc_spd_apply(orc* o, int tau_mode, const double* u, double* out) {
   int Np = o->Np;

@@ -90,6 +90,9 @@ void orc_laplace_apply(orc* o, int dirichlet, int tau_mode, const double* u, dou
 void orc_laplace_apply_bc(orc* o, const uint8_t* bdir, int tau_mode, const double* u, double* out);
 void orc_laplace_bc_rhs(orc* o, const uint8_t* bdir, int tau_mode, const double* g, const double* h,
                         double* out);
+/* out += the jumps of the lifted Dirichlet data that apply_inhomogeneous_as_rhs
+ * leaves out (the consistent boundary-data term is bc_rhs + bc_jump) */
+void orc_laplace_bc_jump(orc* o, const uint8_t* bdir, const double* g, double* out);
 /* SPD form S u = -blockdiag(J_k M) A u, and its diagonal blocks (K x Np x Np) */
 void orc_spd_apply(orc* o, int tau_mode, const double* u, double* out);
 void orc_spd_diag_blocks(orc* o, int tau_mode, double* blocks);

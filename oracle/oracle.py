@@ -77,6 +77,7 @@ def lib():
             L.orc_mass_apply.argtypes = [C.c_void_p, _dp, _dp]
             L.orc_laplace_apply_bc.argtypes = [C.c_void_p, C.c_void_p, C.c_int, _dp, _dp]
             L.orc_laplace_bc_rhs.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, _dp]
+            L.orc_laplace_bc_jump.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, _dp]
             L.orc_grad.argtypes = [C.c_void_p, _dp, C.c_void_p, C.c_double, _dp, _dp]
             L.orc_div.argtypes = [C.c_void_p, _dp, _dp, C.c_void_p, C.c_void_p, C.c_double, _dp]
             L.orc_pcg.restype = C.c_int
@@ -222,14 +223,18 @@ class Oracle:
         lib().orc_laplace_apply_bc(self._h, f.ctypes.data, tau_mode, u, out)
         return out
 
-    def laplace_bc_rhs(self, is_dirichlet, g=None, h=None, tau_mode: int = 0, out=None) -> np.ndarray:
+    def laplace_bc_rhs(self, is_dirichlet, g=None, h=None, tau_mode: int = 0, out=None,
+                       consistent: bool = False) -> np.ndarray:
         """apply_inhomogeneous_as_rhs: adds the boundary-data contribution to out
-        (zeros when not given); g, h = exterior_val(x, y, 0), exterior_grad_n(x, y, 0)."""
+        (zeros when not given); g, h = exterior_val(x, y, 0), exterior_grad_n(x, y, 0).
+        consistent=True adds the jumps of the lifted Dirichlet data as well."""
         out = np.zeros(self.K * self.Np) if out is None else np.array(out, dtype=np.float64).reshape(-1)
         f = np.ascontiguousarray(is_dirichlet, dtype=np.uint8).reshape(-1)
         g, h = self._opt(g), self._opt(h)
         lib().orc_laplace_bc_rhs(self._h, f.ctypes.data, tau_mode, None if g is None else g.ctypes.data,
                                  None if h is None else h.ctypes.data, out)
+        if consistent:
+            lib().orc_laplace_bc_jump(self._h, f.ctypes.data, None if g is None else g.ctypes.data, out)
         return out
 
     @staticmethod

@@ -1,0 +1,109 @@
+"""The Stokes example's pieces on the CPU: the boundary-data term of
+laplace_2d and the dual-splitting step restated in oracle/stokes_oracle.py.
+
+apply_inhomogeneous_as_rhs (src/laplace_2d.h:253-348) lifts the Dirichlet
+data into q_d on the boundary cells but adds only its boundary-face terms; the
+jumps of q_d across interior faces (which apply_homogeneous's second pass has
+for the same lift) are missing.  With non-zero Dirichlet data the reference's
+`operator()` is then not the affine operator of its scheme, and the Stokes
+example (the one caller with such data) does not converge to its analytic
+solution.  The oracle's bc_jump term restores them; these tests pin both
+forms."""
+import numpy as np
+import pytest
+
+from conftest import oracle  # noqa: F401  (puts oracle/ on sys.path)
+import stokes_oracle as so
+from dgc_gb300 import meshes
+
+POLYS = [
+    ("one", lambda x, y: 1.0 + 0 * x, lambda x, y: 0 * x, 1),
+    ("quad", lambda x, y: x * y - x * x + 0.5 * y, lambda x, y: -2.0 + 0 * x, 2),
+    ("cubic", lambda x, y: x * x * y + 0.3 * y ** 3, lambda x, y: 2.0 * y + 1.8 * y, 3),
+]
+
+
+def _setup(n, N, seed=2):
+    m = meshes.jittered_square(n, seed)
+    return m, so.StokesOracle(m.xy, m.cells, N)
+
+
+@pytest.mark.parametrize("N", [1, 2, 3, 4])
+def test_consistent_data_term_exact_on_polynomials(N):
+    """laplace_apply(u) - bc_rhs(2 u|bdry) - bc_jump = lap u for deg u <= N
+    (exterior_val = 2 g - interior, the Stokes example's velocity condition)."""
+    _, s = _setup(4, N)
+    x, y = (a.reshape(-1) for a in s.o.node_xy())
+    bx, by = s.arr["bx"], s.arr["by"]
+    for name, f, lap, deg in POLYS:
+        if deg > N:
+            continue
+        u = f(x, y)
+        d = s.o.laplace_bc_rhs(np.ones(s.nb, np.uint8), 2.0 * f(bx, by), None, consistent=True)
+        F = s.A_D @ u - d
+        assert np.abs(F - lap(x, y)).max() < 1e-9 * max(1.0, np.abs(s.A_D @ u).max()), name
+
+
+def test_reference_data_term_misses_interior_jumps():
+    """For u = 1, g = 1 the reference's operator() leaves a residual, and only
+    on boundary cells and their face neighbours."""
+    _, s = _setup(6, 2)
+    K, Np = s.K, s.Np
+    u = np.ones(K * Np)
+    d_ref = s.o.laplace_bc_rhs(np.ones(s.nb, np.uint8), 2.0 * np.ones(s.nb), None)
+    d_con = s.o.laplace_bc_rhs(np.ones(s.nb, np.uint8), 2.0 * np.ones(s.nb), None, consistent=True)
+    r_ref = (s.A_D @ u - d_ref).reshape(K, Np)
+    r_con = (s.A_D @ u - d_con).reshape(K, Np)
+    assert np.abs(r_con).max() < 1e-9
+    nc = s.arr["nbCell"].reshape(K, 3)
+    isb = np.array([any(nc[c, f] == c for f in range(3)) for c in range(K)])
+    near = isb | np.array([any(isb[nc[c, f]] for f in range(3)) for c in range(K)])
+    assert np.abs(r_ref).max() > 10.0
+    assert np.abs(r_ref[~near]).max() < 1e-9
+
+
+def test_jump_term_zero_without_dirichlet_data():
+    _, s = _setup(3, 3)
+    h = np.linspace(-1, 1, s.nb)
+    a = s.o.laplace_bc_rhs(np.zeros(s.nb, np.uint8), None, h)
+    b = s.o.laplace_bc_rhs(np.zeros(s.nb, np.uint8), None, h, consistent=True)
+    assert np.array_equal(a, b)
+
+
+def test_hp_matches_analytic_curl_free_case():
+    """hp = dgdt.n + (curl curl term).n: for u^n = u^(n-1) = a gradient field
+    (curl 0) the curl-curl term vanishes and hp = dgdt.n exactly."""
+    _, s = _setup(3, 3)
+    x, y = (a.reshape(-1) for a in s.o.node_xy())
+    ux, uy = 2 * x * y, x * x - y * y  # grad(x^2 y - y^3/3)
+    ddx = np.linspace(0, 1, s.nb)
+    ddy = np.linspace(1, 2, s.nb)
+    hp = s.hp(ux, uy, ux, uy, ddx, ddy)
+    nxb, nyb = [], []
+    nx, ny = s.arr["nx"].reshape(s.K, 3), s.arr["ny"].reshape(s.K, 3)
+    for c in range(s.K):
+        for f in range(3):
+            if s._is_boundary(c, f):
+                nxb += [nx[c, f]] * s.Nfp
+                nyb += [ny[c, f]] * s.Nfp
+    assert np.abs(hp - (ddx * np.array(nxb) + ddy * np.array(nyb))).max() < 1e-10
+
+
+def test_step_convergence_consistent_only():
+    """The dual-splitting step (stokes_2d.h:393-423) reaches the example's
+    analytic solution with the consistent data term, not with the reference's."""
+    m = meshes.jittered_square(4, 1)
+    errs = {}
+    for cons in (False, True):
+        s = so.StokesOracle(m.xy, m.cells, 3, consistent=cons)
+        _, _, t, err = s.run(T=0.01, dt=0.001)
+        assert abs(t - 0.01) < 1e-12
+        errs[cons] = err
+    assert errs[True] < 1e-4
+    assert errs[False] > 1e-2
+
+
+def test_step_error_decreases_with_order():
+    m = meshes.jittered_square(4, 1)
+    e = [so.StokesOracle(m.xy, m.cells, N, consistent=True).run(T=0.01, dt=0.001)[3] for N in (2, 3, 4)]
+    assert e[0] > 10 * e[1] and e[1] > 2 * e[2]
