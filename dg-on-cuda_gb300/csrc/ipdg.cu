@@ -6,6 +6,7 @@
 
 #include <chrono>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -813,7 +814,12 @@ extern "C" int dgc_pcg_solve(dgc_handle h, const double* b, double* x, const dgc
   S.converged = rr <= tol2 ? 1 : 0;
   S.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   if (stats) *stats = S;
-  if (!S.converged) return set_error(DGC_ERR_NOT_CONVERGED, "PCG did not reach the requested tolerance");
+  if (!S.converged) {
+    char msg[160];
+    snprintf(msg, sizeof msg, "PCG did not reach the requested tolerance (relative residual %.3e > %.3e after %d iterations)",
+             S.final_relres, opts->rtol, S.iterations);
+    return set_error(DGC_ERR_NOT_CONVERGED, msg);
+  }
   return DGC_OK;
 }
 

@@ -52,7 +52,7 @@ class Stokes:
     velocity's Dirichlet data with the jumps apply_inhomogeneous_as_rhs leaves
     out (BC_DATA_CONSISTENT); the default reproduces the reference."""
 
-    def __init__(self, mesh, order: int, consistent: bool = False, rtol: float = 1e-12,
+    def __init__(self, mesh, order: int, consistent: bool = False, rtol: float = 1e-10,
                  mode: int = SOLVE_MIXED_IR, maxit: int = 200000):
         xy = np.ascontiguousarray(mesh.xy, dtype=np.float64).reshape(-1)
         cells = np.ascontiguousarray(mesh.cells, dtype=np.int32).reshape(-1)
@@ -79,7 +79,7 @@ class Stokes:
         except Exception:
             pass
 
-    def set_solver(self, rtol: float = 1e-12, mode: int = SOLVE_MIXED_IR, maxit: int = 200000,
+    def set_solver(self, rtol: float = 1e-10, mode: int = SOLVE_MIXED_IR, maxit: int = 200000,
                    inner_rtol: float = 1e-4, max_outer: int = 0, graph: bool = True) -> None:
         self._opts = SolveOpts(mode, rtol, maxit, inner_rtol, max_outer, int(graph))
         _check(lib().dgc_stokes_set_solver(self._h, C.byref(self._opts)))

@@ -430,7 +430,8 @@ int dgc_stokes_destroy(dgc_stokes s);
  * node coordinates, layout conversion and boundary nodes come from them. */
 int dgc_stokes_handles(dgc_stokes s, dgc_handle* velocity, dgc_handle* pressure);
 /* Solver of the pressure and viscous systems (default: mixed refinement,
- * rtol 1e-12, maxit 200000). */
+ * rtol 1e-10, maxit 200000).  The FP64 residual of the singular pressure
+ * system stalls near 1e-16 cond(S), so tighter targets fail on fine meshes. */
 int dgc_stokes_set_solver(dgc_stokes s, const dgc_solve_opts* opts);
 /* One step t^n -> t^(n+1) = t^n + dt (advance_timestep, stokes_2d.h:393-423):
  * u_prev = u^(n-1), u = u^n; writes u^(n+1) to ux_out / uy_out (which may

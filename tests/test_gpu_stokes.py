@@ -7,7 +7,7 @@
 * dgc_stokes_step against the dense restatement of advance_timestep
   (oracle/stokes_oracle.py, direct solves), three steps from the example's
   initial data, both modes: velocity to 1e-9 relative (the GPU solves run to
-  a 1e-13 relative residual), pressure to 1e-7.
+  a 1e-11 relative residual), pressure to 1e-7.
 * The example driver with the consistent data term reaches the analytic
   solution; with the reference's term it does not (as the oracle shows).
 """
@@ -85,7 +85,7 @@ def test_consistent_operator_exact_at_scale(N):
 @pytest.mark.parametrize("N", [2, 3])
 def test_stokes_step_matches_dense_restatement(N, consistent):
     m = meshes.jittered_square(4, 1)
-    S = st.Stokes(m, N, consistent=consistent, rtol=1e-13)
+    S = st.Stokes(m, N, consistent=consistent, rtol=1e-11)
     O = so.StokesOracle(m.xy, m.cells, N, consistent=consistent)
     vs = S.velocity_space
     x, y = (a.reshape(-1) for a in vs.node_xy())
@@ -103,7 +103,7 @@ def test_stokes_step_matches_dense_restatement(N, consistent):
         bc = st.example_boundary_data(O.arr["bx"], O.arr["by"], t, t_prev, dt)
         hx, hy, hp = O.step(h[0], h[1], h[2], h[3], dt, bc)
         gx, gy, stats = S.step(d[0], d[1], d[2], d[3], dt, S.boundary_data(t, t_prev, dt), p_out=p)
-        assert stats["converged"] == 1 and stats["final_relres"] <= 1e-13
+        assert stats["converged"] == 1 and stats["final_relres"] <= 1e-11
         assert relerr(vs.download(gx), hx) < 1e-9, k
         assert relerr(vs.download(gy), hy) < 1e-9, k
         assert relerr(vs.download(p), hp) < 1e-7, k
@@ -122,7 +122,9 @@ def test_stokes_outputs_may_alias_previous_state():
     a = S.step(vs.upload(ux), vs.upload(uy), vs.upload(ux), vs.upload(uy), 0.001, bc)
     up = [vs.upload(ux), vs.upload(uy)]
     b = S.step(up[0], up[1], vs.upload(ux), vs.upload(uy), 0.001, bc, out=(up[0], up[1]))
-    assert torch.equal(a[0], b[0]) and torch.equal(a[1], b[1])
+    # the pressure solve warm-starts from the previous step's p: equal to the solver tolerance
+    assert relerr(vs.download(a[0]), vs.download(b[0])) < 1e-9
+    assert relerr(vs.download(a[1]), vs.download(b[1])) < 1e-9
     u = vs.upload(ux)
     with pytest.raises(dg.DgcError):
         S.step(up[0], up[1], u, vs.upload(uy), 0.001, bc, out=(u, up[1]))
