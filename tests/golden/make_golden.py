@@ -17,8 +17,20 @@ they compute as compressed .npz files:
   ref_known_answers.json    mean-square nodal errors of the reference drivers'
                             runs on the reference's coarse mesh (10000 RK4
                             steps of advection, Maxwell to T = 1)
+  ref_stokes_jit4_N<N>.npz  two steps of the Stokes example's dual splitting
+                            from its exact initial data: everything the
+                            reference forms (pressure_bc's hp, right-hand
+                            sides, grad p, the projected u~), with the two
+                            linear systems (the reference's own assembled
+                            matrices) solved densely here in place of its
+                            cuSOLVER host LU, which needs a GPU.  The
+                            all-Neumann pressure matrix is singular and its
+                            right-hand side consistent only to ~1e-4; the
+                            reference leaves that to the LU's pivoting, here
+                            S = -J M A is solved with -J M rhs projected to zero
+                            sum and p taken with zero mean
 
-usage: python tests/golden/make_golden.py [/path/to/reference]
+usage: python tests/golden/make_golden.py [/path/to/reference] [--only stokes]
 """
 from __future__ import annotations
 
@@ -53,10 +65,72 @@ def read_dump(path: str) -> dict:
     return out
 
 
+def stokes_cases(oracle_dir: str, tmp: str) -> None:
+    """Two dual-splitting steps per order on a jittered 4 x 4 mesh (dt = 0.002)."""
+    exe = os.path.join(oracle_dir, "_ref", "ref_stokes")
+    mesh = meshes.jittered_square(4, seed=7)
+    mpath = os.path.join(tmp, "stokes_mesh.bin")
+    meshes.write_bin(mesh, mpath)
+    a, lam = 2.883356, 1.0 + 2.883356 ** 2   # stokes_2d.h:95-96
+
+    def probe(N, t_prev, t, dt, u, p=None):
+        spath, opath = os.path.join(tmp, "state.bin"), os.path.join(tmp, "stokes_out.bin")
+        with open(spath, "wb") as f:
+            f.write(struct.pack("<dddi", t_prev, t, dt, 0 if p is None else 1))
+            for v in list(u) + ([] if p is None else [p]):
+                f.write(np.ascontiguousarray(v, dtype="<f8").tobytes())
+        subprocess.run([exe, mpath, str(N), spath, opath], check=True)
+        return read_dump(opath)
+
+    for N in (2, 3):
+        Np = (N + 1) * (N + 2) // 2
+        n = mesh.cells.shape[0] * Np
+        d0 = probe(N, 0.0, 0.0, 1.0, [np.zeros(n)] * 4)
+        x, y = d0["x"], d0["y"]
+        ux = np.sin(x) * (a * np.sin(a * y) - np.cos(a) * np.sinh(y))   # exact_solution at t = 0
+        uy = np.cos(x) * (np.cos(a * y) + np.cos(a) * np.cosh(y))
+        JM = np.kron(np.diag(d0["J"]), d0["M"].reshape(Np, Np))
+        u = [ux, uy, ux.copy(), uy.copy()]
+        t_prev = t = 0.0
+        dt = 0.002
+        out = dict(mesh_xy=mesh.xy.reshape(-1), mesh_cells=mesh.cells.reshape(-1), x=x, y=y, bx=d0["bx"],
+                   by=d0["by"], dt=np.array([dt]))
+        for k in range(2):
+            da = probe(N, t_prev, t, dt, u)
+            assert np.array_equal(da["hp2"], 2.0 * da["hp"])
+            A = da["A_N"].reshape(n, n)
+            S = -JM @ A
+            b = -JM @ da["p_rhs"]
+            b -= b.mean()
+            p = np.linalg.lstsq(S, b, rcond=None)[0]
+            p -= p.mean()
+            db = probe(N, t_prev, t, dt, u, p)
+            H = db["H"].reshape(n, n)
+            vx = np.linalg.solve(H, db["v_rhs_x"])
+            vy = np.linalg.solve(H, db["v_rhs_y"])
+            rec = dict(t_prev=np.array([t_prev]), t=np.array([t]), u0x=u[0], u0y=u[1], u1x=u[2], u1y=u[3],
+                       ut_x=da["ut_x"], ut_y=da["ut_y"], hp2=da["hp2"], div_ut=da["div_ut"], p_rhs=da["p_rhs"],
+                       p=p, grad_p_x=db["grad_p_x"], grad_p_y=db["grad_p_y"], utp_x=db["utp_x"],
+                       utp_y=db["utp_y"], v_rhs_x=db["v_rhs_x"], v_rhs_y=db["v_rhs_y"], ux=vx, uy=vy)
+            out.update({f"s{k}_{key}": v for key, v in rec.items()})
+            u = [u[2], u[3], vx, vy]
+            t_prev, t = t, t + dt
+        np.savez_compressed(os.path.join(HERE, f"ref_stokes_jit4_N{N}.npz"), **out)
+
+
 def main() -> None:
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    only = sys.argv[sys.argv.index("--only") + 1] if "--only" in sys.argv else None
+    if only:
+        args = [a for a in args if a != only]
+    ref = args[0] if args else "/root/reference"
     oracle_dir = os.path.join(ROOT, "oracle")
     subprocess.run(["make", "-s", "-C", oracle_dir, "ref", f"REF={ref}"], check=True)
+    if only == "stokes":
+        with tempfile.TemporaryDirectory() as tmp:
+            stokes_cases(oracle_dir, tmp)
+        print(f"wrote the Stokes golden cases to {HERE}")
+        return
     dump = os.path.join(oracle_dir, "_ref", "ref_dump")
     timer = os.path.join(oracle_dir, "_ref", "ref_time")
     cases = []
@@ -114,6 +188,7 @@ def main() -> None:
                 rec.pop("gdof_per_s", None)
         with open(os.path.join(HERE, "ref_known_answers.json"), "w") as f:
             json.dump(known, f, indent=1, sort_keys=True)
+        stokes_cases(oracle_dir, tmp)
     print(f"wrote {len(cases)} golden cases + known answers to {HERE}")
 
 

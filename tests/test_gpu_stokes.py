@@ -144,3 +144,28 @@ def test_stokes_example_converges_with_consistent_data():
     assert errs[True] < 1e-5
     assert abs(errs[True] - oerr) < 1e-3 * oerr
     assert errs[False] > 1e-2
+
+
+@pytest.mark.parametrize("N", [2, 3])
+def test_stokes_step_matches_reference_golden(N):
+    """dgc_stokes_step from the reference's own step inputs (tests/golden/
+    ref_stokes_jit4_N*.npz: stokes_2d probed up to its solves, solved densely):
+    velocity at 1e-9, pressure at 1e-7, both steps."""
+    import os
+    from conftest import GOLDEN
+    d = np.load(os.path.join(GOLDEN, f"ref_stokes_jit4_N{N}.npz"))
+    m = meshes.Mesh(xy=d["mesh_xy"].reshape(-1, 2), cells=d["mesh_cells"].reshape(-1, 3))
+    S = st.Stokes(m, N, rtol=1e-11)
+    vs = S.velocity_space
+    b = vs.boundary_nodes()
+    assert np.array_equal(b[:, 0], d["bx"]) and np.array_equal(b[:, 1], d["by"])
+    dt = float(d["dt"][0])
+    p = S.empty()
+    for k in range(2):
+        g = {key[3:]: d[key] for key in d.files if key.startswith(f"s{k}_")}
+        u = [vs.upload(g[c]) for c in ("u0x", "u0y", "u1x", "u1y")]
+        ux, uy, stats = S.step(*u, dt, S.boundary_data(float(g["t"][0]), float(g["t_prev"][0]), dt), p_out=p)
+        assert stats["converged"] == 1
+        assert relerr(vs.download(ux), g["ux"]) < 1e-9, k
+        assert relerr(vs.download(uy), g["uy"]) < 1e-9, k
+        assert relerr(vs.download(p), g["p"]) < 1e-7, k

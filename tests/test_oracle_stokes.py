@@ -107,3 +107,65 @@ def test_step_error_decreases_with_order():
     m = meshes.jittered_square(4, 1)
     e = [so.StokesOracle(m.xy, m.cells, N, consistent=True).run(T=0.01, dt=0.001)[3] for N in (2, 3, 4)]
     assert e[0] > 10 * e[1] and e[1] > 2 * e[2]
+
+
+# ------------------------------------------------------------------ reference goldens
+# tests/golden/ref_stokes_jit4_N*.npz: the reference's stokes_2d probed up to its
+# linear solves (oracle/ref_harness/ref_stokes.cpp), solved densely (make_golden.py)
+import os  # noqa: E402
+
+from conftest import GOLDEN  # noqa: E402
+
+STOKES_CASES = [2, 3]
+
+
+def _golden(N):
+    d = np.load(os.path.join(GOLDEN, f"ref_stokes_jit4_N{N}.npz"))
+    s = so.StokesOracle(d["mesh_xy"].reshape(-1, 2), d["mesh_cells"].reshape(-1, 3), N)
+    return d, s
+
+
+def _rel(a, b):
+    return np.linalg.norm(np.ravel(a) - np.ravel(b)) / max(np.linalg.norm(np.ravel(b)), 1e-300)
+
+
+@pytest.mark.parametrize("N", STOKES_CASES)
+def test_stokes_pieces_match_reference(N):
+    """hp, the pressure right-hand side, grad p, the projected u~ and the viscous
+    right-hand sides of the oracle equal the reference's at 1e-12."""
+    d, s = _golden(N)
+    x, y = (a.reshape(-1) for a in s.o.node_xy())
+    assert _rel(x, d["x"]) < 1e-15 and _rel(y, d["y"]) < 1e-15
+    assert _rel(s.arr["bx"], d["bx"]) < 1e-15 and _rel(s.arr["by"], d["by"]) < 1e-15
+    dt = float(d["dt"][0])
+    for k in range(2):
+        g = {key[3:]: d[key] for key in d.files if key.startswith(f"s{k}_")}
+        t_prev, t = float(g["t_prev"][0]), float(g["t"][0])
+        bc = so.boundary_data(s.arr["bx"], s.arr["by"], t, t_prev, dt)
+        assert _rel((4 * g["u1x"] - g["u0x"]) / 3, g["ut_x"]) < 1e-15
+        hp = s.hp(g["u0x"], g["u0y"], g["u1x"], g["u1y"], bc["dgdt_x"], bc["dgdt_y"])
+        assert _rel(2 * hp, g["hp2"]) < 1e-12
+        w = s.o.div(g["ut_x"], g["ut_y"], bc["ut_x"], bc["ut_y"], -1.0) * (1.5 / dt)
+        assert _rel(w, g["div_ut"]) < 1e-12
+        w = s.o.laplace_bc_rhs(np.zeros(s.nb, np.uint8), None, g["hp2"], out=w)
+        assert _rel(w, g["p_rhs"]) < 1e-12
+        gx, gy = s.o.grad(g["p"], None, 1.0)
+        assert _rel(gx, g["grad_p_x"]) < 1e-12 and _rel(gy, g["grad_p_y"]) < 1e-12
+        assert _rel(g["ut_x"] - 2 * dt * gx / 3, g["utp_x"]) < 1e-12
+        for c, gd in (("x", bc["g_x"]), ("y", bc["g_y"])):
+            v = s.o.laplace_bc_rhs(np.ones(s.nb, np.uint8), gd, None, out=-1.5 * g[f"utp_{c}"] / dt)
+            assert _rel(v, g[f"v_rhs_{c}"]) < 1e-12
+
+
+@pytest.mark.parametrize("N", STOKES_CASES)
+def test_stokes_step_matches_reference(N):
+    """The whole restated step from the reference's inputs: velocity at 1e-10,
+    pressure (same null-space convention) at 1e-9."""
+    d, s = _golden(N)
+    dt = float(d["dt"][0])
+    for k in range(2):
+        g = {key[3:]: d[key] for key in d.files if key.startswith(f"s{k}_")}
+        bc = so.boundary_data(s.arr["bx"], s.arr["by"], float(g["t"][0]), float(g["t_prev"][0]), dt)
+        ux, uy, p = s.step(g["u0x"], g["u0y"], g["u1x"], g["u1y"], dt, bc)
+        assert _rel(ux, g["ux"]) < 1e-10 and _rel(uy, g["uy"]) < 1e-10, k
+        assert _rel(p, g["p"]) < 1e-9, k
