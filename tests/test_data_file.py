@@ -12,7 +12,7 @@ from conftest import GOLDEN
 
 import dgc_gb300 as dg
 
-CASES = sorted(p for p in glob.glob(os.path.join(GOLDEN, "ref_*_N*.npz")) if "adv1d" not in p)
+CASES = sorted(p for p in glob.glob(os.path.join(GOLDEN, "ref_*_N*.npz")) if "adv1d" not in p and "stokes" not in p)
 
 
 @pytest.fixture(scope="module", autouse=True)

@@ -13,7 +13,7 @@ from conftest import GOLDEN
 import dgc_gb300 as dg
 from dgc_gb300 import meshes
 
-CASES = sorted(p for p in glob.glob(os.path.join(GOLDEN, "ref_*_N*.npz")) if "adv1d" not in p)
+CASES = sorted(p for p in glob.glob(os.path.join(GOLDEN, "ref_*_N*.npz")) if "adv1d" not in p and "stokes" not in p)
 SOURCES = [p for p in CASES if "msh_source" in np.load(p).files]
 
 
