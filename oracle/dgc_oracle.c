@@ -334,18 +334,20 @@ int orc_face_vandermonde(int N, int face, double* fV) {
  *  strong form (src/laplace_2d.h:88-112):  Dr = Vr V^-1, Ds = Vs V^-1
  *  LIFT = Minv E with E the face mass matrices (Vf Vf^T)^-1 placed on face rows. */
 int orc_operators(int N, int form, double* Dr, double* Ds, double* L, double* Mout) {
+  if (N < 1 || N > ORC_MAX_ORDER) return -1;
   int Np = (N + 1) * (N + 2) / 2, Nfp = N + 1;
   size_t nn = (size_t)Np * Np;
-  double* V = malloc(sizeof(double) * nn);
-  double* Vr = malloc(sizeof(double) * nn);
-  double* Vs = malloc(sizeof(double) * nn);
-  double* VT = malloc(sizeof(double) * nn);
-  double* Minv = malloc(sizeof(double) * nn);
-  double* M = malloc(sizeof(double) * nn);
-  double* T1 = malloc(sizeof(double) * nn);
-  double* T2 = malloc(sizeof(double) * nn);
+  double* V = calloc(nn, sizeof(double));
+  double* Vr = calloc(nn, sizeof(double));
+  double* Vs = calloc(nn, sizeof(double));
+  double* VT = calloc(nn, sizeof(double));
+  double* Minv = calloc(nn, sizeof(double));
+  double* M = calloc(nn, sizeof(double));
+  double* T1 = calloc(nn, sizeof(double));
+  double* T2 = calloc(nn, sizeof(double));
   double* E = calloc((size_t)Np * 3 * Nfp, sizeof(double));
-  if (orc_vandermonde(N, V) || orc_grad_vandermonde(N, Vr, Vs)) return -1;
+  orc_vandermonde(N, V);
+  orc_grad_vandermonde(N, Vr, Vs);
   mat_transpose(Np, Np, V, VT);
   mat_mul(Np, Np, Np, V, VT, Minv);
   orc_mat_inverse(Np, Minv, M);
@@ -1122,7 +1124,8 @@ int orc_pcg(orc* o, int tau_mode, const double* b, double* x, double rtol, int m
   double* binv = malloc(8 * (size_t)K * Np * Np);
   orc_spd_diag_blocks(o, tau_mode, blk);
   for (int c = 0; c < K; ++c) orc_mat_inverse(Np, blk + (size_t)c * Np * Np, binv + (size_t)c * Np * Np);
-  double *r = malloc(8 * n), *z = malloc(8 * n), *p = malloc(8 * n), *Ap = malloc(8 * n);
+  /* zeroed: gemv reads y even with beta = 0 */
+  double *r = calloc(n, 8), *z = calloc(n, 8), *p = calloc(n, 8), *Ap = calloc(n, 8);
   orc_spd_apply(o, tau_mode, x, Ap);
   for (size_t i = 0; i < n; ++i) r[i] = b[i] - Ap[i];
   double bn = sqrt(dot(b, b, n));
