@@ -3,8 +3,8 @@
 
 #include <algorithm>
 #include <cstdarg>
-#include <cstdlib>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -190,7 +190,10 @@ extern "C" int dgc_create(int nv, const double* vxy, int K, const int32_t* cells
     delete h;
     return fail(DGC_ERR_ARG, "%s", err.c_str());
   }
-  if (!dgc::build_mesh(vxy, nv, cells, K, h->re, h->mesh, err)) {
+  // half-edge matching on the GPU from 16384 cells (DGC_GPU_TOPOLOGY_MIN overrides)
+  int64_t gpu_topo_min = 16384;
+  if (const char* e = std::getenv("DGC_GPU_TOPOLOGY_MIN")) gpu_topo_min = std::atoll(e);
+  if (!dgc::build_mesh(vxy, nv, cells, K, h->re, h->mesh, err, (int64_t)K >= gpu_topo_min)) {
     delete h;
     return fail(DGC_ERR_MESH, "%s", err.c_str());
   }
@@ -654,6 +657,13 @@ extern "C" int dgc_ref_operator(int order, int which, double* out) {
     default: return fail(DGC_ERR_ARG, "unknown operator %d", which);
   }
   std::memcpy(out, src->data(), src->size() * sizeof(double));
+  return DGC_OK;
+}
+
+extern "C" int dgc_mesh_neighbors(dgc_handle h, int32_t* nbr, int* num_bfaces) {
+  if (!h) return fail(DGC_ERR_ARG, "null handle");
+  if (nbr) std::memcpy(nbr, h->mesh.nbr.data(), h->mesh.nbr.size() * sizeof(int32_t));
+  if (num_bfaces) *num_bfaces = h->mesh.num_bfaces;
   return DGC_OK;
 }
 

@@ -272,7 +272,7 @@ bool build_ref_element(int N, RefElement& re, std::string& err) {
 
 // ---------------------------------------------------------------- mesh
 bool build_mesh(const double* vxy, int nv, const int32_t* cells, int K, const RefElement& re,
-                MeshData& m, std::string& err) {
+                MeshData& m, std::string& err, bool gpu_topology) {
   char buf[256];
   if (K <= 0 || nv < 3 || !vxy || !cells) {
     err = "empty mesh";
@@ -341,24 +341,35 @@ bool build_mesh(const double* vxy, int nv, const int32_t* cells, int K, const Re
     }
   }
 
-  // topology: sort half-edges by their unordered vertex pair; equal keys are twins
-  struct HE { uint64_t key; int32_t k, f; };
-  std::vector<HE> he((size_t)3 * K);
   for (int k = 0; k < K; ++k)
-    for (int f = 0; f < 3; ++f) {
-      uint32_t a = (uint32_t)cells[3 * k + f], b = (uint32_t)cells[3 * k + (f + 1) % 3];
-      if (a == b) {
+    for (int f = 0; f < 3; ++f)
+      if (cells[3 * k + f] == cells[3 * k + (f + 1) % 3]) {
         std::snprintf(buf, sizeof buf, "cell %d has a repeated vertex", k);
         err = buf;
         return false;
       }
-      he[(size_t)3 * k + f] = HE{(uint64_t)std::min(a, b) << 32 | std::max(a, b), k, f};
-    }
+  m.nbr.assign((size_t)4 * K, 0);
+  std::vector<int8_t> is_bnd((size_t)3 * K, 1);
+  if (gpu_topology) {
+    std::vector<int32_t> twin;
+    if (!gpu_match_half_edges(cells, K, twin, err)) return false;
+    for (size_t h = 0; h < twin.size(); ++h)
+      if (twin[h] >= 0) {
+        m.nbr[4 * (h / 3) + h % 3] = twin[h];
+        is_bnd[h] = 0;
+      }
+  }
+  // topology: sort half-edges by their unordered vertex pair; equal keys are twins
+  struct HE { uint64_t key; int32_t k, f; };
+  std::vector<HE> he(gpu_topology ? 0 : (size_t)3 * K);
+  for (size_t i = 0; i < he.size(); ++i) {
+    const int k = (int)(i / 3), f = (int)(i % 3);
+    const uint32_t a = (uint32_t)cells[3 * k + f], b = (uint32_t)cells[3 * k + (f + 1) % 3];
+    he[i] = HE{(uint64_t)std::min(a, b) << 32 | std::max(a, b), k, f};
+  }
   std::sort(he.begin(), he.end(), [](const HE& x, const HE& y) {
     return x.key != y.key ? x.key < y.key : (x.k != y.k ? x.k < y.k : x.f < y.f);
   });
-  m.nbr.assign((size_t)4 * K, 0);
-  std::vector<int8_t> is_bnd((size_t)3 * K, 1);
   for (size_t i = 0; i < he.size();) {
     size_t j = i + 1;
     while (j < he.size() && he[j].key == he[i].key) ++j;

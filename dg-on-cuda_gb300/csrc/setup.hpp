@@ -102,7 +102,13 @@ struct MeshData {
   double min_altitude = 0.0;       // smallest triangle altitude
 };
 
+// gpu_topology: match the half-edges on the current GPU (gpu_match_half_edges)
+// instead of sorting them on the host; the results are identical.
 bool build_mesh(const double* vxy, int nv, const int32_t* cells, int K, const RefElement& re,
-                MeshData& out, std::string& err);
+                MeshData& out, std::string& err, bool gpu_topology = false);
+
+// twin[3 k + f] = (k' << 2 | f') of the twin half-edge, or -1 on the boundary
+// (csrc/topology.cu)
+bool gpu_match_half_edges(const int32_t* cells, int K, std::vector<int32_t>& twin, std::string& err);
 
 }  // namespace dgc

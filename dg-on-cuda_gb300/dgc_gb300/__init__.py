@@ -138,6 +138,7 @@ def lib():
             L.dgc_ref_nodes.argtypes = [C.c_int, _dp, _dp]
             L.dgc_ref_operator.argtypes = [C.c_int, C.c_int, _dp]
             L.dgc_host_mesh.argtypes = [C.c_int, _dp, C.c_int, _ip, C.c_int, _dp, _ip, C.POINTER(C.c_int)]
+            L.dgc_mesh_neighbors.argtypes = [_vp, _ip, C.POINTER(C.c_int)]
             L.dgc_batch_create.argtypes = [C.POINTER(_vp), C.c_int, C.POINTER(_vp)]
             L.dgc_batch_destroy.argtypes = [_vp]
             L.dgc_batch_lserk4_step.argtypes = [_vp, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp), _dp, _dp, _vp]
@@ -288,6 +289,14 @@ class Discretization:
         y = np.zeros(self.K * self.Np)
         _check(lib().dgc_node_coordinates(self._h, x, y))
         return x.reshape(self.K, self.Np), y.reshape(self.K, self.Np)
+
+    def neighbors(self):
+        """The twin map [K][4] ((k << 2 | f) of the twin face, -(1 + b) for boundary face b)
+        and the number of boundary faces."""
+        out = np.zeros(4 * self.K, np.int32)
+        nb = C.c_int()
+        _check(lib().dgc_mesh_neighbors(self._h, out, C.byref(nb)))
+        return out.reshape(self.K, 4), nb.value
 
     def operator(self, which: int) -> np.ndarray:
         shape = {OP_LIFT: (self.Np, 3 * self.Nfp)}.get(which, (self.Np, self.Np))

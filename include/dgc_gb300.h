@@ -100,7 +100,11 @@ typedef struct dgc_info {
  * examples/advection_2d/k_advection_2d.cu:45-100): builds the mesh topology,
  * geometry and operator matrices from vertex coordinates (x, y interleaved, as
  * simple_triangular_mesh_2d::fill_vertices takes them) and counter-clockwise
- * triangles (fill_connectivity), and uploads them to the current device. */
+ * triangles (fill_connectivity), and uploads them to the current device.
+ * The twin map (simple_triangular_mesh_2d::build_topology) is matched on the
+ * GPU from 16384 cells (a hash of the edges' vertex pairs; the environment
+ * variable DGC_GPU_TOPOLOGY_MIN sets the threshold) and by a host sort below;
+ * both give the same result. */
 int dgc_create(int num_vertices, const double* vertex_xy, int num_cells, const int32_t* cells,
                const dgc_problem_desc* desc, dgc_handle* out);
 
@@ -519,6 +523,9 @@ int dgc_ref_operator(int order, int which, double* out);
  * src/simple_discretization_2d.h:136-162).  Any output may be NULL. */
 int dgc_host_mesh(int num_vertices, const double* vertex_xy, int num_cells, const int32_t* cells, int order,
                   double* geom, int32_t* nbr, int* num_boundary_faces);
+
+/* The handle's twin map, host array [K][4] in the dgc_host_mesh encoding. */
+int dgc_mesh_neighbors(dgc_handle h, int32_t* nbr, int* num_boundary_faces);
 
 #ifdef __cplusplus
 }
