@@ -250,6 +250,7 @@ LEARN_NSIDE, LEARN_ORDER, LEARN_SEED = 128, 4, 5151
 LEARN_TRAIN, LEARN_HELD = 1600, 400            # the full sequence: 2000 solves
 LEARN_TRAIN_SAMPLE, LEARN_HELD_SAMPLE = 16, 8  # the bounded sample timed here
 LEARN_SNAPSHOTS = (4, 16, 64, 256, 1024)       # PCG iterates giving residual / error pairs
+LEARN_AGGREGATE = 8                             # cells per aggregate of the coarse space
 
 
 def smooth_rhs(x, y, index: int, modes: int = 24):
@@ -267,13 +268,15 @@ def smooth_rhs(x, y, index: int, modes: int = 24):
 
 def measure_learned(dg, meshes):
     """Learned preconditioner on IPDG Poisson (Dirichlet, jittered 128x128 mesh,
-    K = 32768, N = 4): residual / error pairs from plain block-Jacobi PCG iterates
-    of the first training solves train the 4-layer width-64 message-passing network
-    (BF16 weights, FP32 accumulation, energy-norm loss, Adam); on held-out solves
-    the learned solve (truncated flexible CG with the network, block-Jacobi PCG as
+    K = 32768, N = 4), in two-level form: M r = Binv r + P A_c^-1 P^T r + network,
+    the coarse space a smoothed aggregation of LEARN_AGGREGATE cells.  Residual /
+    error pairs from plain block-Jacobi PCG iterates of the first training solves
+    train the 4-layer width-64 message-passing network (BF16 weights, FP32
+    accumulation, energy-norm loss, Adam) on what the two-level base leaves; on
+    held-out solves the learned solve (truncated flexible CG, block-Jacobi PCG as
     fallback and judge once its break-even budget is spent) is timed against plain
-    FP64 block-Jacobi PCG and the mixed FP32/FP64 refinement, all to 1e-10 relative
-    FP64 residual.  A bounded sample of the 2000-solve sequence (1600 train / 400
+    FP64 block-Jacobi PCG, the mixed FP32/FP64 refinement and the same two-level
+    flexible CG without the network, all to 1e-10 relative FP64 residual.  A bounded sample of the 2000-solve sequence (1600 train / 400
     held out): the first LEARN_TRAIN_SAMPLE training and LEARN_HELD_SAMPLE held-out
     right-hand sides."""
     import torch
@@ -283,7 +286,16 @@ def measure_learned(dg, meshes):
     D.block_jacobi()
     c = float(np.sqrt(D.K * D.Np))
     net = dg.MPNN(D, layers=4, seed=LEARN_SEED)
-    bj = dg.MPNN(D, layers=1, seed=0)               # zero output layer: M(r) = Binv r
+    bj = dg.MPNN(D, layers=1, seed=0)               # zero output layer: M(r) = Binv r + coarse
+    # two-level form: the coarse space (smoothed aggregation) removes the smooth
+    # mesh-wide error that a 4-hop network cannot see; the network learns the rest
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    bj.set_coarse(LEARN_AGGREGATE)
+    torch.cuda.synchronize()
+    coarse_s = time.perf_counter() - t0
+    net.set_coarse(LEARN_AGGREGATE)
+    _, n_agg, n_col, omega = D.coarse_info()
 
     def rhs(i):
         return D.mass(D.upload(smooth_rhs(x, y, i).reshape(-1)))
@@ -295,7 +307,8 @@ def measure_learned(dg, meshes):
         torch.cuda.synchronize()
         return r, time.perf_counter() - t0
 
-    # training pairs: x = r c/|r|, t = (e - Binv r) c/|r| at PCG iterates x_k, e = x* - x_k
+    # training pairs: x = r c/|r|, t = (e - M_0 r) c/|r| at PCG iterates x_k, e = x* - x_k,
+    # M_0 = Binv + the coarse correction
     t0 = time.perf_counter()
     X, T, pcg_its = [], [], []
     for i in range(LEARN_TRAIN_SAMPLE):
@@ -313,18 +326,29 @@ def measure_learned(dg, meshes):
     sigma = float(torch.sqrt(torch.mean(torch.stack([torch.mean(t.double() ** 2) for t in T]))))
     T = [t / sigma for t in T]
     rng = np.random.default_rng(LEARN_SEED)
-    losses, batch, epochs = [], 8, 30
+    losses, batch, epochs, lr = [], 8, 30, 1e-4
     t0 = time.perf_counter()
     for ep in range(epochs):
         order = rng.permutation(len(X))
         el = [net.train_step(torch.cat([X[j] for j in order[i:i + batch]]),
-                             torch.cat([T[j] for j in order[i:i + batch]]), lr=3e-4)[0]
+                             torch.cat([T[j] for j in order[i:i + batch]]), lr=lr)[0]
               for i in range(0, len(X), batch)]
         losses.append(float(np.mean(el)))
+    # step length of the network's correction: theta minimises sum_j |t_j - theta y_j|_S^2
+    # over the training pairs (energy norm), so an output uncorrelated with the targets
+    # is scaled towards zero instead of disturbing the flexible CG
+    num = den = 0.0
+    for xj, tj in zip(X, T):
+        yj = net.forward(xj).double()
+        syj = D.spd(yj)
+        num += float(torch.dot(tj.double(), syj))
+        den += float(torch.dot(yj, syj))
+    theta = num / den if den > 0.0 else 0.0
     torch.cuda.synchronize()
     train_s = time.perf_counter() - t0
     w = net.get_weights()
-    w[-(D.NpP * 64 + D.NpP):] *= sigma               # targets were trained in units of sigma
+    # targets were trained in units of sigma; the output layer also takes theta
+    w[-(D.NpP * 64 + D.NpP):] *= sigma * theta
     net.set_weights(w)
 
     # per-iteration costs and the flexible-CG budget beyond which it cannot beat plain PCG
@@ -335,17 +359,20 @@ def measure_learned(dg, meshes):
     budget = int(np.median(pcg_its) * it_p / it_f)
     _, t_fwd = sync_time(lambda: [net.forward(X[0]) for _ in range(20)])
 
-    held = {"fp64_pcg": [], "mixed_ir": [], "learned": []}
-    fell = 0
+    held = {"fp64_pcg": [], "mixed_ir": [], "two_level_no_network": [], "learned": []}
+    fell = fell0 = 0
     agree = []
     for i in range(LEARN_HELD_SAMPLE):
         b = rhs(LEARN_TRAIN + i)
         (xp, sp), tp = sync_time(lambda: D.pcg(b, rtol=1e-10))
         (_, sm), tm = sync_time(lambda: D.pcg(b, mode=dg.SOLVE_MIXED_IR, rtol=1e-10))
+        (_, s0), t0_ = sync_time(lambda: bj.solve(b, rtol=1e-10, fcg_maxit=budget))
         (xl, sl), tl = sync_time(lambda: net.solve(b, rtol=1e-10, fcg_maxit=budget))
         fell += int(sl["fell_back"])
+        fell0 += int(s0["fell_back"])
         held["fp64_pcg"].append((sp["iterations"], tp, sp["final_relres"]))
         held["mixed_ir"].append((sm["iterations"], tm, sm["final_relres"]))
+        held["two_level_no_network"].append((s0["iterations"], t0_, s0["final_relres"]))
         held["learned"].append((sl["iterations"], tl, sl["final_relres"], sl["inner_iterations"]))
         agree.append(float(torch.linalg.norm(xl - xp) / torch.linalg.norm(xp)))
     D.check()
@@ -365,15 +392,25 @@ def measure_learned(dg, meshes):
                       "pairs": len(X), "snapshots": list(LEARN_SNAPSHOTS)},
            "network": {"layers": 4, "width": 64, "params": net.num_params, "weights": "bf16 (fp32 masters)",
                        "accumulate": "fp32", "loss": "energy norm |y - t|_S^2 / |t|_S^2",
-                       "optimizer": f"Adam lr 3e-4, batch {batch}, {epochs} epochs",
+                       "optimizer": f"Adam lr {lr:g}, batch {batch}, {epochs} epochs",
+                       "theta": theta,
                        "forward_ms": t_fwd / 20 * 1e3},
+           "coarse": {"cells_per_aggregate": LEARN_AGGREGATE, "aggregates": n_agg, "colours": n_col,
+                      "omega": omega, "build_s": coarse_s,
+                      "form": "M r = Binv r + P A_c^-1 P^T r + net, P = (I - omega Binv S) P0 (smoothed "
+                              "aggregation), A_c = P^T S P inverted once; smoothing applies in FP32"},
            "datagen_s": datagen_s, "train_s": train_s, "loss_per_epoch": losses,
            "pcg_iteration_ms": it_p * 1e3, "fcg_iteration_ms": it_f * 1e3, "fcg_budget": budget,
            "held_out": {k: summary(v) for k, v in held.items()},
-           "fallback_count": fell,
+           "fallback_count": fell, "fallback_count_two_level_no_network": fell0,
            "max_rel_l2_learned_vs_fp64_pcg": float(max(agree))}
-    out["speedup_learned_vs_fp64_pcg"] = out["held_out"]["fp64_pcg"]["wall_s_total"] / \
-        out["held_out"]["learned"]["wall_s_total"]
+    ho = out["held_out"]
+    out["speedup_learned_vs_fp64_pcg"] = ho["fp64_pcg"]["wall_s_total"] / ho["learned"]["wall_s_total"]
+    out["speedup_learned_vs_mixed_ir"] = ho["mixed_ir"]["wall_s_total"] / ho["learned"]["wall_s_total"]
+    # what the trained network adds to the same two-level method without it
+    out["network_gain"] = {
+        "iterations": ho["two_level_no_network"]["iterations_median"] / ho["learned"]["iterations_median"],
+        "wall_time": ho["two_level_no_network"]["wall_s_total"] / ho["learned"]["wall_s_total"]}
     return out
 
 

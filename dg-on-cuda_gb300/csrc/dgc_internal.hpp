@@ -11,6 +11,7 @@
 
 namespace dgc {
 struct IpdgState;
+struct CoarseSpace;
 }
 
 // the handle behind the opaque C type
@@ -43,6 +44,7 @@ struct dgc_handle_s {
   double graph_dt = 0.0;
   int graph_steps = 0;
   dgc::IpdgState* ipdg = nullptr;
+  dgc::CoarseSpace* coarse = nullptr;  // two-level preconditioner (dgc_coarse_build)
 };
 
 namespace dgc {
@@ -57,6 +59,14 @@ void ipdg_operators_changed(dgc_handle_s* h);
 // block-Jacobi inverse of the SPD laplace form (built once), and z = Binv r (FP64)
 int ipdg_build_preconditioner(dgc_handle_s* h, cudaStream_t s);
 int ipdg_block_jacobi_apply(dgc_handle_s* h, const double* r, double* z, cudaStream_t s);
+// the SPD form's shift, and whether the boundary types are the handle's uniform ones
+double ipdg_shift(const dgc_handle_s* h);
+bool ipdg_uniform_bc(const dgc_handle_s* h);
+// coarse space (csrc/coarse.cu): z (+)= P A_c^-1 P^T r (binv_r = Binv r when the
+// caller has it, else NULL; fp32: the two smoothing applies of S in FP32); freeing
+int coarse_apply(dgc_handle_s* h, const double* r, const double* binv_r, double* z, bool add, bool fp32,
+                 cudaStream_t s);
+void coarse_free(CoarseSpace* c);
 // device list of the cells with a boundary face (laplace handles)
 int ipdg_boundary_cells(const dgc_handle_s* h, const int** cells, int* n);
 // out = S u with the FP32 kernels (any laplace handle; one field, native layout)

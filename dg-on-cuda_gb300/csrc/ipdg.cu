@@ -519,6 +519,8 @@ int ipdg_init(dgc_handle_s* h) {
 }
 
 void ipdg_free(dgc_handle_s* h) {
+  coarse_free(h->coarse);
+  h->coarse = nullptr;
   IpdgState* st = h->ipdg;
   if (!st) return;
   for (int i = 0; i < 2; ++i)
@@ -547,6 +549,10 @@ void ipdg_free(dgc_handle_s* h) {
   delete st;
   h->ipdg = nullptr;
 }
+
+double ipdg_shift(const dgc_handle_s* h) { return h->ipdg ? h->ipdg->shift : 0.0; }
+
+bool ipdg_uniform_bc(const dgc_handle_s* h) { return !h->ipdg || !h->ipdg->bcdir; }
 
 int ipdg_boundary_cells(const dgc_handle_s* h, const int** cells, int* n) {
   if (!h->ipdg) return set_error(DGC_ERR_UNSUPPORTED, "not a laplace handle");

@@ -532,6 +532,7 @@ struct dgc_mpnn_s {
   float *y = nullptr, *dy = nullptr, *dh0 = nullptr, *dh1 = nullptr, *g = nullptr, *m = nullptr;
   float *sd = nullptr, *tm = nullptr, *st = nullptr;  // energy loss: S d, masked t, S t
   int loss_kind = DGC_MPNN_LOSS_ENERGY;
+  bool coarse = false;           // add the handle's coarse-space correction to Binv r
   double* scal = nullptr;        // training: [0] loss, [1..] per-sample target norms; solver: dot products
   double* h_scal = nullptr;      // pinned
   int scal_cap = 0;
@@ -681,6 +682,8 @@ int precondition(dgc_mpnn m, const double* r, double* z, cudaStream_t s, double 
     nr = std::sqrt(rr);
   }
   if (int rc = dgc::ipdg_block_jacobi_apply(h, r, m->bj, s)) return rc;
+  if (m->coarse)
+    if (int rc = dgc::coarse_apply(h, r, m->bj, m->bj, true, true, s)) return rc;
   if (nr == 0.0) {
     CKM(cudaMemsetAsync(z, 0, n * sizeof(double), s));
     return DGC_OK;
@@ -787,6 +790,17 @@ extern "C" int dgc_mpnn_set_loss(dgc_mpnn m, int kind) {
   if (!m) return merr(DGC_ERR_ARG, "null argument");
   if (kind != DGC_MPNN_LOSS_L2 && kind != DGC_MPNN_LOSS_ENERGY) return merr(DGC_ERR_ARG, "unknown loss kind");
   m->loss_kind = kind;
+  return DGC_OK;
+}
+
+extern "C" int dgc_mpnn_set_coarse(dgc_mpnn m, int cells_per_aggregate, void* stream) {
+  if (!m) return merr(DGC_ERR_ARG, "null network");
+  if (cells_per_aggregate <= 0) {
+    m->coarse = false;
+    return DGC_OK;
+  }
+  if (int rc = dgc_coarse_build(m->h, cells_per_aggregate, stream)) return rc;
+  m->coarse = true;
   return DGC_OK;
 }
 

@@ -155,6 +155,11 @@ def lib():
             L.dgc_mpnn_train_step.argtypes = [_vp, _vp, _vp, C.c_int, C.c_float, C.POINTER(C.c_float), _vp, _vp]
             L.dgc_mpnn_forward.argtypes = [_vp, _vp, _vp, _vp]
             L.dgc_mpnn_set_loss.argtypes = [_vp, C.c_int]
+            L.dgc_mpnn_set_coarse.argtypes = [_vp, C.c_int, _vp]
+            L.dgc_coarse_build.argtypes = [_vp, C.c_int, _vp]
+            L.dgc_coarse_apply.argtypes = [_vp, _vp, _vp, C.c_int, _vp]
+            L.dgc_coarse_info.argtypes = [_vp, C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                          C.POINTER(C.c_double)]
             L.dgc_mpnn_precondition.argtypes = [_vp, _vp, _vp, _vp]
             L.dgc_fpcg_solve.argtypes = [_vp, _vp, _vp, _vp, C.POINTER(SolveOpts), C.POINTER(SolveStats), _vp]
             L.dgc_learned_solve.argtypes = [_vp, _vp, _vp, _vp, C.POINTER(SolveOpts), C.c_int,
@@ -488,6 +493,23 @@ class Discretization:
         _check(lib().dgc_block_jacobi(self._h, _ptr(out), _stream(stream)))
         return out.view(self.K, self.Np, self.Np)
 
+    def coarse_build(self, cells_per_aggregate: int, stream=None) -> None:
+        _check(lib().dgc_coarse_build(self._h, cells_per_aggregate, _stream(stream)))
+
+    def coarse_apply(self, r, out=None, precision: int = F64, stream=None):
+        """out = P A_c^-1 P^T r (FP64 device vectors; precision of the smoothing applies)."""
+        import torch
+        out = torch.zeros(self.state_len, dtype=torch.float64, device="cuda") if out is None else out
+        _check(lib().dgc_coarse_apply(self._h, _ptr(r), _ptr(out), precision, _stream(stream)))
+        return out
+
+    def coarse_info(self):
+        """(aggregate of each cell, number of aggregates, number of colours, omega)."""
+        agg = np.zeros(self.K, np.int32)
+        na, nc, om = C.c_int(), C.c_int(), C.c_double()
+        _check(lib().dgc_coarse_info(self._h, agg.ctypes.data, C.byref(na), C.byref(nc), C.byref(om)))
+        return agg, na.value, nc.value, om.value
+
     def pcg(self, b, x=None, mode: int = SOLVE_FP64_PCG, rtol: float = 1e-10, maxit: int = 20000,
             inner_rtol: float = 1e-4, max_outer: int = 20, graph: bool = True, stream=None, check: bool = True):
         """Solve S x = b (FP64 device vectors, native layout).  Returns (x, stats dict)."""
@@ -639,6 +661,10 @@ class MPNN:
     @property
     def num_params(self) -> int:
         return int(lib().dgc_mpnn_num_params(self._h))
+
+    def set_coarse(self, cells_per_aggregate: int, stream=None):
+        """Two-level form: M(r) = Binv r + P A_c^-1 P^T r + network (0 = off)."""
+        _check(lib().dgc_mpnn_set_coarse(self._h, cells_per_aggregate, _stream(stream)))
 
     def set_loss(self, kind: int):
         """MPNN_LOSS_ENERGY (default: |d|_S^2 / |t|_S^2) or MPNN_LOSS_L2 (|d|^2 / |t|^2)."""

@@ -360,6 +360,32 @@ int dgc_mpnn_train_step(dgc_mpnn m, const float* x, const float* t, int samples,
 int dgc_mpnn_forward(dgc_mpnn m, const float* x, float* y, void* stream);
 /* z = M(r) (device FP64, native layout). */
 int dgc_mpnn_precondition(dgc_mpnn m, const double* r, double* z, void* stream);
+
+/* Two-level form of the learned preconditioner: with cells_per_aggregate > 0,
+ * M(r) = Binv r + P A_c^-1 P^T r + (|r|/c) net(c r/|r|), the coarse space of
+ * dgc_coarse_build on the network's handle (built here when missing; shared
+ * by every network of the handle; its smoothing applies of S in FP32).  The network then learns the correction
+ * that is left after both.  0 turns the coarse term off (the default). */
+int dgc_mpnn_set_coarse(dgc_mpnn m, int cells_per_aggregate, void* stream);
+
+/* ---- coarse space (two-level preconditioning of the SPD laplace form) ------
+ * No counterpart in the reference.  Cells are grouped into aggregates of
+ * about cells_per_aggregate face-connected cells (breadth-first, in cell
+ * order; at most 8192 aggregates); P0 is constant on each aggregate, the
+ * prolongation P = (I - omega Binv S) P0 is smoothed once with block Jacobi
+ * (omega = 4 / (3 lambda_max(Binv S)), lambda_max from 20 power iterations
+ * times 1.1), and A_c = P^T S P is the Galerkin coarse matrix of the SPD form
+ * S (FP64 Dirichlet handles with uniform boundary types; the shift at build
+ * time), inverted once on the GPU.  Rebuilding with the same size and shift
+ * is a no-op. */
+int dgc_coarse_build(dgc_handle h, int cells_per_aggregate, void* stream);
+/* z = P A_c^-1 P^T r (device FP64, native layout; z distinct from r).
+ * precision DGC_F32 runs the two applies of S inside P and P^T through the
+ * FP32 kernels (what the learned preconditioner uses); DGC_F64 is exact. */
+int dgc_coarse_apply(dgc_handle h, const double* r, double* z, int precision, void* stream);
+/* The aggregate of each cell (host array of K), their count, the number of
+ * colours used to assemble A_c and omega (any output may be NULL). */
+int dgc_coarse_info(dgc_handle h, int32_t* agg, int* num_aggregates, int* num_colors, double* omega);
 /* Truncated flexible CG (Notay's FCG(m)) on S x = b with M as the
  * preconditioner, to rtol on the true FP64 residual: each direction is
  * S-orthogonalised against the previous m, alpha = p.r / p.S p, and an
