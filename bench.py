@@ -274,7 +274,7 @@ def measure_learned(dg, meshes):
     train the 4-layer width-64 message-passing network (BF16 weights, FP32
     accumulation, energy-norm loss, Adam) on what the two-level base leaves; on
     held-out solves the learned solve (truncated flexible CG, block-Jacobi PCG as
-    fallback and judge once its break-even budget is spent) is timed against plain
+    fallback once its break-even budget is spent) is timed against plain
     FP64 block-Jacobi PCG, the mixed FP32/FP64 refinement and the same two-level
     flexible CG without the network, all to 1e-10 relative FP64 residual.  A bounded sample of the 2000-solve sequence (1600 train / 400
     held out): the first LEARN_TRAIN_SAMPLE training and LEARN_HELD_SAMPLE held-out

@@ -1004,7 +1004,7 @@ extern "C" int dgc_learned_solve(dgc_handle h, dgc_mpnn m, const double* b, doub
     if (stats) *stats = fs;
     return DGC_OK;
   }
-  // fallback and judge: block-Jacobi PCG from the current iterate
+  // fallback: block-Jacobi PCG from the current iterate, to the same true residual
   *fell_back = 1;
   dgc_solve_opts po = *opts;
   po.maxit = std::max(1, opts->maxit - fs.iterations);

@@ -718,7 +718,7 @@ class MPNN:
 
     def solve(self, b, x=None, rtol: float = 1e-10, maxit: int = 100000, fcg_maxit: int = 1000,
               mode: int = SOLVE_FP64_PCG, window: int = 4, stream=None, check: bool = True):
-        """Learned solve with block-Jacobi PCG (mode) as fallback and judge: flexible CG with
+        """Learned solve with block-Jacobi PCG (mode) as fallback and final check: flexible CG with
         this network for at most fcg_maxit iterations, then PCG from the current iterate.
         Returns (x, stats dict with "fell_back")."""
         import torch

@@ -395,7 +395,7 @@ int dgc_coarse_info(dgc_handle h, int32_t* agg, int* num_aggregates, int* num_co
 int dgc_fpcg_solve(dgc_handle h, dgc_mpnn m, const double* b, double* x, const dgc_solve_opts* opts,
                    dgc_solve_stats* stats, void* stream);
 
-/* Learned solve with block-Jacobi PCG as fallback and judge: dgc_fpcg_solve
+/* Learned solve with block-Jacobi PCG as fallback and final check: dgc_fpcg_solve
  * for at most fcg_maxit iterations; if that has not reached opts->rtol,
  * dgc_pcg_solve (opts->mode: FP64 PCG or mixed refinement) continues from the
  * current iterate with the remaining budget.  Either way the result meets
