@@ -53,14 +53,19 @@ struct CoarseSpace {
   double* d_xc = nullptr;             // A_c^-1 P^T r
   double* d_w[3] = {};                // work vectors (K x NpP)
   float* d_f[2] = {};                 // FP32 work vectors of the FP32 smoothing applies
+  double* d_pcg[3] = {};              // two-level PCG: z, p, q = S p (allocated on first use)
+  double* d_dots = nullptr;           // [4] dot products
+  double* h_dots = nullptr;           // pinned mirror
 };
 
 void coarse_free(CoarseSpace* c) {
   if (!c) return;
   for (void* p : {(void*)c->d_ptr, (void*)c->d_cells, (void*)c->d_agg, (void*)c->d_ainv, (void*)c->d_rc,
                   (void*)c->d_xc, (void*)c->d_w[0], (void*)c->d_w[1], (void*)c->d_w[2], (void*)c->d_f[0],
-                  (void*)c->d_f[1]})
+                  (void*)c->d_f[1], (void*)c->d_pcg[0], (void*)c->d_pcg[1], (void*)c->d_pcg[2],
+                  (void*)c->d_dots})
     cudaFree(p);
+  cudaFreeHost(c->h_dots);
   delete c;
 }
 
@@ -94,6 +99,63 @@ __global__ void k_coarse_to_f32(int64_t n, const double* __restrict__ x, float* 
 __global__ void k_coarse_to_f64(int64_t n, const float* __restrict__ x, double* __restrict__ y) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     y[i] = (double)x[i];
+}
+
+// out[j] += a_j . b_j, j < 3 (FP64; unused pairs have a null a)
+struct Dot3 {
+  const double* a[3];
+  const double* b[3];
+};
+__global__ void k_coarse_dots(int64_t n, Dot3 d, double* __restrict__ out) {
+  double s[3] = {0.0, 0.0, 0.0};
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      if (d.a[j]) s[j] += d.a[j][i] * d.b[j][i];
+  __shared__ double red[3][8];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    double v = s[j];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) red[j][w] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 3 && d.a[threadIdx.x]) {
+    double v = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) v += red[threadIdx.x][q];
+    atomicAdd(&out[threadIdx.x], v);
+  }
+}
+// out += sum of z over the valid nodes; z -= *out / count on the valid nodes
+__global__ void k_coarse_valid_sum(int64_t n, int npp, int np, const double* __restrict__ z, double* out) {
+  double v = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    if ((int)(i % npp) < np) v += z[i];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(out, v);
+}
+__global__ void k_coarse_sub_mean(int64_t n, int npp, int np, const double* __restrict__ sum, double count,
+                                  double* __restrict__ z) {
+  const double m = *sum / count;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    if ((int)(i % npp) < np) z[i] -= m;
+}
+
+// x += alpha p, r -= alpha q
+__global__ void k_coarse_step(int64_t n, double alpha, const double* __restrict__ p, const double* __restrict__ q,
+                              double* __restrict__ x, double* __restrict__ r) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    x[i] += alpha * p[i];
+    r[i] -= alpha * q[i];
+  }
+}
+// p = z + beta p
+__global__ void k_coarse_dir(int64_t n, const double* __restrict__ z, double beta, double* __restrict__ p) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = z[i] + beta * p[i];
 }
 
 // in-place Gauss-Jordan step i of an SPD matrix: col[r] = A[r][i]
@@ -261,7 +323,6 @@ extern "C" int dgc_coarse_build(dgc_handle h, int cells_per_aggregate, void* str
   if (!h) return set_error(DGC_ERR_ARG, "null handle");
   if (h->desc.physics != DGC_LAPLACE || h->prec != DGC_F64)
     return set_error(DGC_ERR_UNSUPPORTED, "the coarse space needs an FP64 laplace handle");
-  if (!h->desc.dirichlet) return set_error(DGC_ERR_UNSUPPORTED, "the coarse space needs Dirichlet boundaries");
   if (cells_per_aggregate < 1) return set_error(DGC_ERR_ARG, "cells_per_aggregate must be >= 1");
   if (!ipdg_uniform_bc(h)) return set_error(DGC_ERR_UNSUPPORTED, "the coarse space needs uniform boundary types");
   if (h->coarse && h->coarse->cells_per_agg == cells_per_aggregate && h->coarse->shift == ipdg_shift(h))
@@ -333,6 +394,11 @@ extern "C" int dgc_coarse_build(dgc_handle h, int cells_per_aggregate, void* str
       (e = cudaMalloc(&c->d_w[1], n * 8)) || (e = cudaMalloc(&c->d_w[2], n * 8)) ||
       (e = cudaMalloc(&c->d_f[0], n * 4)) || (e = cudaMalloc(&c->d_f[1], n * 4)))
     return fail(cfail(e, "allocation"));
+  // work vectors are summed whole (padding included): start them at zero
+  for (double* w : c->d_w)
+    if ((e = cudaMemset(w, 0, n * 8)) != cudaSuccess) return fail(cfail(e, "clear"));
+  for (float* f : c->d_f)
+    if ((e = cudaMemset(f, 0, n * 4)) != cudaSuccess) return fail(cfail(e, "clear"));
   if ((e = cudaMemcpy(c->d_ptr, ptr.data(), (nagg + 1) * 4, cudaMemcpyHostToDevice)) ||
       (e = cudaMemcpy(c->d_cells, cells.data(), K * 4, cudaMemcpyHostToDevice)) ||
       (e = cudaMemcpy(c->d_agg, c->agg.data(), K * 4, cudaMemcpyHostToDevice)) ||
@@ -411,6 +477,15 @@ extern "C" int dgc_coarse_build(dgc_handle h, int cells_per_aggregate, void* str
   for (int i = 0; i < nagg; ++i)
     if (!(Ac[(size_t)i * nagg + i] > 0.0))
       return fail(set_error(DGC_ERR_DEVICE, "coarse matrix has a non-positive diagonal"));
+  // all-Neumann without shift: S 1 = 0, so P 1 = 1 and A_c has the coarse constants
+  // as null space.  A_c + a 1 1^T / nagg (a = mean diagonal) is regular and acts as
+  // A_c's pseudo-inverse on the zero-sum right-hand sides a consistent residual gives.
+  if (!h->desc.dirichlet && c->shift == 0.0) {
+    double a = 0.0;
+    for (int i = 0; i < nagg; ++i) a += Ac[(size_t)i * nagg + i];
+    a /= (double)nagg * nagg;
+    for (double& v : Ac) v += a;
+  }
   if ((e = cudaMemcpyAsync(c->d_ainv, Ac.data(), Ac.size() * 8, cudaMemcpyHostToDevice, s)) != cudaSuccess)
     return fail(cfail(e, "upload"));
   // Gauss-Jordan in place (SPD: no pivoting); c->d_rc holds the pivot column
@@ -465,6 +540,80 @@ int dgc::coarse_apply(dgc_handle_s* h, const double* r, const double* binv_r, do
   dgk::k_coarse_axpy<<<grid1(n), 256, 0, s>>>(n, w1, om, w0, z, add ? 1 : 0);
   CKC(cudaGetLastError(), "apply");
   h->launches += 5;
+  return DGC_OK;
+}
+
+int dgc::two_level_pcg(dgc_handle_s* h, double* x, double* r, double tol2, int maxit, int* iterations,
+                       cudaStream_t s) {
+  CoarseSpace* c = h->coarse;
+  if (!c) return set_error(DGC_ERR_ARG, "no coarse space: call dgc_coarse_build first");
+  const int64_t n = (int64_t)h->K * h->NpP;
+  if (!c->d_pcg[0]) {
+    for (double*& v : c->d_pcg) {
+      CKC(cudaMalloc(&v, n * 8), "allocation");
+      CKC(cudaMemset(v, 0, n * 8), "clear");
+    }
+    CKC(cudaMalloc(&c->d_dots, 4 * 8), "allocation");
+    CKC(cudaMallocHost(&c->h_dots, 4 * 8), "allocation");
+  }
+  double *z = c->d_pcg[0], *p = c->d_pcg[1], *q = c->d_pcg[2];
+  const int gd = grid1(n);
+  // dots of up to three pairs, returned on the host
+  auto dots = [&](dgk::Dot3 d, double* out) -> int {
+    CKC(cudaMemsetAsync(c->d_dots, 0, 3 * 8, s), "dots");
+    dgk::k_coarse_dots<<<gd, 256, 0, s>>>(n, d, c->d_dots);
+    CKC(cudaGetLastError(), "dots");
+    CKC(cudaMemcpyAsync(c->h_dots, c->d_dots, 3 * 8, cudaMemcpyDeviceToHost, s), "dots");
+    CKC(cudaStreamSynchronize(s), "dots");
+    for (int j = 0; j < 3; ++j) out[j] = c->h_dots[j];
+    ++h->launches;
+    return DGC_OK;
+  };
+  // all-Neumann without shift: the constants are S's null space.  Rounding in the
+  // FP32 smoothing leaks a little of them into the coarse term; unchecked, x drifts
+  // along them until S x loses its accuracy, so z is kept at zero mean.
+  const bool singular = !h->desc.dirichlet && c->shift == 0.0;
+  auto precondition = [&]() -> int {  // z = Binv r + P A_c^-1 P^T r
+    if (int rc = ipdg_block_jacobi_apply(h, r, z, s)) return rc;
+    if (int rc = coarse_apply(h, r, z, z, true, true, s)) return rc;
+    if (singular) {
+      CKC(cudaMemsetAsync(c->d_dots + 3, 0, 8, s), "mean");
+      dgk::k_coarse_valid_sum<<<gd, 256, 0, s>>>(n, h->NpP, h->Np, z, c->d_dots + 3);
+      dgk::k_coarse_sub_mean<<<gd, 256, 0, s>>>(n, h->NpP, h->Np, c->d_dots + 3, (double)h->K * h->Np, z);
+      CKC(cudaGetLastError(), "mean");
+      h->launches += 2;
+    }
+    return DGC_OK;
+  };
+  double d[3];
+  if (int rc = precondition()) return rc;
+  if (int rc = dots({{r, z, nullptr}, {r, r, nullptr}}, d)) return rc;
+  double rr = d[0], rz = d[1];
+  CKC(cudaMemcpyAsync(p, z, n * 8, cudaMemcpyDeviceToDevice, s), "copy");
+  int it = 0;
+  while (rr > tol2 && it < maxit) {
+    if (int rc = dgc_laplace_spd_apply(h, p, q, s)) return rc;
+    if (int rc = dots({{p, nullptr, nullptr}, {q, nullptr, nullptr}}, d)) return rc;
+    // at the rounding floor p.Sp or z.r can lose their sign: leave it to the
+    // caller's true-residual check
+    if (!(d[0] > 0.0) || !(rz > 0.0)) break;
+    const double alpha = rz / d[0];
+    dgk::k_coarse_step<<<gd, 256, 0, s>>>(n, alpha, p, q, x, r);
+    if (int rc = precondition()) return rc;
+    // rr, z.r and z.q (Polak-Ribiere: beta = -alpha z.q / rz_old, robust to the
+    // FP32 rounding inside the coarse term)
+    if (int rc = dots({{r, z, z}, {r, r, q}}, d)) return rc;
+    if (!std::isfinite(d[0]) || !std::isfinite(d[1]) || !std::isfinite(d[2]))
+      return set_error(DGC_ERR_NOT_CONVERGED, "two-level PCG: non-finite residual");
+    rr = d[0];
+    const double beta = -alpha * d[2] / rz;
+    rz = d[1];
+    dgk::k_coarse_dir<<<gd, 256, 0, s>>>(n, z, beta, p);
+    CKC(cudaGetLastError(), "update");
+    h->launches += 2;
+    ++it;
+  }
+  *iterations = it;
   return DGC_OK;
 }
 

@@ -772,8 +772,10 @@ extern "C" int dgc_pcg_solve(dgc_handle h, const double* b, double* x, const dgc
   // r = b - S x (x is the caller's initial guess)
   if (int rc = true_residual<double>(h, b, x, r64, &rr, s)) return rc;
   const bool graph = opts->use_graph != 0;
-  if (opts->mode != DGC_SOLVE_FP64_PCG && opts->mode != DGC_SOLVE_MIXED_IR)
+  if (opts->mode != DGC_SOLVE_FP64_PCG && opts->mode != DGC_SOLVE_MIXED_IR && opts->mode != DGC_SOLVE_TWO_LEVEL)
     return set_error(DGC_ERR_ARG, "unknown solve mode");
+  if (opts->mode == DGC_SOLVE_TWO_LEVEL && !h->coarse)
+    return set_error(DGC_ERR_ARG, "DGC_SOLVE_TWO_LEVEL needs dgc_coarse_build first");
   // Refinement loop on the true FP64 residual.  FP64 mode: each pass solves
   // S d = r in FP64 to a little below the remaining target (a second pass
   // mops up the drift between CG's recursive and true residuals).  Mixed
@@ -788,6 +790,14 @@ extern "C" int dgc_pcg_solve(dgc_handle h, const double* b, double* x, const dgc
     if (budget <= 0) break;
     const double nr = std::sqrt(rr);
     int it = 0, conv = 0;
+    if (opts->mode == DGC_SOLVE_TWO_LEVEL) {
+      // on x and the true residual directly, to a little below the target
+      if (int rc = two_level_pcg(h, x, r64, 0.25 * tol2, budget, &it, s)) return rc;
+      S.inner_iterations += it;
+      ++outer;
+      if (int rc = true_residual<double>(h, b, x, r64, &rr, s)) return rc;
+      continue;
+    }
     if (fp64) {
       CKI(cudaMemcpyAsync(st->w64[W_R], r64, n * 8, cudaMemcpyDeviceToDevice, s));
       const double rel = std::max(0.5 * std::sqrt(tol2 / rr), 1e-15);

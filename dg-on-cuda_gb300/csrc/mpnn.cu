@@ -567,6 +567,13 @@ int grid_for(const dgc_mpnn_s* m, int64_t work, int per_block) {
 
 size_t field_len(const dgc_mpnn_s* m) { return (size_t)m->h->K * m->h->NpP; }
 
+// device allocation cleared to zero: solver vectors are summed whole, padding included
+template <typename T>
+cudaError_t zalloc(T** p, size_t count) {
+  cudaError_t e = cudaMalloc(p, count * sizeof(T));
+  return e == cudaSuccess ? cudaMemset(*p, 0, count * sizeof(T)) : e;
+}
+
 // device scalars (and their pinned host copy) for at least `count` doubles
 int ensure_scal(dgc_mpnn m, int count) {
   if (count <= m->scal_cap) return DGC_OK;
@@ -595,17 +602,17 @@ int ensure_train(dgc_mpnn m, int S) {
   const size_t nW = (size_t)S * m->h->K * dgk::kW, nY = (size_t)S * field_len(m);
   m->hs.assign(m->lay.L + 1, nullptr);
   m->as.assign(m->lay.L, nullptr);
-  for (auto& p : m->hs) CKM(cudaMalloc(&p, nW * 4));
-  for (auto& p : m->as) CKM(cudaMalloc(&p, nW * 4));
-  CKM(cudaMalloc(&m->y, nY * 4));
-  CKM(cudaMalloc(&m->dy, nY * 4));
-  CKM(cudaMalloc(&m->dh0, nW * 4));
-  CKM(cudaMalloc(&m->dh1, nW * 4));
-  CKM(cudaMalloc(&m->g, nW * 4));
-  CKM(cudaMalloc(&m->m, nW * 4));
-  CKM(cudaMalloc(&m->sd, nY * 4));
-  CKM(cudaMalloc(&m->tm, nY * 4));
-  CKM(cudaMalloc(&m->st, nY * 4));
+  for (auto& p : m->hs) CKM(zalloc(&p, nW));
+  for (auto& p : m->as) CKM(zalloc(&p, nW));
+  CKM(zalloc(&m->y, nY));
+  CKM(zalloc(&m->dy, nY));
+  CKM(zalloc(&m->dh0, nW));
+  CKM(zalloc(&m->dh1, nW));
+  CKM(zalloc(&m->g, nW));
+  CKM(zalloc(&m->m, nW));
+  CKM(zalloc(&m->sd, nY));
+  CKM(zalloc(&m->tm, nY));
+  CKM(zalloc(&m->st, nY));
   m->cap = S;
   // [0] loss, [1..S] target norms (L2 loss), [1+S .. 1+3S) per-sample d.Sd, t.St (energy loss)
   return ensure_scal(m, 1 + 3 * S);
@@ -614,11 +621,11 @@ int ensure_train(dgc_mpnn m, int S) {
 int ensure_apply(dgc_mpnn m) {
   if (m->px) return DGC_OK;
   const size_t nW = (size_t)m->h->K * dgk::kW, nY = field_len(m);
-  CKM(cudaMalloc(&m->px, nY * 4));
-  CKM(cudaMalloc(&m->py, nY * 4));
-  CKM(cudaMalloc(&m->ph0, nW * 4));
-  CKM(cudaMalloc(&m->ph1, nW * 4));
-  for (double** p : {&m->bj, &m->r, &m->z}) CKM(cudaMalloc(p, nY * 8));
+  CKM(zalloc(&m->px, nY));
+  CKM(zalloc(&m->py, nY));
+  CKM(zalloc(&m->ph0, nW));
+  CKM(zalloc(&m->ph1, nW));
+  for (double** p : {&m->bj, &m->r, &m->z}) CKM(zalloc(p, nY));
   return ensure_scal(m, 4);
 }
 
@@ -626,8 +633,8 @@ int ensure_apply(dgc_mpnn m) {
 int ensure_fcg(dgc_mpnn m, int window) {
   const size_t nY = field_len(m);
   for (int i = 0; i <= window; ++i) {
-    if (!m->pv[i]) CKM(cudaMalloc(&m->pv[i], nY * 8));
-    if (!m->qv[i]) CKM(cudaMalloc(&m->qv[i], nY * 8));
+    if (!m->pv[i]) CKM(zalloc(&m->pv[i], nY));
+    if (!m->qv[i]) CKM(zalloc(&m->qv[i], nY));
   }
   return ensure_scal(m, dgk::kMaxDots);
 }

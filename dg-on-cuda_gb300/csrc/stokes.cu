@@ -215,8 +215,12 @@ extern "C" int dgc_stokes_handles(dgc_stokes s, dgc_handle* velocity, dgc_handle
 extern "C" int dgc_stokes_set_solver(dgc_stokes s, const dgc_solve_opts* opts) {
   if (!s || !opts) return set_error(DGC_ERR_ARG, "null argument");
   if (!(opts->rtol > 0.0) || opts->maxit <= 0 ||
-      (opts->mode != DGC_SOLVE_FP64_PCG && opts->mode != DGC_SOLVE_MIXED_IR))
+      (opts->mode != DGC_SOLVE_FP64_PCG && opts->mode != DGC_SOLVE_MIXED_IR && opts->mode != DGC_SOLVE_TWO_LEVEL))
     return set_error(DGC_ERR_ARG, "bad solver settings");
+  // two-level: the pressure system gets the coarse space (aggregates of 8 cells,
+  // built once: the pressure handle's shift never changes)
+  if (opts->mode == DGC_SOLVE_TWO_LEVEL)
+    if (int rc = dgc_coarse_build(s->pres, 8, nullptr)) return rc;
   s->opts = *opts;
   return DGC_OK;
 }
@@ -277,6 +281,10 @@ extern "C" int dgc_stokes_step(dgc_stokes s, const double* ux_prev, const double
   // stage 3, viscous (stokes_2d.h:373-390): (A_D - 1.5/dt I) u = -1.5/dt u~ + data
   //   <=>  (S_D + 1.5/dt J M) u = -J M (-1.5/dt u~ + data)
   if (int rc = dgc_laplace_set_shift(vel, 1.5 / dt)) return rc;
+  // the viscous systems are well conditioned (shifted by 1.5/dt J M): block-Jacobi
+  // refinement, also when the pressure solve is two-level
+  dgc_solve_opts vo = s->opts;
+  if (vo.mode == DGC_SOLVE_TWO_LEVEL) vo.mode = DGC_SOLVE_MIXED_IR;
   const double* gdir[2] = {bc->g_x, bc->g_y};
   double* uo[2] = {ux_out, uy_out};
   for (int c = 0; c < 2; ++c) {
@@ -288,7 +296,7 @@ extern "C" int dgc_stokes_step(dgc_stokes s, const double* ux_prev, const double
     // initial guess: u~ after the projection
     e = cudaMemcpyAsync(uo[c], s->ut[c], n * 8, cudaMemcpyDeviceToDevice, st);
     if (e != cudaSuccess) return cuda_fail(e, "viscous initial guess");
-    if (int rc = dgc_pcg_solve(vel, s->b, uo[c], &s->opts, &S, st)) return solve_fail(rc, c ? "viscous y" : "viscous x");
+    if (int rc = dgc_pcg_solve(vel, s->b, uo[c], &vo, &S, st)) return solve_fail(rc, c ? "viscous y" : "viscous x");
     accum();
   }
   if (p_out) {

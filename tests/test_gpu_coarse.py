@@ -127,14 +127,62 @@ def test_learned_solve_two_level_needs_no_fallback():
     assert relerr(D.download(x), D.download(xp)) < 1e-8
 
 
+def test_coarse_apply_neumann_is_pseudo_inverse():
+    """All-Neumann: A_c is singular (P 1 = 1); on zero-sum residuals the
+    regularised inverse equals A_c's pseudo-inverse."""
+    m = meshes.jittered_square(6, 4)
+    D = dg.Discretization(m, "laplace", 2, dg.F64, tau=dg.TAU_ONE, dirichlet=False)
+    D.coarse_build(4)
+    agg, na, _, om = D.coarse_info()
+    O = oracle.Oracle(m.xy, m.cells, 2)
+    n = D.K * D.Np
+    S = np.stack([O.laplace(e, dirichlet=False) for e in np.eye(n)], axis=1)
+    S = -np.stack([O.mass(c) for c in S.T], axis=1)       # -J M A
+    P0 = np.zeros((n, na))
+    Binv = np.zeros((n, n))
+    for k in range(D.K):
+        b = slice(k * D.Np, (k + 1) * D.Np)
+        P0[b, agg[k]] = 1.0
+        Binv[b, b] = np.linalg.inv(S[b, b])
+    P = P0 - om * Binv @ S @ P0
+    Ac = P.T @ S @ P
+    r = np.random.default_rng(0).standard_normal(n)
+    r -= r.mean()
+    ref = P @ np.linalg.pinv(Ac, rcond=1e-12) @ P.T @ r
+    assert relerr(D.download(D.coarse_apply(D.upload(r))), ref) < 1e-9
+
+
+@pytest.mark.parametrize("dirichlet", [True, False])
+def test_two_level_mode_matches_fp64_pcg(dirichlet):
+    m = meshes.jittered_square(40, 6)
+    D = dg.Discretization(m, "laplace", 3, dg.F64, tau=dg.TAU_SCALED if dirichlet else dg.TAU_ONE,
+                          dirichlet=dirichlet)
+    b = poisson_rhs(D)
+    xp, stp = D.pcg(b, rtol=1e-10)
+    D.coarse_build(8)
+    xt, stt = D.pcg(b, mode=dg.SOLVE_TWO_LEVEL, rtol=1e-10)
+    print(f"dirichlet={dirichlet}: two-level {stt['iterations']} vs block-Jacobi {stp['iterations']} iterations")
+    assert stt["converged"] and stt["final_relres"] <= 1e-10
+    assert stt["iterations"] * 3 < stp["iterations"]
+    assert relerr(D.download(xt), D.download(xp)) < 1e-8
+
+
+def test_two_level_mode_needs_coarse_space():
+    m = meshes.jittered_square(4, 1)
+    D = dg.Discretization(m, "laplace", 2, dg.F64, tau=dg.TAU_SCALED, dirichlet=True)
+    with pytest.raises(dg.DgcError):
+        D.pcg(poisson_rhs(D), mode=dg.SOLVE_TWO_LEVEL)
+
+
 def test_coarse_space_refusals():
     m = meshes.jittered_square(4, 1)
     D32 = dg.Discretization(m, "laplace", 2, dg.F32, tau=dg.TAU_SCALED, dirichlet=True)
     with pytest.raises(dg.DgcError):
         D32.coarse_build(4)
-    Dn = dg.Discretization(m, "laplace", 2, dg.F64, tau=dg.TAU_SCALED, dirichlet=False)
+    Dm = dg.Discretization(m, "laplace", 2, dg.F64, tau=dg.TAU_SCALED, dirichlet=True)
+    Dm.set_bc_types((Dm.boundary_nodes()[:, 0] > 0).astype(np.uint8))
     with pytest.raises(dg.DgcError):
-        Dn.coarse_build(4)
+        Dm.coarse_build(4)                              # per-node boundary types
     D = dg.Discretization(m, "laplace", 2, dg.F64, tau=dg.TAU_SCALED, dirichlet=True)
     with pytest.raises(dg.DgcError):
         D.coarse_apply(D.upload(np.ones(D.K * D.Np)))   # not built
@@ -142,3 +190,19 @@ def test_coarse_space_refusals():
     D.set_shift(3.0)
     with pytest.raises(dg.DgcError):
         D.coarse_apply(D.upload(np.ones(D.K * D.Np)))   # built for shift 0
+
+
+@pytest.mark.parametrize("prec", [dg.F64, dg.F32])
+@pytest.mark.parametrize("N", [1, 2, 3, 4, 5, 8])
+def test_spd_apply_writes_zero_padding(N, prec):
+    """Solvers sum whole vectors: S u must leave 0, not stale memory, in the
+    padded node slots of its output (orders where NpP > Np)."""
+    m = meshes.jittered_square(5, 1)
+    D = dg.Discretization(m, "laplace", N, prec, tau=dg.TAU_SCALED, dirichlet=True)
+    assert D.NpP > D.Np
+    u = D.upload(np.random.default_rng(N).standard_normal(D.K * D.Np))
+    out = torch.full((D.state_len,), float("nan"), dtype=D.torch_dtype, device="cuda")
+    D.spd(u, out=out)
+    pad = out.view(D.K, D.NpP)[:, D.Np:]
+    assert torch.all(pad == 0)
+    assert torch.isfinite(out).all()

@@ -180,3 +180,20 @@ def test_learned_solve_without_fallback_when_budget_suffices():
     x, st = net.solve(b, rtol=1e-10, fcg_maxit=2 * stp["iterations"])
     assert not st["fell_back"] and st["converged"] and st["final_relres"] <= 1e-10
     assert st["iterations"] == st["inner_iterations"]
+
+
+def test_fcg_independent_of_stale_device_memory():
+    """Work vectors start at zero and S u writes its padding: a flexible CG run
+    after NaN-filled memory went back to the driver behaves as in a fresh process."""
+    junk = torch.full((256 << 20,), float("nan"), dtype=torch.float32, device="cuda")
+    del junk
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    m = meshes.jittered_square(8, 9)
+    D = dg.Discretization(m, "laplace", 3, dg.F64, tau=dg.TAU_SCALED, dirichlet=True)
+    b = poisson_rhs(D)
+    xp, stp = D.pcg(b, mode=dg.SOLVE_FP64_PCG, rtol=1e-10, graph=False)
+    net = dg.MPNN(D, layers=1, seed=0)
+    xf, stf = net.fpcg(b, rtol=1e-10, window=4)
+    assert stf["converged"] and abs(stf["iterations"] - stp["iterations"]) <= max(2, 0.05 * stp["iterations"])
+    assert relerr(D.download(xf), D.download(xp)) < 1e-8

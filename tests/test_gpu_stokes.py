@@ -81,11 +81,12 @@ def test_consistent_operator_exact_at_scale(N):
     assert np.abs(r + 2.0).max() > 1.0
 
 
+@pytest.mark.parametrize("mode", [dg.SOLVE_MIXED_IR, dg.SOLVE_TWO_LEVEL])
 @pytest.mark.parametrize("consistent", [False, True])
 @pytest.mark.parametrize("N", [2, 3])
-def test_stokes_step_matches_dense_restatement(N, consistent):
+def test_stokes_step_matches_dense_restatement(N, consistent, mode):
     m = meshes.jittered_square(4, 1)
-    S = st.Stokes(m, N, consistent=consistent, rtol=1e-11)
+    S = st.Stokes(m, N, consistent=consistent, rtol=1e-11, mode=mode)
     O = so.StokesOracle(m.xy, m.cells, N, consistent=consistent)
     vs = S.velocity_space
     x, y = (a.reshape(-1) for a in vs.node_xy())
