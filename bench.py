@@ -193,6 +193,7 @@ def measured_peak():
 
 
 POISSON_NSIDE, POISSON_ORDER, POISSON_SEED = 256, 4, 4242
+POISSON_AGGREGATE = 32                          # cells per aggregate of the two-level line
 
 
 def fourier_rhs(x, y, seed: int, modes: int = 32):
@@ -211,21 +212,32 @@ def measure_poisson(dg, meshes):
     """IPDG Poisson -lap u = f, Dirichlet u = 0, jittered 256x256 mesh (K = 131072),
     N = 4, tau = (N+1)^2 / h: FP64 block-Jacobi PCG against FP32 inner PCG in
     FP64 iterative refinement, both to 1e-10 relative FP64 residual, for the
-    manufactured solution sin(pi x) sin(pi y) and a 32-mode Fourier right-hand side."""
+    manufactured solution sin(pi x) sin(pi y) and a 32-mode Fourier right-hand side.
+    An extra line (no counterpart in the workload's definition): the two-level PCG
+    (block-Jacobi + smoothed-aggregation coarse space of POISSON_AGGREGATE cells)."""
     import torch
     m = meshes.jittered_square(POISSON_NSIDE, POISSON_SEED)
     D = dg.Discretization(m, "laplace", POISSON_ORDER, dg.F64, tau=dg.TAU_SCALED, dirichlet=True)
     x, y = D.node_xy()
     D.block_jacobi()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    D.coarse_build(POISSON_AGGREGATE)
+    torch.cuda.synchronize()
+    _, n_agg, n_col, omega = D.coarse_info()
     out = {"workload": f"ipdg_poisson_dirichlet_k{D.K}_n{POISSON_ORDER}", "num_cells": D.K,
-           "order": POISSON_ORDER, "rtol": 1e-10, "cases": {}}
+           "order": POISSON_ORDER, "rtol": 1e-10,
+           "two_level": {"cells_per_aggregate": POISSON_AGGREGATE, "aggregates": n_agg, "colours": n_col,
+                         "omega": omega, "build_s": time.perf_counter() - t0},
+           "cases": {}}
     cases = {"manufactured": 2 * np.pi ** 2 * np.sin(np.pi * x) * np.sin(np.pi * y),
              "fourier32": fourier_rhs(x, y, POISSON_SEED)}
     for name, f in cases.items():
         b = D.mass(D.upload(f.reshape(-1)))
         res = {}
         sols = {}
-        for mode, tag in ((dg.SOLVE_FP64_PCG, "fp64_pcg"), (dg.SOLVE_MIXED_IR, "mixed_ir")):
+        for mode, tag in ((dg.SOLVE_FP64_PCG, "fp64_pcg"), (dg.SOLVE_MIXED_IR, "mixed_ir"),
+                          (dg.SOLVE_TWO_LEVEL, "two_level")):
             D.pcg(b, mode=mode, rtol=1e-10, maxit=40000, check=False)  # warm-up (graphs, preconditioner)
             torch.cuda.synchronize()
             t0 = time.perf_counter()
@@ -236,13 +248,46 @@ def measure_poisson(dg, meshes):
             res[tag] = {k: st[k] for k in ("iterations", "outer_iterations", "converged", "final_relres", "wall_s")}
         ref = sols["fp64_pcg"]
         res["rel_l2_mixed_vs_fp64"] = float(np.linalg.norm(sols["mixed_ir"] - ref) / np.linalg.norm(ref))
+        res["rel_l2_two_level_vs_fp64"] = float(np.linalg.norm(sols["two_level"] - ref) / np.linalg.norm(ref))
         if name == "manufactured":
             ex = (np.sin(np.pi * x) * np.sin(np.pi * y)).reshape(-1)
             for tag in sols:
                 res[tag]["rel_l2_vs_exact"] = float(np.linalg.norm(sols[tag] - ex) / np.linalg.norm(ex))
         res["speedup_mixed_vs_fp64"] = res["fp64_pcg"]["wall_s"] / res["mixed_ir"]["wall_s"]
+        res["speedup_two_level_vs_fp64"] = res["fp64_pcg"]["wall_s"] / res["two_level"]["wall_s"]
+        res["speedup_two_level_vs_mixed"] = res["mixed_ir"]["wall_s"] / res["two_level"]["wall_s"]
         out["cases"][name] = res
     D.check()
+    return out
+
+
+STOKES_NSIDE, STOKES_ORDER, STOKES_SEED, STOKES_STEPS, STOKES_DT = 128, 4, 77, 10, 1e-3
+
+
+def measure_stokes(dg, meshes):
+    """The Stokes example's dual-splitting step (examples/stokes_2d) on a jittered
+    128x128 mesh (K = 32768), N = 4, from its exact initial velocity (u^-1 = u^0),
+    STOKES_STEPS steps of dt = 1e-3, the Dirichlet data in the consistent form:
+    time per step and the error against the analytic solution, with the pressure
+    system solved by block-Jacobi refinement and by the two-level PCG."""
+    import torch
+    from dgc_gb300 import stokes as st
+    m = meshes.jittered_square(STOKES_NSIDE, STOKES_SEED)
+    out = {"workload": f"stokes_dual_splitting_k{m.cells.shape[0]}_n{STOKES_ORDER}", "num_cells": m.cells.shape[0],
+           "order": STOKES_ORDER, "dt": STOKES_DT, "steps": STOKES_STEPS,
+           "data": "exact initial velocity, consistent Dirichlet data, rtol 1e-10 per solve"}
+    for tag, mode in (("mixed_ir", dg.SOLVE_MIXED_IR), ("two_level", dg.SOLVE_TWO_LEVEL)):
+        S = st.Stokes(m, STOKES_ORDER, consistent=True, rtol=1e-10, mode=mode)
+        S.run_example(T=2 * STOKES_DT, dt=STOKES_DT)                     # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        _, _, t, err, iters = S.run_example(T=STOKES_STEPS * STOKES_DT, dt=STOKES_DT)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        out[tag] = {"ms_per_step": wall / STOKES_STEPS * 1e3, "solver_iterations_per_step": iters / STOKES_STEPS,
+                    "error_norm": err, "T": t}
+        S.close()
+    out["speedup_two_level_vs_mixed"] = out["mixed_ir"]["ms_per_step"] / out["two_level"]["ms_per_step"]
     return out
 
 
@@ -603,6 +648,7 @@ def main():
     ap.add_argument("--no-poisson", action="store_true", help="skip the IPDG Poisson solver comparison")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-instances comparison")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-preconditioner comparison")
+    ap.add_argument("--no-stokes", action="store_true", help="skip the Stokes dual-splitting timing")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -709,6 +755,9 @@ def main():
     learned = None
     if rank == 0 and not args.no_learned:
         learned = measure_learned(dg, meshes)
+    stokes = None
+    if rank == 0 and not args.no_stokes:
+        stokes = measure_stokes(dg, meshes)
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         csteps = 10
@@ -725,7 +774,7 @@ def main():
                 "clocks": clocks, "fp64_plain": fp64,
                 "speedup_mixed_vs_fp64": (value / ws / fp64["value"]) if fp64 else None,
                 "accuracy": accuracy, "poisson": poisson, "batched": batched, "learned_precond": learned,
-                "wall_s_timed_region": wall}
+                "stokes": stokes, "wall_s_timed_region": wall}
         print(json.dumps(line))
     if ws > 1:
         import torch.distributed as tdist
