@@ -237,7 +237,7 @@ def measure_poisson(dg, meshes):
         res = {}
         sols = {}
         for mode, tag in ((dg.SOLVE_FP64_PCG, "fp64_pcg"), (dg.SOLVE_MIXED_IR, "mixed_ir"),
-                          (dg.SOLVE_TWO_LEVEL, "two_level")):
+                          (dg.SOLVE_TWO_LEVEL, "two_level"), (dg.SOLVE_TWO_LEVEL_MIXED, "two_level_mixed")):
             D.pcg(b, mode=mode, rtol=1e-10, maxit=40000, check=False)  # warm-up (graphs, preconditioner)
             torch.cuda.synchronize()
             t0 = time.perf_counter()
@@ -249,6 +249,8 @@ def measure_poisson(dg, meshes):
         ref = sols["fp64_pcg"]
         res["rel_l2_mixed_vs_fp64"] = float(np.linalg.norm(sols["mixed_ir"] - ref) / np.linalg.norm(ref))
         res["rel_l2_two_level_vs_fp64"] = float(np.linalg.norm(sols["two_level"] - ref) / np.linalg.norm(ref))
+        res["rel_l2_two_level_mixed_vs_fp64"] = float(np.linalg.norm(sols["two_level_mixed"] - ref) /
+                                                      np.linalg.norm(ref))
         if name == "manufactured":
             ex = (np.sin(np.pi * x) * np.sin(np.pi * y)).reshape(-1)
             for tag in sols:
@@ -256,6 +258,7 @@ def measure_poisson(dg, meshes):
         res["speedup_mixed_vs_fp64"] = res["fp64_pcg"]["wall_s"] / res["mixed_ir"]["wall_s"]
         res["speedup_two_level_vs_fp64"] = res["fp64_pcg"]["wall_s"] / res["two_level"]["wall_s"]
         res["speedup_two_level_vs_mixed"] = res["mixed_ir"]["wall_s"] / res["two_level"]["wall_s"]
+        res["speedup_two_level_mixed_vs_mixed"] = res["mixed_ir"]["wall_s"] / res["two_level_mixed"]["wall_s"]
         out["cases"][name] = res
     D.check()
     return out
@@ -276,7 +279,8 @@ def measure_stokes(dg, meshes):
     out = {"workload": f"stokes_dual_splitting_k{m.cells.shape[0]}_n{STOKES_ORDER}", "num_cells": m.cells.shape[0],
            "order": STOKES_ORDER, "dt": STOKES_DT, "steps": STOKES_STEPS,
            "data": "exact initial velocity, consistent Dirichlet data, rtol 1e-10 per solve"}
-    for tag, mode in (("mixed_ir", dg.SOLVE_MIXED_IR), ("two_level", dg.SOLVE_TWO_LEVEL)):
+    for tag, mode in (("mixed_ir", dg.SOLVE_MIXED_IR), ("two_level", dg.SOLVE_TWO_LEVEL),
+                      ("two_level_mixed", dg.SOLVE_TWO_LEVEL_MIXED)):
         S = st.Stokes(m, STOKES_ORDER, consistent=True, rtol=1e-10, mode=mode)
         S.run_example(T=2 * STOKES_DT, dt=STOKES_DT)                     # warm-up
         torch.cuda.synchronize()

@@ -543,7 +543,7 @@ int dgc::coarse_apply(dgc_handle_s* h, const double* r, const double* binv_r, do
   return DGC_OK;
 }
 
-int dgc::two_level_pcg(dgc_handle_s* h, double* x, double* r, double tol2, int maxit, int* iterations,
+int dgc::two_level_pcg(dgc_handle_s* h, double* x, double* r, double tol2, int maxit, int* iterations, bool op32,
                        cudaStream_t s) {
   CoarseSpace* c = h->coarse;
   if (!c) return set_error(DGC_ERR_ARG, "no coarse space: call dgc_coarse_build first");
@@ -591,8 +591,18 @@ int dgc::two_level_pcg(dgc_handle_s* h, double* x, double* r, double tol2, int m
   double rr = d[0], rz = d[1];
   CKC(cudaMemcpyAsync(p, z, n * 8, cudaMemcpyDeviceToDevice, s), "copy");
   int it = 0;
+  // q = S p in FP64, or through the FP32 kernels (the caller refines on the FP64 residual)
+  auto apply = [&]() -> int {
+    if (!op32) return dgc_laplace_spd_apply(h, p, q, s);
+    dgk::k_coarse_to_f32<<<gd, 256, 0, s>>>(n, p, c->d_f[0]);
+    if (int rc = ipdg_spd_apply_f32(h, c->d_f[0], c->d_f[1], s)) return rc;
+    dgk::k_coarse_to_f64<<<gd, 256, 0, s>>>(n, c->d_f[1], q);
+    CKC(cudaGetLastError(), "apply");
+    h->launches += 2;
+    return DGC_OK;
+  };
   while (rr > tol2 && it < maxit) {
-    if (int rc = dgc_laplace_spd_apply(h, p, q, s)) return rc;
+    if (int rc = apply()) return rc;
     if (int rc = dots({{p, nullptr, nullptr}, {q, nullptr, nullptr}}, d)) return rc;
     // at the rounding floor p.Sp or z.r can lose their sign: leave it to the
     // caller's true-residual check

@@ -68,8 +68,9 @@ int coarse_apply(dgc_handle_s* h, const double* r, const double* binv_r, double*
                  cudaStream_t s);
 void coarse_free(CoarseSpace* c);
 // flexible PCG with M = Binv + coarse term from the residual r (updated) on x, until
-// r.r <= tol2 or maxit iterations
-int two_level_pcg(dgc_handle_s* h, double* x, double* r, double tol2, int maxit, int* iterations, cudaStream_t s);
+// r.r <= tol2 or maxit iterations; op32: S applied through the FP32 kernels
+int two_level_pcg(dgc_handle_s* h, double* x, double* r, double tol2, int maxit, int* iterations, bool op32,
+                  cudaStream_t s);
 // device list of the cells with a boundary face (laplace handles)
 int ipdg_boundary_cells(const dgc_handle_s* h, const int** cells, int* n);
 // out = S u with the FP32 kernels (any laplace handle; one field, native layout)

@@ -772,10 +772,10 @@ extern "C" int dgc_pcg_solve(dgc_handle h, const double* b, double* x, const dgc
   // r = b - S x (x is the caller's initial guess)
   if (int rc = true_residual<double>(h, b, x, r64, &rr, s)) return rc;
   const bool graph = opts->use_graph != 0;
-  if (opts->mode != DGC_SOLVE_FP64_PCG && opts->mode != DGC_SOLVE_MIXED_IR && opts->mode != DGC_SOLVE_TWO_LEVEL)
+  const bool two_level = opts->mode == DGC_SOLVE_TWO_LEVEL || opts->mode == DGC_SOLVE_TWO_LEVEL_MIXED;
+  if (opts->mode != DGC_SOLVE_FP64_PCG && opts->mode != DGC_SOLVE_MIXED_IR && !two_level)
     return set_error(DGC_ERR_ARG, "unknown solve mode");
-  if (opts->mode == DGC_SOLVE_TWO_LEVEL && !h->coarse)
-    return set_error(DGC_ERR_ARG, "DGC_SOLVE_TWO_LEVEL needs dgc_coarse_build first");
+  if (two_level && !h->coarse) return set_error(DGC_ERR_ARG, "the two-level modes need dgc_coarse_build first");
   // Refinement loop on the true FP64 residual.  FP64 mode: each pass solves
   // S d = r in FP64 to a little below the remaining target (a second pass
   // mops up the drift between CG's recursive and true residuals).  Mixed
@@ -790,9 +790,12 @@ extern "C" int dgc_pcg_solve(dgc_handle h, const double* b, double* x, const dgc
     if (budget <= 0) break;
     const double nr = std::sqrt(rr);
     int it = 0, conv = 0;
-    if (opts->mode == DGC_SOLVE_TWO_LEVEL) {
-      // on x and the true residual directly, to a little below the target
-      if (int rc = two_level_pcg(h, x, r64, 0.25 * tol2, budget, &it, s)) return rc;
+    if (two_level) {
+      // on x and the true residual directly: to a little below the target in FP64,
+      // by inner_rtol per pass with the FP32 operator (the true residual is refined here)
+      const bool op32 = opts->mode == DGC_SOLVE_TWO_LEVEL_MIXED;
+      const double t2 = op32 ? std::max(0.25 * tol2, inner * inner * rr) : 0.25 * tol2;
+      if (int rc = two_level_pcg(h, x, r64, t2, budget, &it, op32, s)) return rc;
       S.inner_iterations += it;
       ++outer;
       if (int rc = true_residual<double>(h, b, x, r64, &rr, s)) return rc;

@@ -215,11 +215,11 @@ extern "C" int dgc_stokes_handles(dgc_stokes s, dgc_handle* velocity, dgc_handle
 extern "C" int dgc_stokes_set_solver(dgc_stokes s, const dgc_solve_opts* opts) {
   if (!s || !opts) return set_error(DGC_ERR_ARG, "null argument");
   if (!(opts->rtol > 0.0) || opts->maxit <= 0 ||
-      (opts->mode != DGC_SOLVE_FP64_PCG && opts->mode != DGC_SOLVE_MIXED_IR && opts->mode != DGC_SOLVE_TWO_LEVEL))
+      opts->mode < DGC_SOLVE_FP64_PCG || opts->mode > DGC_SOLVE_TWO_LEVEL_MIXED)
     return set_error(DGC_ERR_ARG, "bad solver settings");
   // two-level: the pressure system gets the coarse space (aggregates of 8 cells,
   // built once: the pressure handle's shift never changes)
-  if (opts->mode == DGC_SOLVE_TWO_LEVEL)
+  if (opts->mode == DGC_SOLVE_TWO_LEVEL || opts->mode == DGC_SOLVE_TWO_LEVEL_MIXED)
     if (int rc = dgc_coarse_build(s->pres, 8, nullptr)) return rc;
   s->opts = *opts;
   return DGC_OK;
@@ -284,7 +284,7 @@ extern "C" int dgc_stokes_step(dgc_stokes s, const double* ux_prev, const double
   // the viscous systems are well conditioned (shifted by 1.5/dt J M): block-Jacobi
   // refinement, also when the pressure solve is two-level
   dgc_solve_opts vo = s->opts;
-  if (vo.mode == DGC_SOLVE_TWO_LEVEL) vo.mode = DGC_SOLVE_MIXED_IR;
+  if (vo.mode == DGC_SOLVE_TWO_LEVEL || vo.mode == DGC_SOLVE_TWO_LEVEL_MIXED) vo.mode = DGC_SOLVE_MIXED_IR;
   const double* gdir[2] = {bc->g_x, bc->g_y};
   double* uo[2] = {ux_out, uy_out};
   for (int c = 0; c < 2; ++c) {

@@ -61,7 +61,7 @@ class SolveStats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
-SOLVE_FP64_PCG, SOLVE_MIXED_IR, SOLVE_TWO_LEVEL = 0, 1, 2
+SOLVE_FP64_PCG, SOLVE_MIXED_IR, SOLVE_TWO_LEVEL, SOLVE_TWO_LEVEL_MIXED = 0, 1, 2, 3
 BC_DATA_REFERENCE, BC_DATA_CONSISTENT = 0, 1
 ERR_NOT_CONVERGED = -6
 

@@ -288,9 +288,11 @@ int dgc_mass_apply(dgc_handle h, const double* f, double* out, void* stream);
 typedef enum dgc_solve_mode {
   DGC_SOLVE_FP64_PCG = 0, /* block-Jacobi PCG in FP64 */
   DGC_SOLVE_MIXED_IR = 1, /* FP32 block-Jacobi PCG inside FP64 iterative refinement */
-  DGC_SOLVE_TWO_LEVEL = 2 /* FP64 PCG with M = Binv + P A_c^-1 P^T, the coarse space of
-                             dgc_coarse_build (which must precede the solve); restarts
-                             from the true residual; no counterpart in the reference */
+  DGC_SOLVE_TWO_LEVEL = 2, /* FP64 PCG with M = Binv + P A_c^-1 P^T, the coarse space of
+                              dgc_coarse_build (which must precede the solve); restarts
+                              from the true residual; no counterpart in the reference */
+  DGC_SOLVE_TWO_LEVEL_MIXED = 3 /* the same with S applied in FP32 inside each pass, each
+                                   pass to inner_rtol, refined on the FP64 residual */
 } dgc_solve_mode;
 
 typedef struct dgc_solve_opts {
@@ -463,8 +465,8 @@ int dgc_stokes_destroy(dgc_stokes s);
  * node coordinates, layout conversion and boundary nodes come from them. */
 int dgc_stokes_handles(dgc_stokes s, dgc_handle* velocity, dgc_handle* pressure);
 /* Solver of the pressure and viscous systems (default: mixed refinement,
- * rtol 1e-10, maxit 200000).  DGC_SOLVE_TWO_LEVEL builds the coarse space on
- * the pressure handle (aggregates of 8 cells) and solves the pressure system
+ * rtol 1e-10, maxit 200000).  The two-level modes build the coarse space on
+ * the pressure handle (aggregates of 8 cells) and solve the pressure system
  * with it; the viscous systems then use mixed refinement.  The FP64 residual of the singular pressure
  * system stalls near 1e-16 cond(S), so tighter targets fail on fine meshes. */
 int dgc_stokes_set_solver(dgc_stokes s, const dgc_solve_opts* opts);

@@ -81,7 +81,7 @@ def test_consistent_operator_exact_at_scale(N):
     assert np.abs(r + 2.0).max() > 1.0
 
 
-@pytest.mark.parametrize("mode", [dg.SOLVE_MIXED_IR, dg.SOLVE_TWO_LEVEL])
+@pytest.mark.parametrize("mode", [dg.SOLVE_MIXED_IR, dg.SOLVE_TWO_LEVEL, dg.SOLVE_TWO_LEVEL_MIXED])
 @pytest.mark.parametrize("consistent", [False, True])
 @pytest.mark.parametrize("N", [2, 3])
 def test_stokes_step_matches_dense_restatement(N, consistent, mode):
