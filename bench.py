@@ -587,11 +587,15 @@ def measure_e2e(D32, bufs, res, flush, stream, t, dt, steps, ws, dofs, barrier):
         h_out.copy_(bufs[1], non_blocking=True)
         evs[it][1].record(stream)
     barrier()
-    ms = replicas.max_over_ranks(float(np.mean([a.elapsed_time(b) for a, b in evs])), device="cuda")
+    per = np.array([a.elapsed_time(b) for a, b in evs])
+    ms = replicas.max_over_ranks(float(np.mean(per)), device="cuda")
     nbytes = D32.state_len * 4
+    # the host's memory and CPU-GPU link are shared with other jobs on the machine:
+    # the spread of the per-step times shows how much of that this run met
     return {"value": replicas.job_throughput(dofs * 5, ms * 1e-3, ws) / 1e9, "unit": UNIT,
             "h2d_bytes_per_step": nbytes,
             "d2h_bytes_per_step": nbytes, "ms_per_step": ms,
+            "ms_per_step_min_median_max": [float(per.min()), float(np.median(per)), float(per.max())],
             "path": "dgc_lserk4_step via ctypes, pinned host state in and out every step"}
 
 
@@ -663,6 +667,9 @@ def main():
     from dgc_gb300 import meshes, replicas
 
     ws, rank, local = dist_env()
+    # host threads and pinned buffers next to this rank's GPU: the e2e copies then
+    # take the GPU's own CPU link instead of crossing between sockets
+    bound = replicas.bind_local_cpus(local)
     torch.cuda.set_device(local)
     if ws > 1:
         import torch.distributed as tdist
@@ -745,6 +752,9 @@ def main():
                          "ctas_per_sm": D32.info.rhs_blocks_per_sm, "autotune_ms": tune_ms}}
 
     e2e = None if args.no_e2e else measure_e2e(D32, bufs, res, flush, stream, t, dt, args.steps, ws, dofs, barrier)
+    if e2e is not None:
+        e2e["host_cpus"] = (f"{len(bound)} CPUs of the GPU's NUMA node ({bound[0]}-{bound[-1]})" if bound
+                            else "unbound (GPU NUMA node not found)")
     D64, fp64 = (None, None) if args.no_fp64 else measure_fp64(dg, m, q_init, dt, flush, stream,
                                                                 max(3, min(args.steps, 10)), dofs)
     accuracy = None

@@ -36,3 +36,54 @@ def job_throughput(units_per_rank: float, seconds_slowest: float, world_size: in
     if seconds_slowest <= 0.0:
         raise ValueError("seconds_slowest must be positive")
     return world_size * units_per_rank / seconds_slowest
+
+
+def _parse_cpulist(text: str) -> set:
+    """'0-3,8,10-11' -> {0, 1, 2, 3, 8, 10, 11}."""
+    cpus = set()
+    for part in text.strip().split(","):
+        if not part:
+            continue
+        if "-" in part:
+            a, b = part.split("-")
+            cpus.update(range(int(a), int(b) + 1))
+        else:
+            cpus.add(int(part))
+    return cpus
+
+
+def gpu_local_cpus(pci_bus_id: str, sysfs: str = "/sys") -> set:
+    """CPUs of the NUMA node the GPU at `pci_bus_id` (e.g. "00000009:01:00.0")
+    is attached to, from sysfs; an empty set when the node is unknown."""
+    import os
+    dom, rest = pci_bus_id.strip().lower().split(":", 1)
+    dev = f"{int(dom, 16):04x}:{rest}"
+    try:
+        with open(os.path.join(sysfs, "bus", "pci", "devices", dev, "numa_node")) as f:
+            node = int(f.read().strip())
+        if node < 0:
+            return set()
+        with open(os.path.join(sysfs, "devices", "system", "node", f"node{node}", "cpulist")) as f:
+            return _parse_cpulist(f.read())
+    except (OSError, ValueError):
+        return set()
+
+
+def bind_local_cpus(device: int = 0) -> list:
+    """Restrict this process to the CPUs next to GPU `device` (before any pinned
+    host memory is allocated: first touch then places it on that node, so
+    host-device copies take the GPU's own CPU link).  Returns the CPUs bound,
+    [] when the placement could not be determined (then nothing changes)."""
+    import os
+    import subprocess
+    try:
+        out = subprocess.run(["nvidia-smi", "--query-gpu=pci.bus_id", "--format=csv,noheader", "-i", str(device)],
+                             capture_output=True, text=True, timeout=30)
+        cpus = gpu_local_cpus(out.stdout.strip()) if out.returncode == 0 else set()
+        cpus &= os.sched_getaffinity(0)
+        if not cpus:
+            return []
+        os.sched_setaffinity(0, cpus)
+        return sorted(cpus)
+    except (OSError, ValueError, subprocess.SubprocessError):
+        return []

@@ -55,3 +55,25 @@ def test_single_process_is_identity():
     assert replicas.job_throughput(10.0, 2.0, 1) == 5.0
     with pytest.raises(ValueError):
         replicas.job_throughput(1.0, 0.0, 1)
+
+
+def test_gpu_local_cpus_from_sysfs(tmp_path):
+    from dgc_gb300 import replicas
+    dev = tmp_path / "bus" / "pci" / "devices" / "0009:01:00.0"
+    dev.mkdir(parents=True)
+    (dev / "numa_node").write_text("1\n")
+    node = tmp_path / "devices" / "system" / "node" / "node1"
+    node.mkdir(parents=True)
+    (node / "cpulist").write_text("72-75,80,90-91\n")
+    assert replicas.gpu_local_cpus("00000009:01:00.0", sysfs=str(tmp_path)) == {72, 73, 74, 75, 80, 90, 91}
+    (dev / "numa_node").write_text("-1\n")
+    assert replicas.gpu_local_cpus("00000009:01:00.0", sysfs=str(tmp_path)) == set()
+    assert replicas.gpu_local_cpus("00000001:02:00.0", sysfs=str(tmp_path)) == set()
+
+
+def test_bind_local_cpus_without_gpu_changes_nothing():
+    import os
+    from dgc_gb300 import replicas
+    before = os.sched_getaffinity(0)
+    assert replicas.bind_local_cpus(0) == [] or set(replicas.bind_local_cpus(0)) <= before
+    assert os.sched_getaffinity(0) <= before
