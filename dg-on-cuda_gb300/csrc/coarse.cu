@@ -54,8 +54,9 @@ struct CoarseSpace {
   double* d_w[3] = {};                // work vectors (K x NpP)
   float* d_f[2] = {};                 // FP32 work vectors of the FP32 smoothing applies
   double* d_pcg[3] = {};              // two-level PCG: z, p, q = S p (allocated on first use)
-  double* d_dots = nullptr;           // [4] dot products
-  double* h_dots = nullptr;           // pinned mirror
+  double* d_dots = nullptr;           // [4] dot products of the current kernel pair, [3] a mean
+  double* d_sc = nullptr;             // [8] device-resident CG scalars (k_coarse_step_dev)
+  double* h_sc = nullptr;             // pinned mirror
 };
 
 void coarse_free(CoarseSpace* c) {
@@ -63,9 +64,9 @@ void coarse_free(CoarseSpace* c) {
   for (void* p : {(void*)c->d_ptr, (void*)c->d_cells, (void*)c->d_agg, (void*)c->d_ainv, (void*)c->d_rc,
                   (void*)c->d_xc, (void*)c->d_w[0], (void*)c->d_w[1], (void*)c->d_w[2], (void*)c->d_f[0],
                   (void*)c->d_f[1], (void*)c->d_pcg[0], (void*)c->d_pcg[1], (void*)c->d_pcg[2],
-                  (void*)c->d_dots})
+                  (void*)c->d_dots, (void*)c->d_sc})
     cudaFree(p);
-  cudaFreeHost(c->h_dots);
+  cudaFreeHost(c->h_sc);
   delete c;
 }
 
@@ -144,18 +145,42 @@ __global__ void k_coarse_sub_mean(int64_t n, int npp, int np, const double* __re
     if ((int)(i % npp) < np) z[i] -= m;
 }
 
-// x += alpha p, r -= alpha q
-__global__ void k_coarse_step(int64_t n, double alpha, const double* __restrict__ p, const double* __restrict__ q,
-                              double* __restrict__ x, double* __restrict__ r) {
+// The two-level PCG keeps its scalars on the device, so that its kernels queue
+// back to back: sc[0], sc[1] = z.r by iteration parity, sc[3] = r.r, sc[5] =
+// alpha, sc[6] = stop flag (positivity lost); t = the dot products of the kernel
+// just before.
+// x += alpha p, r -= alpha q with alpha = z.r / p.q (t[0] = p.q)
+__global__ void k_coarse_step_dev(int64_t n, const double* __restrict__ p, const double* __restrict__ q,
+                                  double* __restrict__ x, double* __restrict__ r, double* sc,
+                                  const double* __restrict__ t, int cur) {
+  const double rz = sc[cur], pq = t[0];
+  // at the rounding floor p.Sp or z.r can lose their sign: stop, the caller
+  // checks the true residual
+  const bool ok = pq > 0.0 && rz > 0.0 && sc[6] == 0.0;
+  const double alpha = ok ? rz / pq : 0.0;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    sc[5] = alpha;
+    if (!ok) sc[6] = 1.0;
+  }
+  if (!ok) return;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     x[i] += alpha * p[i];
     r[i] -= alpha * q[i];
   }
 }
-// p = z + beta p
-__global__ void k_coarse_dir(int64_t n, const double* __restrict__ z, double beta, double* __restrict__ p) {
+// p = z + beta p, beta = -alpha z.q / (z.r)_old (Polak-Ribiere, robust to the FP32
+// rounding inside the coarse term); t = (r.r, z.r, z.q) of the new residual.  The
+// new z.r goes to the other parity slot: no block reads what another writes.
+__global__ void k_coarse_dir_dev(int64_t n, const double* __restrict__ z, double* __restrict__ p, double* sc,
+                                 const double* __restrict__ t, int cur, int nxt, int first) {
+  const double rzo = sc[cur];
+  const double beta = (first || sc[6] != 0.0 || !(rzo > 0.0)) ? 0.0 : -sc[5] * t[2] / rzo;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    p[i] = z[i] + beta * p[i];
+    p[i] = first ? z[i] : z[i] + beta * p[i];
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    sc[nxt] = t[1];
+    sc[3] = t[0];
+  }
 }
 
 // in-place Gauss-Jordan step i of an SPD matrix: col[r] = A[r][i]
@@ -554,18 +579,19 @@ int dgc::two_level_pcg(dgc_handle_s* h, double* x, double* r, double tol2, int m
       CKC(cudaMemset(v, 0, n * 8), "clear");
     }
     CKC(cudaMalloc(&c->d_dots, 4 * 8), "allocation");
-    CKC(cudaMallocHost(&c->h_dots, 4 * 8), "allocation");
+    CKC(cudaMalloc(&c->d_sc, 8 * 8), "allocation");
+    CKC(cudaMallocHost(&c->h_sc, 8 * 8), "allocation");
   }
   double *z = c->d_pcg[0], *p = c->d_pcg[1], *q = c->d_pcg[2];
+  double *t = c->d_dots, *sc = c->d_sc;
   const int gd = grid1(n);
-  // dots of up to three pairs, returned on the host
-  auto dots = [&](dgk::Dot3 d, double* out) -> int {
-    CKC(cudaMemsetAsync(c->d_dots, 0, 3 * 8, s), "dots");
-    dgk::k_coarse_dots<<<gd, 256, 0, s>>>(n, d, c->d_dots);
+  // reductions end in one atomic per block on the same few addresses: 2 blocks per SM
+  const int gr = std::max(1, std::min(gd, 2 * h->sm_count));
+  // dots of up to three pairs into t, left on the device
+  auto dots = [&](dgk::Dot3 d) -> int {
+    CKC(cudaMemsetAsync(t, 0, 3 * 8, s), "dots");
+    dgk::k_coarse_dots<<<gr, 256, 0, s>>>(n, d, t);
     CKC(cudaGetLastError(), "dots");
-    CKC(cudaMemcpyAsync(c->h_dots, c->d_dots, 3 * 8, cudaMemcpyDeviceToHost, s), "dots");
-    CKC(cudaStreamSynchronize(s), "dots");
-    for (int j = 0; j < 3; ++j) out[j] = c->h_dots[j];
     ++h->launches;
     return DGC_OK;
   };
@@ -577,20 +603,14 @@ int dgc::two_level_pcg(dgc_handle_s* h, double* x, double* r, double tol2, int m
     if (int rc = ipdg_block_jacobi_apply(h, r, z, s)) return rc;
     if (int rc = coarse_apply(h, r, z, z, true, true, s)) return rc;
     if (singular) {
-      CKC(cudaMemsetAsync(c->d_dots + 3, 0, 8, s), "mean");
-      dgk::k_coarse_valid_sum<<<gd, 256, 0, s>>>(n, h->NpP, h->Np, z, c->d_dots + 3);
-      dgk::k_coarse_sub_mean<<<gd, 256, 0, s>>>(n, h->NpP, h->Np, c->d_dots + 3, (double)h->K * h->Np, z);
+      CKC(cudaMemsetAsync(t + 3, 0, 8, s), "mean");
+      dgk::k_coarse_valid_sum<<<gr, 256, 0, s>>>(n, h->NpP, h->Np, z, t + 3);
+      dgk::k_coarse_sub_mean<<<gd, 256, 0, s>>>(n, h->NpP, h->Np, t + 3, (double)h->K * h->Np, z);
       CKC(cudaGetLastError(), "mean");
       h->launches += 2;
     }
     return DGC_OK;
   };
-  double d[3];
-  if (int rc = precondition()) return rc;
-  if (int rc = dots({{r, z, nullptr}, {r, r, nullptr}}, d)) return rc;
-  double rr = d[0], rz = d[1];
-  CKC(cudaMemcpyAsync(p, z, n * 8, cudaMemcpyDeviceToDevice, s), "copy");
-  int it = 0;
   // q = S p in FP64, or through the FP32 kernels (the caller refines on the FP64 residual)
   auto apply = [&]() -> int {
     if (!op32) return dgc_laplace_spd_apply(h, p, q, s);
@@ -601,27 +621,40 @@ int dgc::two_level_pcg(dgc_handle_s* h, double* x, double* r, double tol2, int m
     h->launches += 2;
     return DGC_OK;
   };
-  while (rr > tol2 && it < maxit) {
+  // read r.r and the stop flag (synchronises the stream)
+  auto check = [&](double* rr, bool* stop) -> int {
+    CKC(cudaMemcpyAsync(c->h_sc, sc, 8 * 8, cudaMemcpyDeviceToHost, s), "scalars");
+    CKC(cudaStreamSynchronize(s), "scalars");
+    *rr = c->h_sc[3];
+    *stop = c->h_sc[6] != 0.0;
+    if (!std::isfinite(*rr)) return set_error(DGC_ERR_NOT_CONVERGED, "two-level PCG: non-finite residual");
+    return DGC_OK;
+  };
+  CKC(cudaMemsetAsync(sc, 0, 8 * 8, s), "scalars");
+  if (int rc = precondition()) return rc;
+  if (int rc = dots({{r, z, nullptr}, {r, r, nullptr}})) return rc;
+  dgk::k_coarse_dir_dev<<<gd, 256, 0, s>>>(n, z, p, sc, t, 0, 0, 1);  // p = z, sc[0] = z.r, sc[3] = r.r
+  CKC(cudaGetLastError(), "start");
+  double rr = 0.0;
+  bool stop = false;
+  if (int rc = check(&rr, &stop)) return rc;
+  // the host looks at r.r every kCheck iterations: the kernels in between queue
+  // without a round trip
+  constexpr int kCheck = 8;
+  int it = 0;
+  while (rr > tol2 && !stop && it < maxit) {
+    const int cur = it & 1;
     if (int rc = apply()) return rc;
-    if (int rc = dots({{p, nullptr, nullptr}, {q, nullptr, nullptr}}, d)) return rc;
-    // at the rounding floor p.Sp or z.r can lose their sign: leave it to the
-    // caller's true-residual check
-    if (!(d[0] > 0.0) || !(rz > 0.0)) break;
-    const double alpha = rz / d[0];
-    dgk::k_coarse_step<<<gd, 256, 0, s>>>(n, alpha, p, q, x, r);
+    if (int rc = dots({{p, nullptr, nullptr}, {q, nullptr, nullptr}})) return rc;
+    dgk::k_coarse_step_dev<<<gd, 256, 0, s>>>(n, p, q, x, r, sc, t, cur);
     if (int rc = precondition()) return rc;
-    // rr, z.r and z.q (Polak-Ribiere: beta = -alpha z.q / rz_old, robust to the
-    // FP32 rounding inside the coarse term)
-    if (int rc = dots({{r, z, z}, {r, r, q}}, d)) return rc;
-    if (!std::isfinite(d[0]) || !std::isfinite(d[1]) || !std::isfinite(d[2]))
-      return set_error(DGC_ERR_NOT_CONVERGED, "two-level PCG: non-finite residual");
-    rr = d[0];
-    const double beta = -alpha * d[2] / rz;
-    rz = d[1];
-    dgk::k_coarse_dir<<<gd, 256, 0, s>>>(n, z, beta, p);
+    if (int rc = dots({{r, z, z}, {r, r, q}})) return rc;
+    dgk::k_coarse_dir_dev<<<gd, 256, 0, s>>>(n, z, p, sc, t, cur, cur ^ 1, 0);
     CKC(cudaGetLastError(), "update");
     h->launches += 2;
     ++it;
+    if (it % kCheck == 0 || it == maxit)
+      if (int rc = check(&rr, &stop)) return rc;
   }
   *iterations = it;
   return DGC_OK;
