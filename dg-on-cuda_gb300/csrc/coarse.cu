@@ -1,7 +1,8 @@
-// coarse.cu -- coarse space of the two-level learned preconditioner (C ABI:
-// dgc_coarse_build / dgc_coarse_apply / dgc_coarse_aggregates; used by the
-// flexible CG of mpnn.cu through dgc_mpnn_set_coarse).  No counterpart in the
-// reference, which solves its systems directly.
+// coarse.cu -- two-level preconditioning of the SPD laplace form (C ABI:
+// dgc_coarse_build / dgc_coarse_apply / dgc_coarse_info): the coarse space, the
+// two-level PCG behind dgc_pcg_solve's DGC_SOLVE_TWO_LEVEL(_MIXED) modes, and the
+// coarse term of the learned preconditioner (mpnn.cu, dgc_mpnn_set_coarse).  No
+// counterpart in the reference, which solves its systems directly.
 //
 // Block-Jacobi on the element blocks of S = -J M A removes the error inside
 // each element, but the smooth, mesh-wide error modes it leaves are what
@@ -26,8 +27,11 @@
 // A_c; A_c inverted in place on the GPU by Gauss-Jordan without pivoting
 // (SPD).  Apply: P^T r = P0^T (r - w S Binv r), a deterministic restriction
 // (one warp per aggregate over its cells, fixed order), a dense FP64 product
-// with A_c^-1 (one warp per row; the matrix stays in L2), the prolongation
-// y = P0 x_c and z += y - w Binv S y.
+// with A_c^-1 (one warp per row), the prolongation y = P0 x_c and
+// z += y - w Binv S y.  All-Neumann handles without shift have the constants as
+// null space (P 1 = 1): A_c gets a rank-one term that makes it regular and
+// leaves its action on consistent (zero-sum) residuals unchanged, and the
+// two-level PCG keeps its preconditioned residual at zero mean.
 #include <cuda_runtime.h>
 
 #include <algorithm>

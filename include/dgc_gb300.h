@@ -380,9 +380,11 @@ int dgc_mpnn_set_coarse(dgc_mpnn m, int cells_per_aggregate, void* stream);
  * prolongation P = (I - omega Binv S) P0 is smoothed once with block Jacobi
  * (omega = 4 / (3 lambda_max(Binv S)), lambda_max from 20 power iterations
  * times 1.1), and A_c = P^T S P is the Galerkin coarse matrix of the SPD form
- * S (FP64 Dirichlet handles with uniform boundary types; the shift at build
- * time), inverted once on the GPU.  Rebuilding with the same size and shift
- * is a no-op. */
+ * S (FP64 laplace handles with uniform boundary types; the shift at build
+ * time), inverted once on the GPU.  All-Neumann handles without shift: A_c is
+ * singular (P 1 = 1) and is used through a rank-one regularisation that acts
+ * as its pseudo-inverse on zero-sum residuals.  Rebuilding with the same size
+ * and shift is a no-op; a failed rebuild leaves the handle without one. */
 int dgc_coarse_build(dgc_handle h, int cells_per_aggregate, void* stream);
 /* z = P A_c^-1 P^T r (device FP64, native layout; z distinct from r).
  * precision DGC_F32 runs the two applies of S inside P and P^T through the
