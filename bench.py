@@ -576,8 +576,14 @@ def measure_e2e(D32, bufs, res, flush, stream, t, dt, steps, ws, dofs, barrier):
     from dgc_gb300 import replicas
     h_state = torch.empty(D32.state_len, dtype=torch.float32, pin_memory=True)
     h_state.copy_(bufs[0].cpu())
-    h_out = torch.empty_like(h_state)
+    # pinned as well (empty_like would not pin it): a pageable target is staged
+    # through a bounce buffer and page-faults on its first write
+    h_out = torch.empty(D32.state_len, dtype=torch.float32, pin_memory=True)
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for _ in range(3):  # warm-up: the same three calls, untimed
+        bufs[0].copy_(h_state, non_blocking=True)
+        D32.lserk4_step(bufs[0], bufs[1], res, t, dt)
+        h_out.copy_(bufs[1], non_blocking=True)
     barrier()
     for it in range(steps):
         flush.fill_(float(it))

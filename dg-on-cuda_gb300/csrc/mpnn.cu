@@ -565,6 +565,10 @@ int grid_for(const dgc_mpnn_s* m, int64_t work, int per_block) {
   return (int)std::max<int64_t>(1, std::min<int64_t>(b, (int64_t)m->sm_count * 8));
 }
 
+// reductions end in one atomic per block and product on the same few addresses:
+// 2 blocks per SM
+int dot_grid(const dgc_mpnn_s* m, int64_t n) { return std::min(grid_for(m, n, 256), 2 * std::max(m->sm_count, 1)); }
+
 size_t field_len(const dgc_mpnn_s* m) { return (size_t)m->h->K * m->h->NpP; }
 
 // device allocation cleared to zero: solver vectors are summed whole, padding included
@@ -670,7 +674,7 @@ int dots(dgc_mpnn m, const double* a, std::initializer_list<const double*> bs, d
   d.cnt = 0;
   for (const double* b : bs) d.b[d.cnt++] = b;
   CKM(cudaMemsetAsync(m->scal, 0, d.cnt * sizeof(double), s));
-  dgk::k_mdot<<<grid_for(m, n, 256), 256, 0, s>>>(n, d, m->scal);
+  dgk::k_mdot<<<dot_grid(m, n), 256, 0, s>>>(n, d, m->scal);
   CKM(cudaGetLastError());
   CKM(cudaMemcpyAsync(m->h_scal, m->scal, d.cnt * sizeof(double), cudaMemcpyDeviceToHost, s));
   CKM(cudaStreamSynchronize(s));
@@ -939,7 +943,7 @@ extern "C" int dgc_fpcg_solve(dgc_handle h, dgc_mpnn m, const double* b, double*
       dl.b[0] = m->r;
       for (int j = 0; j < nprev; ++j) dl.b[1 + j] = m->qv[(k - 1 - j + slots) % slots];
       CKM(cudaMemsetAsync(m->scal, 0, dl.cnt * sizeof(double), s));
-      dgk::k_mdot<<<gd, 256, 0, s>>>(n, dl, m->scal);
+      dgk::k_mdot<<<dot_grid(m, n), 256, 0, s>>>(n, dl, m->scal);
       CKM(cudaGetLastError());
       CKM(cudaMemcpyAsync(m->h_scal, m->scal, dl.cnt * sizeof(double), cudaMemcpyDeviceToHost, s));
       CKM(cudaStreamSynchronize(s));
