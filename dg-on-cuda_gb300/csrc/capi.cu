@@ -699,7 +699,7 @@ std::string tune_key(dgc_handle h) {
   cudaGetDeviceProperties(&prop, h->device);
   int kb = 0;
   while ((1 << (kb + 1)) <= h->K) ++kb;  // K bucket: floor(log2 K)
-  char buf[256];
+  char buf[sizeof prop.name + 96];  // the device name can fill its 256 bytes
   std::snprintf(buf, sizeof buf, "%s|sm%d|phys%d|prec%d|N%d|K2^%d", prop.name, prop.multiProcessorCount,
                 h->desc.physics, h->prec, h->N, kb);
   for (char* c = buf; *c; ++c)

@@ -391,9 +391,10 @@ __global__ void __launch_bounds__(256) ipdg_div_kernel(const IpdgParams p) {
       }
     }
     // padded output nodes are written as 0 (callers sum over whole vectors)
-    if (NpP > Np)
-      for (int q = threadIdx.x; q < ne * (NpP - Np); q += blockDim.x)
-        static_cast<R*>(p.out)[(size_t)(k0 + q / (NpP - Np)) * NpP + Np + q % (NpP - Np)] = (R)0;
+    constexpr int kPad = NpP - Np;
+    if constexpr (kPad > 0)
+      for (int q = threadIdx.x; q < ne * kPad; q += blockDim.x)
+        static_cast<R*>(p.out)[(size_t)(k0 + q / kPad) * NpP + Np + q % kPad] = (R)0;
     __syncthreads();
   }
   if (MODE == DIV_SPD_DOT || MODE == DIV_RESID) {

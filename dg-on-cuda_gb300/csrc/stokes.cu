@@ -55,8 +55,8 @@ __global__ void k_stokes_bdf2(size_t n, const double* __restrict__ ux0, const do
   }
 }
 
-// y = a x, or y += a x when acc
-__global__ void k_stokes_scal(size_t n, double a, const double* __restrict__ x, double* __restrict__ y, int acc) {
+// y = a x, or y += a x when acc (y may be x: scaled in place)
+__global__ void k_stokes_scal(size_t n, double a, const double* x, double* y, int acc) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
     y[i] = acc ? y[i] + a * x[i] : a * x[i];
 }

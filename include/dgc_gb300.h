@@ -3,7 +3,7 @@
  *
  * A drop-in for the GPU path of hsongxa/dg-on-cuda on 2D triangle meshes:
  * the device discretisation and operators (src/d_simple_discretization_2d.cuh,
- * examples/*\/d_*_2d.cuh), their launchers (src/device_SemiDiscOp_wrapper.cuh,
+ * examples/<example>/d_<example>.cuh), their launchers (src/device_SemiDiscOp_wrapper.cuh,
  * src/kernel_adapter.cuh), the time integrator (src/explicit_runge_kutta.h,
  * src/k_axpy.cuh) and the laplace_2d IPDG operator (src/laplace_2d.h).
  *
