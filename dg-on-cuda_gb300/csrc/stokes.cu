@@ -9,7 +9,7 @@
 // The reference's boundary objects become per-node arrays over the boundary
 // face nodes (the caller evaluates the example's analytic functions at
 // dgc_boundary_nodes).  The pressure Neumann data hp (eq. 18 of Fehn et al.
-// 2017, formed as in stokes_2d.h:190-263) is computed here on the boundary
+// 2017, formed as in stokes_2d.h:191-269) is computed here on the boundary
 // cells: the curl-curl term of u^n and u^(n-1) with the strong Dr, Ds, plus
 // the caller's dg/dt dotted with the face normal.  Where the reference
 // assembles A column by column and factors it with cuSOLVER's host LU
@@ -45,7 +45,7 @@ struct dgc_stokes_s {
 
 namespace dgk {
 
-// ut = (4 u - u_prev) / 3 for both components (stokes_2d.h:407-411)
+// ut = (4 u - u_prev) / 3 for both components (stokes_2d.h:394-405)
 __global__ void k_stokes_bdf2(size_t n, const double* __restrict__ ux0, const double* __restrict__ uy0,
                               const double* __restrict__ ux1, const double* __restrict__ uy1,
                               double* __restrict__ utx, double* __restrict__ uty) {
@@ -62,7 +62,7 @@ __global__ void k_stokes_scal(size_t n, double a, const double* x, double* y, in
 }
 
 // Pressure Neumann data on the boundary cells, one CTA of 64 threads each
-// (stokes_2d.h:190-263):
+// (stokes_2d.h:191-269):
 //   c = curl u^(n-1) - 2 curl u^n,  curl u = Dx uy - Dy ux,
 //   h2[b] = 2 hp[b],  hp = (dg/dt).n + (Dy c) nx - (Dx c) ny   at boundary node b,
 // the reference's exterior_grad_n(x, y, 0) = 2 hp.  Strong-form Dr, Ds

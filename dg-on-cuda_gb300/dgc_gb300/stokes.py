@@ -14,7 +14,7 @@ import numpy as np
 from . import (BC_DATA_CONSISTENT, BC_DATA_REFERENCE, LAYOUT_REF_CPU, SOLVE_MIXED_IR, Discretization, SolveOpts,
                SolveStats, _check, _ptr, _stream, _vp, lib)
 
-# the example problem (examples/stokes_2d/stokes_2d.h:95-96)
+# the example problem (examples/stokes_2d/stokes_2d.h:103-104)
 A = 2.883356
 LAMBDA = 1.0 + A * A
 
@@ -28,7 +28,7 @@ def _gy(x, y):
 
 
 def exact_velocity(x, y, t):
-    """stokes_2d::exact_solution (stokes_2d.h:308-340)."""
+    """stokes_2d::exact_solution (stokes_2d.h:313-340)."""
     e = np.exp(-LAMBDA * t)
     return _gx(x, y) * e, _gy(x, y) * e
 
@@ -36,7 +36,7 @@ def exact_velocity(x, y, t):
 def example_boundary_data(bx, by, t, t_prev, dt):
     """The example's boundary objects at the boundary nodes for the step
     t -> t + dt: u_tilde_bc and u_x_bc / u_y_bc exterior_val(x, y, 0), and the
-    dgdt terms of pressure_bc's hp (stokes_2d.h:100-184, 245-248)."""
+    dgdt terms of pressure_bc's hp (stokes_2d.h:108-188, 245-248)."""
     gx, gy = _gx(bx, by), _gy(bx, by)
     e_t, e_p, e_n = np.exp(-LAMBDA * t), np.exp(-LAMBDA * t_prev), np.exp(-LAMBDA * (t + dt))
     return dict(ut_x=2.0 * (4.0 * gx * e_t - gx * e_p) / 3.0, ut_y=2.0 * (4.0 * gy * e_t - gy * e_p) / 3.0,

@@ -242,7 +242,7 @@ int dgc_laplace_apply(dgc_handle h, const void* u, void* out, void* stream);
 
 /* Shift of the SPD form: S = -blockdiag(J_k M) (A - shift I) = S_0 + shift J M
  * for the Helmholtz-type systems (A - shift I) u = f of implicit diffusion
- * steps (examples/stokes_2d/stokes_2d.h:464-481 assembles A - 1.5/dt I).
+ * steps (examples/stokes_2d/stokes_2d.h:442-460 assembles A - 1.5/dt I).
  * Used by dgc_laplace_spd_apply, dgc_pcg_solve and the block-Jacobi blocks
  * (rebuilt when the shift changes); shift >= 0, default 0. */
 int dgc_laplace_set_shift(dgc_handle h, double shift);
@@ -452,13 +452,13 @@ typedef struct dgc_stokes_s* dgc_stokes;
 typedef struct dgc_stokes_bc {
   const double* ut_x;   /* u_tilde_bc::exterior_val(x, y, 0): 2 (4 g(t^n) - g(t^(n-1))) / 3 */
   const double* ut_y;
-  const double* dgdt_x; /* the dgdt term of pressure_bc's hp at t^(n+1) (stokes_2d.h:245-248; the
+  const double* dgdt_x; /* the dgdt term of pressure_bc's hp at t^(n+1) (stokes_2d.h:260-262; the
                            example's lamda g e^(-lamda t), i.e. -dg/dt) */
   const double* dgdt_y;
   const double* g_x;    /* u_x_bc / u_y_bc::exterior_val(x, y, 0): 2 g(t^(n+1)) */
   const double* g_y;
 } dgc_stokes_bc;
-/* Replaces stokes_2d(mesh, order) (examples/stokes_2d/stokes_2d.h:265-276):
+/* Replaces stokes_2d(mesh, order) (examples/stokes_2d/stokes_2d.h:271-282):
  * two laplace handles on the mesh plus workspace.  order in [1, 8]. */
 int dgc_stokes_create(int num_vertices, const double* vertex_xy, int num_cells, const int32_t* cells, int order,
                       dgc_stokes* out);

@@ -21,7 +21,7 @@ import numpy as np
 
 from oracle import Oracle, face_nodes, operators, STRONG
 
-# the example problem (stokes_2d.h:95-96)
+# the example problem (stokes_2d.h:103-104)
 A = 2.883356
 LAMBDA = 1.0 + A * A
 
@@ -36,14 +36,14 @@ def gy_fn(x, y):
 
 
 def exact(x, y, t):
-    """exact_solution (stokes_2d.h:308-340)."""
+    """exact_solution (stokes_2d.h:313-340)."""
     e = np.exp(-LAMBDA * t)
     return gx_fn(x, y) * e, gy_fn(x, y) * e
 
 
 def boundary_data(bx, by, t, t_prev, dt):
     """The example's boundary objects at boundary nodes (bx, by) for the step
-    t -> t + dt (stokes_2d.h:100-184, 245-247): u_tilde_bc exterior_val(x, y, 0),
+    t -> t + dt (stokes_2d.h:108-188, 245-247): u_tilde_bc exterior_val(x, y, 0),
     the dgdt terms of pressure_bc's hp, u_x_bc / u_y_bc exterior_val(x, y, 0)."""
     gx, gy = gx_fn(bx, by), gy_fn(bx, by)
     e_t, e_p, e_n = np.exp(-LAMBDA * t), np.exp(-LAMBDA * t_prev), np.exp(-LAMBDA * (t + dt))
@@ -79,7 +79,7 @@ class StokesOracle:
         self.bxy = np.stack([self.arr["bx"], self.arr["by"]], axis=1)
 
     def hp(self, ux0, uy0, ux1, uy1, dgdt_x, dgdt_y):
-        """pressure_bc's hp per boundary node (stokes_2d.h:190-263); u0 = u^(n-1), u1 = u^n."""
+        """pressure_bc's hp per boundary node (stokes_2d.h:191-269); u0 = u^(n-1), u1 = u^n."""
         K, Np = self.K, self.Np
         invJ = self.arr["invJ"].reshape(K, 4)
         nx, ny = self.arr["nx"].reshape(K, 3), self.arr["ny"].reshape(K, 3)

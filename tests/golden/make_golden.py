@@ -71,7 +71,7 @@ def stokes_cases(oracle_dir: str, tmp: str) -> None:
     mesh = meshes.jittered_square(4, seed=7)
     mpath = os.path.join(tmp, "stokes_mesh.bin")
     meshes.write_bin(mesh, mpath)
-    a, lam = 2.883356, 1.0 + 2.883356 ** 2   # stokes_2d.h:95-96
+    a, lam = 2.883356, 1.0 + 2.883356 ** 2   # stokes_2d.h:103-104
 
     def probe(N, t_prev, t, dt, u, p=None):
         spath, opath = os.path.join(tmp, "state.bin"), os.path.join(tmp, "stokes_out.bin")
