@@ -266,7 +266,7 @@ int dgc_laplace_bc_rhs(dgc_handle h, const double* g, const double* hn, void* ou
 /* What dgc_laplace_bc_rhs adds for Dirichlet data.  REFERENCE (default):
  * exactly apply_inhomogeneous_as_rhs, whose second pass adds the lifted data
  * q_d = -LIFT(n g faceJ / 2) / J only through boundary-face terms
- * (src/laplace_2d.h:302-347).  CONSISTENT: also the jumps of q_d across
+ * (src/laplace_2d.h:310-348).  CONSISTENT: also the jumps of q_d across
  * interior faces and 2 q_d.n on Neumann faces, which apply_homogeneous has for
  * the same lift (same file:222-242); dgc_laplace_apply(u) minus this term is
  * then the affine operator of the scheme, exact on polynomials of degree <= N
