@@ -575,7 +575,7 @@ __global__ void __launch_bounds__(64) ipdg_bc_rhs_kernel(const IpdgParams p, con
 
 // The jumps of the lifted Dirichlet data q_d that apply_inhomogeneous_as_rhs
 // leaves out (its second pass adds only boundary-face terms, laplace_2d.h:
-// 302-347, where apply_homogeneous's dqN also holds the jumps of q across
+// 310-348, where apply_homogeneous's dqN also holds the jumps of q across
 // interior faces and 2 q.n on Neumann faces, :222-242).  q_d as stored by
 // ipdg_bc_rhs_kernel in p.qx / p.qy (zero off the boundary cells); on each
 // listed cell (a boundary cell or a face neighbour of one), one CTA of 64
