@@ -17,7 +17,7 @@ they compute as compressed .npz files:
   ref_known_answers.json    mean-square nodal errors of the reference drivers'
                             runs on the reference's coarse mesh (10000 RK4
                             steps of advection, Maxwell to T = 1)
-  ref_stokes_jit4_N<N>.npz  two steps of the Stokes example's dual splitting
+  ref_stokes_jit4_N<N>.npz  two steps of the Stokes example's dual splitting (N = 2, 3, 4)
                             from its exact initial data: everything the
                             reference forms (pressure_bc's hp, right-hand
                             sides, grad p, the projected u~), with the two
@@ -82,7 +82,7 @@ def stokes_cases(oracle_dir: str, tmp: str) -> None:
         subprocess.run([exe, mpath, str(N), spath, opath], check=True)
         return read_dump(opath)
 
-    for N in (2, 3):
+    for N in (2, 3, 4):
         Np = (N + 1) * (N + 2) // 2
         n = mesh.cells.shape[0] * Np
         d0 = probe(N, 0.0, 0.0, 1.0, [np.zeros(n)] * 4)

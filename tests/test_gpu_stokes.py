@@ -147,7 +147,7 @@ def test_stokes_example_converges_with_consistent_data():
     assert errs[False] > 1e-2
 
 
-@pytest.mark.parametrize("N", [2, 3])
+@pytest.mark.parametrize("N", [2, 3, 4])
 def test_stokes_step_matches_reference_golden(N):
     """dgc_stokes_step from the reference's own step inputs (tests/golden/
     ref_stokes_jit4_N*.npz: stokes_2d probed up to its solves, solved densely):

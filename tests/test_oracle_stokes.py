@@ -116,7 +116,7 @@ import os  # noqa: E402
 
 from conftest import GOLDEN  # noqa: E402
 
-STOKES_CASES = [2, 3]
+STOKES_CASES = [2, 3, 4]
 
 
 def _golden(N):
