@@ -169,3 +169,19 @@ def test_stokes_step_matches_reference(N):
         ux, uy, p = s.step(g["u0x"], g["u0y"], g["u1x"], g["u1y"], dt, bc)
         assert _rel(ux, g["ux"]) < 1e-10 and _rel(uy, g["uy"]) < 1e-10, k
         assert _rel(p, g["p"]) < 1e-9, k
+
+
+def test_product_example_data_matches_oracle():
+    """The Stokes example's boundary data and exact velocity are written twice,
+    in the product module and in the oracle: they must agree."""
+    from dgc_gb300 import stokes as st
+    rng = np.random.default_rng(3)
+    x, y = rng.uniform(-1, 1, 50), rng.uniform(-1, 1, 50)
+    for t, tp, dt in ((0.0, 0.0, 1e-3), (0.02, 0.019, 1e-3), (0.5, 0.49, 0.01)):
+        a = st.example_boundary_data(x, y, t, tp, dt)
+        b = so.boundary_data(x, y, t, tp, dt)
+        assert a.keys() == b.keys()
+        for k in a:
+            assert np.array_equal(a[k], b[k]), k
+        for u, v in zip(st.exact_velocity(x, y, t), so.exact(x, y, t)):
+            assert np.array_equal(u, v)
