@@ -157,16 +157,24 @@ __global__ void k_coarse_sub_mean(int64_t n, int npp, int np, const double* __re
 __global__ void k_coarse_step_dev(int64_t n, const double* __restrict__ p, const double* __restrict__ q,
                                   double* __restrict__ x, double* __restrict__ r, double* sc,
                                   const double* __restrict__ t, int cur) {
-  const double rz = sc[cur], pq = t[0];
-  // at the rounding floor p.Sp or z.r can lose their sign: stop, the caller
-  // checks the true residual
-  const bool ok = pq > 0.0 && rz > 0.0 && sc[6] == 0.0;
-  const double alpha = ok ? rz / pq : 0.0;
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    sc[5] = alpha;
-    if (!ok) sc[6] = 1.0;
+  // one FP64 division per block, not per thread (GB300's FP64 rate is low)
+  __shared__ double s_alpha;
+  __shared__ int s_ok;
+  if (threadIdx.x == 0) {
+    const double rz = sc[cur], pq = t[0];
+    // at the rounding floor p.Sp or z.r can lose their sign: stop, the caller
+    // checks the true residual
+    const bool ok = pq > 0.0 && rz > 0.0 && sc[6] == 0.0;
+    s_alpha = ok ? rz / pq : 0.0;
+    s_ok = ok;
+    if (blockIdx.x == 0) {
+      sc[5] = s_alpha;
+      if (!ok) sc[6] = 1.0;
+    }
   }
-  if (!ok) return;
+  __syncthreads();
+  const double alpha = s_alpha;
+  if (!s_ok) return;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     x[i] += alpha * p[i];
     r[i] -= alpha * q[i];
@@ -177,8 +185,13 @@ __global__ void k_coarse_step_dev(int64_t n, const double* __restrict__ p, const
 // new z.r goes to the other parity slot: no block reads what another writes.
 __global__ void k_coarse_dir_dev(int64_t n, const double* __restrict__ z, double* __restrict__ p, double* sc,
                                  const double* __restrict__ t, int cur, int nxt, int first) {
-  const double rzo = sc[cur];
-  const double beta = (first || sc[6] != 0.0 || !(rzo > 0.0)) ? 0.0 : -sc[5] * t[2] / rzo;
+  __shared__ double s_beta;
+  if (threadIdx.x == 0) {
+    const double rzo = sc[cur];
+    s_beta = (first || sc[6] != 0.0 || !(rzo > 0.0)) ? 0.0 : -sc[5] * t[2] / rzo;
+  }
+  __syncthreads();
+  const double beta = s_beta;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     p[i] = first ? z[i] : z[i] + beta * p[i];
   if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -553,7 +566,7 @@ int dgc::coarse_apply(dgc_handle_s* h, const double* r, const double* binv_r, do
   };
   // P^T r = P0^T (r - w S Binv r)
   if (!binv_r) {
-    if (int rc = ipdg_block_jacobi_apply(h, r, w0, s)) return rc;
+    if (int rc = ipdg_block_jacobi_apply(h, r, w0, s, fp32)) return rc;
     binv_r = w0;
   }
   if (int rc = S(binv_r, w1)) return rc;
@@ -565,7 +578,7 @@ int dgc::coarse_apply(dgc_handle_s* h, const double* r, const double* binv_r, do
   dgk::k_coarse_prolong<<<grid1(n), 256, 0, s>>>(n, h->NpP, h->Np, c->d_agg, c->d_xc, 0, w1);
   CKC(cudaGetLastError(), "apply");
   if (int rc = S(w1, w2)) return rc;
-  if (int rc = ipdg_block_jacobi_apply(h, w2, w0, s)) return rc;
+  if (int rc = ipdg_block_jacobi_apply(h, w2, w0, s, fp32)) return rc;
   dgk::k_coarse_axpy<<<grid1(n), 256, 0, s>>>(n, w1, om, w0, z, add ? 1 : 0);
   CKC(cudaGetLastError(), "apply");
   h->launches += 5;
@@ -603,8 +616,8 @@ int dgc::two_level_pcg(dgc_handle_s* h, double* x, double* r, double tol2, int m
   // FP32 smoothing leaks a little of them into the coarse term; unchecked, x drifts
   // along them until S x loses its accuracy, so z is kept at zero mean.
   const bool singular = !h->desc.dirichlet && c->shift == 0.0;
-  auto precondition = [&]() -> int {  // z = Binv r + P A_c^-1 P^T r
-    if (int rc = ipdg_block_jacobi_apply(h, r, z, s)) return rc;
+  auto precondition = [&]() -> int {  // z = Binv r + P A_c^-1 P^T r, Binv and the coarse term in FP32
+    if (int rc = ipdg_block_jacobi_apply(h, r, z, s, true)) return rc;
     if (int rc = coarse_apply(h, r, z, z, true, true, s)) return rc;
     if (singular) {
       CKC(cudaMemsetAsync(t + 3, 0, 8, s), "mean");

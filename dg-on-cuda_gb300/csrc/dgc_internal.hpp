@@ -56,9 +56,10 @@ void device_free(dgc_handle_s* h);
 int ipdg_init(dgc_handle_s* h);
 void ipdg_free(dgc_handle_s* h);
 void ipdg_operators_changed(dgc_handle_s* h);
-// block-Jacobi inverse of the SPD laplace form (built once), and z = Binv r (FP64)
+// block-Jacobi inverse of the SPD laplace form (built once), and z = Binv r
+// (FP64 vectors; the blocks and sums in FP32 with fp32)
 int ipdg_build_preconditioner(dgc_handle_s* h, cudaStream_t s);
-int ipdg_block_jacobi_apply(dgc_handle_s* h, const double* r, double* z, cudaStream_t s);
+int ipdg_block_jacobi_apply(dgc_handle_s* h, const double* r, double* z, cudaStream_t s, bool fp32 = false);
 // the SPD form's shift, and whether the boundary types are the handle's uniform ones
 double ipdg_shift(const dgc_handle_s* h);
 bool ipdg_uniform_bc(const dgc_handle_s* h);

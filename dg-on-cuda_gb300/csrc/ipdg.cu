@@ -393,26 +393,33 @@ int ipdg_build_preconditioner(dgc_handle_s* h, cudaStream_t s) {
   return DGC_OK;
 }
 
-// z = Binv r elementwise (FP64, native layout; padding nodes of z set to 0)
-__global__ void k_bj_apply(int K, int Np, int NpP, int bstr, const double* __restrict__ binv,
+// z = Binv r elementwise (FP64 vectors, native layout; padding nodes of z set to
+// 0), the blocks and the sums in B's type: FP64 for block-Jacobi PCG, FP32
+// inside the two-level preconditioner (half the bytes; measured at the same
+// time per launch, so the access pattern, not the arithmetic, bounds it)
+template <typename B>
+__global__ void k_bj_apply(int K, int Np, int NpP, int bstr, const B* __restrict__ binv,
                            const double* __restrict__ r, double* __restrict__ z) {
   const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (g >= (int64_t)K * NpP) return;
   const int k = (int)(g / NpP), i = (int)(g % NpP);
-  double s = 0.0;
+  B s = 0;
   if (i < Np) {
-    const double* B = binv + (size_t)k * bstr;
+    const B* Bk = binv + (size_t)k * bstr;
     const double* rk = r + (size_t)k * NpP;
-    for (int j = 0; j < Np; ++j) s += B[j * Np + i] * rk[j];
+    for (int j = 0; j < Np; ++j) s += Bk[j * Np + i] * (B)rk[j];
   }
-  z[g] = s;
+  z[g] = (double)s;
 }
 
-int ipdg_block_jacobi_apply(dgc_handle_s* h, const double* r, double* z, cudaStream_t s) {
+int ipdg_block_jacobi_apply(dgc_handle_s* h, const double* r, double* z, cudaStream_t s, bool fp32) {
   if (int rc = ipdg_build_preconditioner(h, s)) return rc;
   const int64_t n = (int64_t)h->K * h->NpP;
-  k_bj_apply<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(h->K, h->Np, h->NpP, h->ipdg->bstr, h->ipdg->binv64, r,
-                                                        z);
+  const unsigned grid = (unsigned)((n + 255) / 256);
+  if (fp32)
+    k_bj_apply<float><<<grid, 256, 0, s>>>(h->K, h->Np, h->NpP, h->ipdg->bstr, h->ipdg->binv32, r, z);
+  else
+    k_bj_apply<double><<<grid, 256, 0, s>>>(h->K, h->Np, h->NpP, h->ipdg->bstr, h->ipdg->binv64, r, z);
   CKI(cudaGetLastError());
   ++h->launches;
   return DGC_OK;

@@ -289,8 +289,9 @@ typedef enum dgc_solve_mode {
   DGC_SOLVE_FP64_PCG = 0, /* block-Jacobi PCG in FP64 */
   DGC_SOLVE_MIXED_IR = 1, /* FP32 block-Jacobi PCG inside FP64 iterative refinement */
   DGC_SOLVE_TWO_LEVEL = 2, /* FP64 PCG with M = Binv + P A_c^-1 P^T, the coarse space of
-                              dgc_coarse_build (which must precede the solve); restarts
-                              from the true residual; no counterpart in the reference */
+                              dgc_coarse_build (which must precede the solve), M applied
+                              with FP32 blocks and smoothing; restarts from the true
+                              residual; no counterpart in the reference */
   DGC_SOLVE_TWO_LEVEL_MIXED = 3 /* the same with S applied in FP32 inside each pass, each
                                    pass to inner_rtol, refined on the FP64 residual */
 } dgc_solve_mode;
