@@ -395,31 +395,39 @@ int ipdg_build_preconditioner(dgc_handle_s* h, cudaStream_t s) {
 
 // z = Binv r elementwise (FP64 vectors, native layout; padding nodes of z set to
 // 0), the blocks and the sums in B's type: FP64 for block-Jacobi PCG, FP32
-// inside the two-level preconditioner (half the bytes; measured at the same
-// time per launch, so the access pattern, not the arithmetic, bounds it)
+// inside the two-level preconditioner.  A CTA holds whole elements (blockDim =
+// E * NpP) and stages r once per node in shared memory, in B's type: read per
+// (node, j) instead, the FP64-to-FP32 conversions ran at GB300's FP64 rate and
+// the FP32 form took as long as the FP64 one.
 template <typename B>
 __global__ void k_bj_apply(int K, int Np, int NpP, int bstr, const B* __restrict__ binv,
                            const double* __restrict__ r, double* __restrict__ z) {
-  const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (g >= (int64_t)K * NpP) return;
-  const int k = (int)(g / NpP), i = (int)(g % NpP);
+  __shared__ B rs[256];
+  const int E = blockDim.x / NpP;
+  const int t = threadIdx.x, e = t / NpP, i = t - e * NpP;
+  const int64_t k = (int64_t)blockIdx.x * E + e;
+  const bool live = k < K;
+  rs[t] = live ? (B)r[k * NpP + i] : (B)0;
+  __syncthreads();
+  if (!live) return;
   B s = 0;
   if (i < Np) {
     const B* Bk = binv + (size_t)k * bstr;
-    const double* rk = r + (size_t)k * NpP;
-    for (int j = 0; j < Np; ++j) s += Bk[j * Np + i] * (B)rk[j];
+    const B* rk = rs + e * NpP;
+    for (int j = 0; j < Np; ++j) s += Bk[j * Np + i] * rk[j];
   }
-  z[g] = (double)s;
+  z[k * NpP + i] = (double)s;
 }
 
 int ipdg_block_jacobi_apply(dgc_handle_s* h, const double* r, double* z, cudaStream_t s, bool fp32) {
   if (int rc = ipdg_build_preconditioner(h, s)) return rc;
-  const int64_t n = (int64_t)h->K * h->NpP;
-  const unsigned grid = (unsigned)((n + 255) / 256);
+  const IpdgState* st = h->ipdg;
+  const int E = 256 / h->NpP;  // whole elements per CTA (NpP <= 48)
+  const unsigned grid = (unsigned)((h->K + E - 1) / E), block = (unsigned)(E * h->NpP);
   if (fp32)
-    k_bj_apply<float><<<grid, 256, 0, s>>>(h->K, h->Np, h->NpP, h->ipdg->bstr, h->ipdg->binv32, r, z);
+    k_bj_apply<float><<<grid, block, 0, s>>>(h->K, h->Np, h->NpP, st->bstr, st->binv32, r, z);
   else
-    k_bj_apply<double><<<grid, 256, 0, s>>>(h->K, h->Np, h->NpP, h->ipdg->bstr, h->ipdg->binv64, r, z);
+    k_bj_apply<double><<<grid, block, 0, s>>>(h->K, h->Np, h->NpP, st->bstr, st->binv64, r, z);
   CKI(cudaGetLastError());
   ++h->launches;
   return DGC_OK;
