@@ -396,9 +396,9 @@ int ipdg_build_preconditioner(dgc_handle_s* h, cudaStream_t s) {
 // z = Binv r elementwise (FP64 vectors, native layout; padding nodes of z set to
 // 0), the blocks and the sums in B's type: FP64 for block-Jacobi PCG, FP32
 // inside the two-level preconditioner.  A CTA holds whole elements (blockDim =
-// E * NpP) and stages r once per node in shared memory, in B's type: read per
-// (node, j) instead, the FP64-to-FP32 conversions ran at GB300's FP64 rate and
-// the FP32 form took as long as the FP64 one.
+// E * NpP) and stages r once per node in shared memory, in B's type: converted
+// per (node, j) instead, the FP32 form took as long as the FP64 one (FP64 work,
+// conversions included, is slow on GB300).
 template <typename B>
 __global__ void k_bj_apply(int K, int Np, int NpP, int bstr, const B* __restrict__ binv,
                            const double* __restrict__ r, double* __restrict__ z) {
