@@ -388,8 +388,9 @@ int dgc_mpnn_set_coarse(dgc_mpnn m, int cells_per_aggregate, void* stream);
  * and shift is a no-op; a failed rebuild leaves the handle without one. */
 int dgc_coarse_build(dgc_handle h, int cells_per_aggregate, void* stream);
 /* z = P A_c^-1 P^T r (device FP64, native layout; z distinct from r).
- * precision DGC_F32 runs the two applies of S inside P and P^T through the
- * FP32 kernels (what the learned preconditioner uses); DGC_F64 is exact. */
+ * precision DGC_F32 runs the two smoothing steps inside P and P^T (S and
+ * Binv) in FP32 (what the two-level and learned preconditioners use);
+ * DGC_F64 is exact. */
 int dgc_coarse_apply(dgc_handle h, const double* r, double* z, int precision, void* stream);
 /* The aggregate of each cell (host array of K), their count, the number of
  * colours used to assemble A_c and omega (any output may be NULL). */
