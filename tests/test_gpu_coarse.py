@@ -53,6 +53,12 @@ def test_coarse_apply_matches_dense(n_side, N, size, shift):
     assert agg.min() == 0 and agg.max() == na - 1 and nc >= 1 and 0.0 < om < 2.0
     if n_side > 6:
         assert nc < na / 4
+    check_dense(D, m, N, shift, 1e-10, 1e-4)
+
+
+def check_dense(D, m, N, shift, tol64, tol32):
+    """D.coarse_apply against P A_c^-1 P^T r formed densely from the oracle's S."""
+    agg, na, _, om = D.coarse_info()
     O = oracle.Oracle(m.xy, m.cells, N)
     n = D.K * D.Np
     S = np.stack([O.spd(e) for e in np.eye(n)], axis=1)
@@ -70,8 +76,18 @@ def test_coarse_apply_matches_dense(n_side, N, size, shift):
     for _ in range(2):
         r = rng.standard_normal(n)
         ref = P @ np.linalg.solve(Ac, P.T @ r)
-        assert relerr(D.download(D.coarse_apply(D.upload(r))), ref) < 1e-10
-        assert relerr(D.download(D.coarse_apply(D.upload(r), precision=dg.F32)), ref) < 1e-4
+        assert relerr(D.download(D.coarse_apply(D.upload(r))), ref) < tol64
+        assert relerr(D.download(D.coarse_apply(D.upload(r), precision=dg.F32)), ref) < tol32
+
+
+@pytest.mark.parametrize("N", [5, 6, 7, 8])
+def test_coarse_apply_high_orders(N):
+    """Orders whose padded element (NpP = 24, 28, 36, 48) gives CTAs of 240-252
+    threads in the block-Jacobi apply."""
+    m = meshes.jittered_square(4, 2)
+    D = dg.Discretization(m, "laplace", N, dg.F64, tau=dg.TAU_SCALED, dirichlet=True)
+    D.coarse_build(4)
+    check_dense(D, m, N, 0.0, 1e-9, 1e-3)
 
 
 @pytest.mark.parametrize("size", [4, 16, 32])
