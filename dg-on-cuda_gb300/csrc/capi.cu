@@ -741,6 +741,11 @@ extern "C" int dgc_set_variant(dgc_handle h, int v) {
   if (!h) return fail(DGC_ERR_ARG, "null handle");
   const int nv = dgc_num_variants(h);
   if (v < 0 || v >= nv) return fail(DGC_ERR_ARG, "variant %d outside [0, %d)", v, nv);
+  if (v != h->rhs_variant && h->graph_exec) {
+    // the cached LSERK4 graph holds the previous variant's kernel
+    cudaGraphExecDestroy(h->graph_exec);
+    h->graph_exec = nullptr;
+  }
   h->rhs_variant = v;
   return h->desc.physics == DGC_LAPLACE ? DGC_OK : refresh_rhs_info(h);
 }
@@ -761,20 +766,21 @@ extern "C" int dgc_autotune(dgc_handle h, int reps, double* times_ms, int* chose
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const size_t bytes = (size_t)h->K * h->Nf * h->NpP * (h->prec == DGC_F64 ? 8 : 4);
   void *qa = nullptr, *qb = nullptr, *res = nullptr;
-  CK(cudaMalloc(&qa, bytes));
-  CK(cudaMalloc(&qb, bytes));
-  CK(cudaMalloc(&res, bytes));
-  CK(cudaMemsetAsync(qa, 0, bytes, s));
-  CK(cudaMemsetAsync(qb, 0, bytes, s));
-  CK(cudaMemsetAsync(res, 0, bytes, s));
-  cudaEvent_t e0, e1;
-  CK(cudaEventCreate(&e0));
-  CK(cudaEventCreate(&e1));
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
   const int keep = h->rhs_variant;
   const int64_t l0 = h->launches;
   int best = 0;
   double best_ms = 1e300;
   int rc = DGC_OK;
+  cudaError_t ce = cudaMalloc(&qa, bytes);
+  if (ce == cudaSuccess) ce = cudaMalloc(&qb, bytes);
+  if (ce == cudaSuccess) ce = cudaMalloc(&res, bytes);
+  if (ce == cudaSuccess) ce = cudaMemsetAsync(qa, 0, bytes, s);
+  if (ce == cudaSuccess) ce = cudaMemsetAsync(qb, 0, bytes, s);
+  if (ce == cudaSuccess) ce = cudaMemsetAsync(res, 0, bytes, s);
+  if (ce == cudaSuccess) ce = cudaEventCreate(&e0);
+  if (ce == cudaSuccess) ce = cudaEventCreate(&e1);
+  if (ce != cudaSuccess) rc = cuda_fail(ce, "autotune scratch set-up");
   for (int v = 0; v < nv && rc == DGC_OK; ++v) {
     h->rhs_variant = v;
     std::vector<float> ms;
@@ -795,16 +801,15 @@ extern "C" int dgc_autotune(dgc_handle h, int reps, double* times_ms, int* chose
       best = v;
     }
   }
+  // one exit path: the scratch and the events are released whatever failed
   h->launches = l0;
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
   cudaFree(qa);
   cudaFree(qb);
   cudaFree(res);
-  if (rc != DGC_OK) {
-    h->rhs_variant = keep;
-    return rc;
-  }
+  h->rhs_variant = keep;
+  if (rc != DGC_OK) return rc;
   cache_store(key, best);
   if (chosen) *chosen = best;
   return dgc_set_variant(h, best);

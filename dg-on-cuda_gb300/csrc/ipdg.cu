@@ -329,6 +329,16 @@ int cuda_err(cudaError_t e, const char* what) {
 
 size_t nvec(const dgc_handle_s* h) { return (size_t)h->K * h->NpP; }
 
+// The chunk graphs capture IpdgParams by value (shift, boundary-type array):
+// every change of those drops them, and the next graphed solve captures anew.
+void drop_chunk_graphs(IpdgState* st) {
+  for (int i = 0; i < 2; ++i) {
+    if (st->chunk[i]) cudaGraphExecDestroy(st->chunk[i]);
+    st->chunk[i] = nullptr;
+    st->chunk_key[i] = nullptr;
+  }
+}
+
 template <typename R>
 dgk::IpdgParams base(const dgc_handle_s* h) {
   dgk::IpdgParams p{};
@@ -886,12 +896,16 @@ extern "C" int dgc_laplace_set_bc_types(dgc_handle h, const uint8_t* flags) {
   IpdgState* st = h->ipdg;
   const size_t nb = (size_t)h->mesh.num_bfaces * h->Nfp;
   if (!flags) {
+    if (st->bcdir) drop_chunk_graphs(st);
     cudaFree(st->bcdir);
     st->bcdir = nullptr;
     return DGC_OK;
   }
   if (nb == 0) return DGC_OK;
-  if (!st->bcdir) CKI(cudaMalloc(&st->bcdir, nb));
+  if (!st->bcdir) {
+    drop_chunk_graphs(st);
+    CKI(cudaMalloc(&st->bcdir, nb));
+  }
   CKI(cudaMemcpy(st->bcdir, flags, nb, cudaMemcpyHostToDevice));
   return DGC_OK;
 }
@@ -944,6 +958,7 @@ extern "C" int dgc_laplace_set_shift(dgc_handle h, double shift) {
   if (st->shift != shift) {
     st->shift = shift;
     st->ready = false;  // the block-Jacobi blocks depend on the shift
+    drop_chunk_graphs(st);
   }
   return DGC_OK;
 }

@@ -46,6 +46,9 @@ extern "C" int dgc_rk4_step_static(dgc_handle h, void* q, double t, double dt, v
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
     return dgc::set_error(DGC_ERR_CUDA, "dgc_rk4_step_static: no usable current device");
+  // the array is looked up per device; a handle's kernels run on its own device
+  if (dev != h->device)
+    return dgc::set_error(DGC_ERR_ARG, "dgc_rk4_step_static: the handle's device is not the current device");
   void* base = nullptr;
   {
     // one-time set-up per device, with that device current: the host-side name

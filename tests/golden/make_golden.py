@@ -123,7 +123,9 @@ def main() -> None:
     only = sys.argv[sys.argv.index("--only") + 1] if "--only" in sys.argv else None
     if only:
         args = [a for a in args if a != only]
-    ref = args[0] if args else "/root/reference"
+    ref = args[0] if args else os.environ.get("DGC_REFERENCE_DIR", "")
+    if not ref:
+        sys.exit("make_golden.py: name the reference checkout (first argument or DGC_REFERENCE_DIR)")
     oracle_dir = os.path.join(ROOT, "oracle")
     subprocess.run(["make", "-s", "-C", oracle_dir, "ref", f"REF={ref}"], check=True)
     if only == "stokes":

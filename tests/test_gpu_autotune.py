@@ -86,3 +86,25 @@ def test_variants_repeatable_at_scale(prec):
             D.rhs(q, 0.1, out=out)
             assert torch.equal(out, ref), v
         D.check()
+
+
+def test_graphed_run_follows_variant_change():
+    """A graphed dgc_lserk4_run, a variant change, and a second graphed run on
+    the same buffers and dt: the second run replays the new variant (bitwise
+    equal to its launch-by-launch run), not the graph of the first."""
+    m = meshes.jittered_square(16, 7)
+    D = dg.Discretization(m, "maxwell_te", 5, dg.F32)
+    o = oracle.Oracle(m.xy, m.cells, 5)
+    q0 = o.exact(oracle.problem(oracle.MAXWELL_TE, 1.0, 1.0, 0), 0.0)
+    dt = 0.3 * D.info.min_edge / 36.0
+    qa, qb, res = D.empty_state(), D.empty_state(), D.empty_state()
+    out = {}
+    for v in (0, 5, 0):
+        D.set_variant(v)
+        for graph in (True, False):
+            qa.copy_(D.upload(q0))
+            res.zero_()
+            fin = D.lserk4_run(qa, qb, res, 0.0, dt, 20, graph=graph)
+            out[(v, graph)] = fin.clone()
+        assert torch.equal(out[(v, True)], out[(v, False)]), v
+    D.check()

@@ -248,6 +248,24 @@ def test_shifted_spd_form_and_helmholtz_solve():
     assert relerr(D.spd(u).cpu().numpy(), s0) < 1e-15
 
 
+def test_graphed_solve_after_shift_change_uses_new_operator():
+    # the CG chunk graph captures the shift by value: a graphed solve, a new
+    # shift, and a second graphed solve must solve the second system
+    m = meshes.jittered_square(4, 14)
+    D = dg.Discretization(m, "laplace", 3, dg.F64, tau=dg.TAU_SCALED, dirichlet=True)
+    u = torch.from_numpy(np.random.default_rng(3).standard_normal(D.state_len)).cuda()
+    b = D.mass(u)
+    for gamma in (0.0, 250.0, 11.0):
+        D.set_shift(gamma)
+        S, idx = dense_spd(D)
+        xd = np.linalg.solve(S, b.cpu().numpy()[idx])
+        for mode, tol in ((dg.SOLVE_FP64_PCG, 1e-9), (dg.SOLVE_MIXED_IR, 1e-8)):
+            x, st = D.pcg(b, mode=mode, rtol=1e-12 if mode == dg.SOLVE_FP64_PCG else 1e-11, graph=True)
+            assert st["converged"], (gamma, mode)
+            assert relerr(x.cpu().numpy()[idx], xd) < tol, (gamma, mode)
+    D.set_shift(0.0)
+
+
 def test_all_neumann_pcg_solves_the_consistent_system():
     m = meshes.jittered_square(4, 13)
     D = dg.Discretization(m, "laplace", 2, dg.F64, tau=dg.TAU_SCALED, dirichlet=False)
