@@ -469,10 +469,13 @@ BATCH_INSTANCES, BATCH_SEED, BATCH_STEPS = 96, 777, 10
 def measure_batched(dg, meshes):
     """96 independent FP32 instances (advection with a random velocity direction
     and Gaussian pulse, or a Maxwell TE / TM cavity mode) on jittered meshes with
-    n log-uniform in [8, 160] squares per side and N uniform in {2..8}: aggregate
-    GDOF/s of the batched persistent launches (one launch per LSERK4 stage for
-    all instances, the step replayed from a CUDA graph) against the same steps
-    as per-instance sequential launches of the same tile code."""
+    n log-uniform in [8, 160] squares per side and N uniform in {2..8}.  Every
+    instance is autotuned first.  Batched: one persistent launch per LSERK4
+    stage for all instances, the step replayed from a CUDA graph, each instance
+    on the faster of the two tile codes the batch offers (variant 0 or the
+    register-blocked variant, by its autotune times).  Sequential: instance
+    after instance, each with its own autotuned variant, its steps replayed
+    from its own CUDA graph.  Aggregate GDOF/s of both."""
     import torch
     rng = np.random.default_rng(BATCH_SEED)
     insts = []
@@ -495,12 +498,16 @@ def measure_batched(dg, meshes):
             # TE: Hz = cos cos; TM: Ez = sin sin (both PEC cavity modes)
             q[2] = (np.cos(np.pi * x) * np.cos(np.pi * y) if kind == "maxwell_te"
                     else np.sin(np.pi * x) * np.sin(np.pi * y))
-        D.set_variant(0)
-        insts.append((D, q.reshape(-1), 0.5 * D.info.min_edge / (N + 1) ** 2))
-    dofs = sum(D.Nf * D.Np * D.K for D, _, _ in insts)
-    B = dg.Batch([D for D, _, _ in insts])
-    dts = [dt for *_, dt in insts]
-    qa = [D.upload(q) for D, q, _ in insts]
+        tuned, times = D.autotune(reps=5)
+        blk = 5 if N <= 6 else 1
+        batch_v = blk if times[blk] < times[0] else 0
+        insts.append((D, q.reshape(-1), 0.5 * D.info.min_edge / (N + 1) ** 2, tuned, batch_v))
+    dofs = sum(D.Nf * D.Np * D.K for D, *_ in insts)
+    for D, _, _, _, bv in insts:
+        D.set_variant(bv)
+    B = dg.Batch([D for D, *_ in insts])
+    dts = [it[2] for it in insts]
+    qa = [D.upload(q) for D, q, *_ in insts]
     qb = [D.empty_state() for D, *_ in insts]
     rs = [D.empty_state() for D, *_ in insts]
     B.lserk4_run(qa, qb, rs, [0.0] * len(insts), dts, 4, graph=True)  # warm-up (even: back in qa)
@@ -513,37 +520,47 @@ def measure_batched(dg, meshes):
     torch.cuda.synchronize()
     batched_ms = ev0.elapsed_time(ev1)
     batch_launches = B.launch_count() - l0
-    # sequential: the same steps, instance after instance, 5 launches per step each
-    sa = [D.upload(q) for D, q, _ in insts]
+    B.close()
+    # sequential: the same steps, instance after instance, each with its autotuned variant
+    for D, _, _, tv, _ in insts:
+        D.set_variant(tv)
+    sa = [D.upload(q) for D, q, *_ in insts]
     sb = [D.empty_state() for D, *_ in insts]
     sr = [D.empty_state() for D, *_ in insts]
     for (D, *_), a, b, r, dt in zip(insts, sa, sb, sr, dts):
-        for s in range(4):
-            D.lserk4_step(a if s % 2 == 0 else b, b if s % 2 == 0 else a, r, s * dt, dt)
+        D.lserk4_run(a, b, r, 0.0, dt, 4, graph=True)                  # warm-up, graph capture
+    sa = [D.upload(q) for D, q, *_ in insts]
+    sr = [D.empty_state() for D, *_ in insts]
     torch.cuda.synchronize()
+    seq_fin = []
     ev0.record()
     for (D, *_), a, b, r, dt in zip(insts, sa, sb, sr, dts):
-        x, y = a, b
-        for s in range(BATCH_STEPS):
-            D.lserk4_step(x, y, r, s * dt, dt)
-            x, y = y, x
+        seq_fin.append(D.lserk4_run(a, b, r, 0.0, dt, BATCH_STEPS, graph=True))
     ev1.record()
     torch.cuda.synchronize()
     seq_ms = ev0.elapsed_time(ev1)
-    seq_fin = sb if BATCH_STEPS % 2 else sa
+    # instances whose batch tile code is their tuned variant must agree bit for bit
+    same = [i for i, it in enumerate(insts) if it[3] == it[4]]
+    bitwise = all(torch.equal(fin[i], seq_fin[i]) for i in same)
     diff = max(float((f - g).abs().max()) / max(float(g.abs().max()), 1e-30) for f, g in zip(fin, seq_fin))
-    B.close()
     for D, *_ in insts:
         D.check()
     Ks = [D.K for D, *_ in insts]
+    codes = [it[4] for it in insts]
     return {"workload": f"batched_{len(insts)}_instances", "instances": len(insts),
             "dofs_total": dofs, "K_range": [min(Ks), max(Ks)],
             "orders": sorted({D.N for D, *_ in insts}), "steps": BATCH_STEPS,
+            "geometry": "fp32 records rounded from fp64 set-up (rounding measured without effect on the "
+                        "error floor)",
             "batched": {"gdofs": dofs * 5 * BATCH_STEPS / (batched_ms * 1e-3) / 1e9, "ms": batched_ms,
-                        "launches_per_step": batch_launches / BATCH_STEPS, "graph": True},
+                        "launches_per_step": batch_launches / BATCH_STEPS, "graph": True,
+                        "instances_on_blocked_tiles": sum(1 for c in codes if c != 0)},
             "sequential": {"gdofs": dofs * 5 * BATCH_STEPS / (seq_ms * 1e-3) / 1e9, "ms": seq_ms,
-                           "launches_per_step": 5 * len(insts)},
+                           "launches_per_step": 5 * len(insts), "graph": True,
+                           "variants": {str(v): sum(1 for it in insts if it[3] == v)
+                                        for v in sorted({it[3] for it in insts})}},
             "speedup_batched_vs_sequential": seq_ms / batched_ms,
+            "bitwise_equal_where_same_tile_code": bitwise, "instances_same_tile_code": len(same),
             "max_rel_diff_batched_vs_sequential": diff}
 
 
@@ -648,6 +665,82 @@ def measure_accuracy(dg, D32, D64, q_init, x, y, dt):
             "fp32_run_s": t32, "fp64_run_s": t64}
 
 
+EQ_MESHES = (16, 32, 64, 128)
+EQ_ORDERS = (2, 3, 4, 5, 6)
+EQ_TARGETS = (1e-4, 1e-5, 1e-6, 1e-7)
+
+
+def measure_equal_error(dg, meshes):
+    """Accuracy against time for the TE cavity to T = 1: every (mesh, order) of
+    EQ_MESHES x EQ_ORDERS in FP64, FP32 and compensated FP32 (FP32 arithmetic,
+    hi + lo state), graph-replayed LSERK4 with dt = 0.5 min(edge) / (N+1)^2,
+    device time of the whole run (CUDA events), relative L2 error against the
+    exact mode.  Two comparisons at equal error:
+      * per configuration: where a mixed path's error equals FP64's (within 5 %),
+        the ratio of their GDOF/s on that configuration;
+      * per target error E: the fastest configuration of each precision whose
+        error is <= E, and the ratio of their times to solution."""
+    import torch
+    stream = torch.cuda.current_stream()
+    rows = []
+    for n in EQ_MESHES:
+        m = meshes.jittered_square(n, SEED)
+        for N in EQ_ORDERS:
+            row = {"n": n, "num_cells": 2 * n * n, "order": N}
+            for tag, prec in (("fp64", dg.F64), ("fp32", dg.F32), ("fp32c", dg.F32C)):
+                D = dg.Discretization(m, "maxwell_te", N, prec)
+                if prec == dg.F32:
+                    D.autotune(reps=5)
+                x, y = D.node_xy()
+                dt0 = 0.5 * D.info.min_edge / (N + 1) ** 2
+                ns = int(np.ceil(1.0 / dt0))
+                qa, qb, res = D.upload(te_initial(x, y)), D.empty_state(), D.empty_state()
+                D.lserk4_run(qa, qb, res, 0.0, 1.0 / ns, 20, graph=True)     # warm-up, graph capture
+                qa, res = D.upload(te_initial(x, y)), D.empty_state()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                fin = D.lserk4_run(qa, qb, res, 0.0, 1.0 / ns, ns, graph=True)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                ms = e0.elapsed_time(e1)
+                D.check()
+                ex = te_exact(x, y, 1.0).reshape(-1)
+                err = float(np.linalg.norm(D.download(fin) - ex) / np.linalg.norm(ex))
+                row["steps"] = ns
+                row[tag] = {"rel_l2": err, "ms_to_t1": ms,
+                            "gdofs": 3 * D.Np * D.K * 5 * ns / (ms * 1e-3) / 1e9}
+                del D, qa, qb, res, fin
+            rows.append(row)
+    same = []
+    for r in rows:
+        for tag in ("fp32", "fp32c"):
+            if abs(r[tag]["rel_l2"] - r["fp64"]["rel_l2"]) <= 0.05 * r["fp64"]["rel_l2"]:
+                same.append({"n": r["n"], "order": r["order"], "precision": tag, "rel_l2": r[tag]["rel_l2"],
+                             "gdofs": r[tag]["gdofs"], "fp64_gdofs": r["fp64"]["gdofs"],
+                             "speedup": r[tag]["gdofs"] / r["fp64"]["gdofs"]})
+    best = {}
+    for tag in ("fp64", "fp32", "fp32c"):
+        floor = min(r[tag]["rel_l2"] for r in rows)
+        best[tag + "_min_error"] = floor
+    targets = list(EQ_TARGETS) + [best["fp32c_min_error"] * 1.05]
+    frontier = []
+    for E in targets:
+        ent = {"target_rel_l2": E}
+        for tag in ("fp64", "fp32", "fp32c"):
+            ok = [r for r in rows if r[tag]["rel_l2"] <= E]
+            if ok:
+                b = min(ok, key=lambda r: r[tag]["ms_to_t1"])
+                ent[tag] = {"n": b["n"], "order": b["order"], "ms_to_t1": b[tag]["ms_to_t1"],
+                            "rel_l2": b[tag]["rel_l2"]}
+        for tag in ("fp32", "fp32c"):
+            if tag in ent and "fp64" in ent:
+                ent["speedup_" + tag] = ent["fp64"]["ms_to_t1"] / ent[tag]["ms_to_t1"]
+        frontier.append(ent)
+    return {"workload": "maxwell_te_pec_cavity to T=1, jittered n x n meshes, LSERK4",
+            "meshes": list(EQ_MESHES), "orders": list(EQ_ORDERS), "rows": rows,
+            "same_error_configs": same, "min_error": best, "time_to_error": frontier}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -663,6 +756,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-instances comparison")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-preconditioner comparison")
     ap.add_argument("--no-stokes", action="store_true", help="skip the Stokes dual-splitting timing")
+    ap.add_argument("--no-equal-error", action="store_true", help="skip the accuracy-against-time sweep")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -778,6 +872,9 @@ def main():
     stokes = None
     if rank == 0 and not args.no_stokes:
         stokes = measure_stokes(dg, meshes)
+    equal_error = None
+    if rank == 0 and not args.no_equal_error:
+        equal_error = measure_equal_error(dg, meshes)
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         csteps = 10
@@ -794,7 +891,7 @@ def main():
                 "clocks": clocks, "fp64_plain": fp64,
                 "speedup_mixed_vs_fp64": (value / ws / fp64["value"]) if fp64 else None,
                 "accuracy": accuracy, "poisson": poisson, "batched": batched, "learned_precond": learned,
-                "stokes": stokes, "wall_s_timed_region": wall}
+                "stokes": stokes, "equal_error": equal_error, "wall_s_timed_region": wall}
         print(json.dumps(line))
     if ws > 1:
         import torch.distributed as tdist

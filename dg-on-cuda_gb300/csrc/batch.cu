@@ -8,8 +8,17 @@
 // weighted by Np for the O(Np^2) contractions) so that the longest items start
 // first.  A launch zeroes the queue head; every CTA takes items with one
 // atomicAdd per item, loads that instance's operator matrices into shared
-// memory and runs the tiles with the tile code of dg_rhs_kernel
-// (rhs_v1_load_mats / rhs_v1_tile), dispatching on (order, physics).
+// memory and runs the tiles, dispatching on (order, physics, tile code):
+//   code 0: the tile code of dg_rhs_kernel (rhs_v1_load_mats / rhs_v1_tile,
+//           the handle's variant 0);
+//   code 1: the register-blocked tiles of dg_rhs_blk_kernel with one element
+//           per thread slot (blk_tiles, variant 5 at orders 1..6 and 1 at
+//           orders 7, 8), double-buffered within each work item.
+// An instance runs code 1 when its handle is set to that variant (e.g. by
+// dgc_autotune) and code 0 otherwise, so a batched step is bitwise equal to
+// the handle's own dgc_lserk4_step with either of those two variants.  The
+// launch's dynamic shared memory is the largest layout among the batch's
+// instances, which sets the resident CTAs per SM.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -24,7 +33,7 @@ namespace dgk {
 
 struct BatchLaunch {
   const RhsParams* params;  // [instances] parameters of this stage
-  const int* kinds;         // [instances] (N - 1) * 3 + physics
+  const int* kinds;         // [instances] ((N - 1) * 3 + physics) * 2 + tile code
   const int4* items;        // [items] {instance, first tile, tiles, 0}
   int nitems;
   unsigned int* head;       // work-queue head, zero at launch
@@ -43,12 +52,33 @@ __device__ __forceinline__ bool batch_item(const RhsParams& p, unsigned char* sm
   return true;
 }
 
-// largest dynamic shared memory of the FP32 tile layouts, orders 1..8
+// One work item with either tile code.  Not inlined: each (order, physics,
+// code) body gets its own register allocation instead of the union of all of
+// them in one kernel body.
+template <int N, int P>
+__device__ __noinline__ bool batch_item_v0(const RhsParams& p, unsigned char* smem, uint32_t* ph, int tile0,
+                                           int ntile) {
+  return batch_item<N, P>(p, smem, ph[0], tile0, ntile);
+}
+template <int N, int P>
+__device__ __noinline__ bool batch_item_blk(const RhsParams& p, unsigned char* smem, uint32_t* ph, int tile0,
+                                            int ntile) {
+  uint32_t loc[3] = {ph[0], ph[1], ph[2]};
+  const bool ok = blk_tiles<N, P, 1, 0>(p, smem, loc, tile0, 1, tile0 + ntile);
+  ph[0] = loc[0];
+  ph[1] = loc[1];
+  ph[2] = loc[2];
+  return ok;
+}
+
+// largest dynamic shared memory of the FP32 tile layouts (both codes), orders 1..8
+constexpr uint32_t umax(uint32_t a, uint32_t b) { return a > b ? a : b; }
 template <int N>
 constexpr uint32_t batch_smem_upto() {
-  constexpr uint32_t a = RhsConfig<float, N, PHYS_ADV>::kSmem, b = RhsConfig<float, N, PHYS_TM>::kSmem,
-                     c = RhsConfig<float, N, PHYS_TE>::kSmem;
-  constexpr uint32_t m = a > b ? (a > c ? a : c) : (b > c ? b : c);
+  constexpr uint32_t a = umax(RhsConfig<float, N, PHYS_ADV>::kSmem, BlkConfig<N, PHYS_ADV, 1, 0>::kSmem),
+                     b = umax(RhsConfig<float, N, PHYS_TM>::kSmem, BlkConfig<N, PHYS_TM, 1, 0>::kSmem),
+                     c = umax(RhsConfig<float, N, PHYS_TE>::kSmem, BlkConfig<N, PHYS_TE, 1, 0>::kSmem);
+  constexpr uint32_t m = umax(a, umax(b, c));
   if constexpr (N == 1) {
     return m;
   } else {
@@ -58,16 +88,20 @@ constexpr uint32_t batch_smem_upto() {
 }
 constexpr uint32_t kBatchSmem = batch_smem_upto<8>();
 
-__global__ void __launch_bounds__(256) dg_batch_kernel(const BatchLaunch b) {
+__global__ void __launch_bounds__(256, 3) dg_batch_kernel(const BatchLaunch b) {
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ int s_item;
-  uint64_t* bar = reinterpret_cast<uint64_t*>(smem);  // offset 0 in every RhsConfig layout
+  // offset 0 of both tile layouts: barrier 0 (tiles of code 0, buffer 0 of
+  // code 1), 1 (buffer 1 of code 1), 2 (operators of code 1)
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
   if (threadIdx.x == 0) {
-    mbar_init(bar, 1);
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    mbar_init(&bar[2], 1);
     fence_barrier_init();
   }
   __syncthreads();
-  uint32_t phase = 0;
+  uint32_t ph[3] = {0, 0, 0};
   for (;;) {
     if (threadIdx.x == 0) s_item = (int)atomicAdd(b.head, 1u);
     __syncthreads();
@@ -78,13 +112,14 @@ __global__ void __launch_bounds__(256) dg_batch_kernel(const BatchLaunch b) {
     const RhsParams& p = b.params[w.x];
     bool ok = false;
     switch (b.kinds[w.x]) {
-#define DGK_BATCH_CASE(n)                                                              \
-  case (n - 1) * 3 + PHYS_ADV: ok = batch_item<n, PHYS_ADV>(p, smem, phase, w.y, w.z); break; \
-  case (n - 1) * 3 + PHYS_TM: ok = batch_item<n, PHYS_TM>(p, smem, phase, w.y, w.z); break;   \
-  case (n - 1) * 3 + PHYS_TE: ok = batch_item<n, PHYS_TE>(p, smem, phase, w.y, w.z); break;
+#define DGK_BATCH_PHYS(n, P)                                                                   \
+  case ((n - 1) * 3 + P) * 2: ok = batch_item_v0<n, P>(p, smem, ph, w.y, w.z); break;         \
+  case ((n - 1) * 3 + P) * 2 + 1: ok = batch_item_blk<n, P>(p, smem, ph, w.y, w.z); break;
+#define DGK_BATCH_CASE(n) DGK_BATCH_PHYS(n, PHYS_ADV) DGK_BATCH_PHYS(n, PHYS_TM) DGK_BATCH_PHYS(n, PHYS_TE)
       DGK_BATCH_CASE(1) DGK_BATCH_CASE(2) DGK_BATCH_CASE(3) DGK_BATCH_CASE(4)
       DGK_BATCH_CASE(5) DGK_BATCH_CASE(6) DGK_BATCH_CASE(7) DGK_BATCH_CASE(8)
 #undef DGK_BATCH_CASE
+#undef DGK_BATCH_PHYS
       default: ok = false;
     }
     if (!ok) break;  // uniform: every wait ends in a CTA-wide AND
@@ -102,6 +137,7 @@ __global__ void k_batch_clock(int n, double* const* t, const double* dt) {
 struct dgc_batch_s {
   std::vector<dgc_handle> inst;
   int device = 0, sm_count = 0, blocks_per_sm = 1;
+  int smem = 0;                     // dynamic shared memory of a launch (largest instance layout)
   std::vector<int> tile_size;       // per instance
   int nitems = 0;
   int* d_kinds = nullptr;
@@ -136,13 +172,14 @@ int physics_kind(int phys) {
   return phys == DGC_ADVECTION ? dgk::PHYS_ADV : (phys == DGC_MAXWELL_TM ? dgk::PHYS_TM : dgk::PHYS_TE);
 }
 
-int tile_size(int N, int P) {
-  dgk::LaunchInfo li;
+// the FP32 variant that runs the register-blocked tiles with one element per
+// thread slot (batch tile code 1)
+int blk_variant(int N) { return N <= 6 ? 5 : 1; }
+
+// tile size and shared memory of an (order, physics, variant) stage kernel
+bool tile_info(int N, int phys, int variant, dgk::LaunchInfo* li) {
   dgk::RhsParams dummy{};
-  const int phys = P == dgk::PHYS_ADV ? DGC_ADVECTION : (P == dgk::PHYS_TM ? DGC_MAXWELL_TM : DGC_MAXWELL_TE);
-  // the variant-0 tile of this (order, physics): dg_rhs_kernel's RhsConfig
-  if (dgk::rhs_dispatch<float>(N, phys, 0, dummy, 1, 0, &li) != cudaSuccess) return 0;
-  return li.tile;
+  return dgk::rhs_dispatch<float>(N, phys, variant, dummy, 1, 0, li) == cudaSuccess;
 }
 
 // parameters of one LSERK stage for every instance, into b->h_params[stage]
@@ -178,7 +215,7 @@ int launch_step(dgc_batch b, cudaStream_t s) {
   CKB(cudaMemsetAsync(b->d_head, 0, 5 * sizeof(unsigned int), s));
   for (int st = 0; st < 5; ++st) {
     dgk::BatchLaunch L{b->d_params + (size_t)st * n, b->d_kinds, b->d_items, b->nitems, b->d_head + st};
-    dgk::dg_batch_kernel<<<grid, 256, dgk::kBatchSmem, s>>>(L);
+    dgk::dg_batch_kernel<<<grid, 256, b->smem, s>>>(L);
     CKB(cudaGetLastError());
     ++b->launches;
   }
@@ -217,9 +254,13 @@ extern "C" int dgc_batch_create(const dgc_handle* handles, int n, dgc_batch* out
     if (h->prec != DGC_F32) return fail(berr(DGC_ERR_UNSUPPORTED, "batches run FP32 handles"));
     if (h->desc.physics == DGC_LAPLACE) return fail(berr(DGC_ERR_UNSUPPORTED, "batches run time-dependent handles"));
     const int P = physics_kind(h->desc.physics);
-    kinds[i] = (h->N - 1) * 3 + P;
-    const int te = tile_size(h->N, P);
-    if (te <= 0) return fail(berr(DGC_ERR_CUDA, "configure batch tile"));
+    const int code = h->rhs_variant == blk_variant(h->N) ? 1 : 0;
+    kinds[i] = ((h->N - 1) * 3 + P) * 2 + code;
+    dgk::LaunchInfo li;
+    if (!tile_info(h->N, h->desc.physics, code ? blk_variant(h->N) : 0, &li) || li.tile <= 0)
+      return fail(berr(DGC_ERR_CUDA, "configure batch tile"));
+    const int te = li.tile;
+    b->smem = std::max(b->smem, li.smem);
     b->tile_size.push_back(te);
     const int ntiles = (h->K + te - 1) / te;
     for (int t0 = 0; t0 < ntiles; t0 += kChunk) {
@@ -237,7 +278,7 @@ extern "C" int dgc_batch_create(const dgc_handle* handles, int n, dgc_batch* out
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(dgk::dg_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, dgk::kBatchSmem);
   if (e == cudaSuccess)
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b->blocks_per_sm, dgk::dg_batch_kernel, 256, dgk::kBatchSmem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b->blocks_per_sm, dgk::dg_batch_kernel, 256, b->smem);
   if (e == cudaSuccess) e = cudaMalloc(&b->d_kinds, n * sizeof(int));
   if (e == cudaSuccess) e = cudaMemcpy(b->d_kinds, kinds.data(), n * sizeof(int), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMalloc(&b->d_items, hitems.size() * sizeof(int4));

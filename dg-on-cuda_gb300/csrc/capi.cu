@@ -76,6 +76,37 @@ __global__ void k_layout(int K, int Nf, int Np, int NpP, int layout, int to_nati
   }
 }
 
+// the same for DGC_F32C states: FP64 reference arrays <-> native [hi | lo]
+// pairs (hi = the FP32 rounding of the value, lo = the FP32 rounding of the
+// rest)
+__global__ void k_layout_x2(int K, int Nf, int Np, int NpP, int layout, int to_native, const void* src_v,
+                            void* dst_v) {
+  const size_t n = (size_t)K * Nf * NpP;
+  for (size_t idx = blockIdx.x * (size_t)blockDim.x + threadIdx.x; idx < n; idx += (size_t)gridDim.x * blockDim.x) {
+    const int j = (int)(idx % NpP);
+    const size_t kf = idx / NpP;
+    const int f = (int)(kf % Nf);
+    const size_t k = kf / Nf;
+    if (j >= Np) {
+      if (to_native) {
+        static_cast<float*>(dst_v)[idx] = 0.0f;
+        static_cast<float*>(dst_v)[n + idx] = 0.0f;
+      }
+      continue;
+    }
+    const size_t r = layout == DGC_LAYOUT_REF_CPU ? ((size_t)f * K + k) * Np + j : ((size_t)f * Np + j) * K + k;
+    if (to_native) {
+      const double v = static_cast<const double*>(src_v)[r];
+      const float hi = __double2float_rn(v);
+      static_cast<float*>(dst_v)[idx] = hi;
+      static_cast<float*>(dst_v)[n + idx] = __double2float_rn(v - (double)hi);
+    } else {
+      const float* q = static_cast<const float*>(src_v);
+      static_cast<double*>(dst_v)[r] = (double)q[idx] + (double)q[n + idx];
+    }
+  }
+}
+
 __global__ void k_clock(double* t, double dt) { t[0] += dt; }
 
 template <typename R>
@@ -129,6 +160,21 @@ int upload_operators(dgc_handle_s* h, int form) {
     if (!h->d_blk_b) CK(cudaMalloc(&h->d_blk_b, bk.size() * sizeof(float)));
     CK(cudaMemcpy(h->d_blk_b, bk.data(), bk.size() * sizeof(float), cudaMemcpyHostToDevice));
   }
+  if (form == 1) {
+    // compensated-state kernel operand: rows j of the strong-form Dr^T, Ds^T
+    // and m of LIFT^T, each padded with zeros to NpP columns
+    const int Np = re.Np, NF = 3 * re.Nfp, NpP = dgc::padded_nodes(re.N);
+    std::vector<float> bk((size_t)(2 * Np + NF) * NpP, 0.0f);
+    for (int j = 0; j < Np; ++j)
+      for (int i = 0; i < Np; ++i) {
+        bk[(size_t)j * NpP + i] = (float)Dr[(size_t)i * Np + j];
+        bk[(size_t)(Np + j) * NpP + i] = (float)Ds[(size_t)i * Np + j];
+      }
+    for (int m = 0; m < NF; ++m)
+      for (int i = 0; i < Np; ++i) bk[(size_t)(2 * Np + m) * NpP + i] = (float)L[(size_t)i * NF + m];
+    if (!h->d_blk_bs) CK(cudaMalloc(&h->d_blk_bs, bk.size() * sizeof(float)));
+    CK(cudaMemcpy(h->d_blk_bs, bk.data(), bk.size() * sizeof(float), cudaMemcpyHostToDevice));
+  }
   if (form == 1 && re.N <= 6) {
     // tensor-core operand (the FP32 tcgen05 kernel evaluates the strong form):
     // row n = output node, K = [Dr(n,:) pad | Ds(n,:) pad | LIFT(n,:)] with the
@@ -169,34 +215,27 @@ int upload_operators(dgc_handle_s* h, int form) {
 
 extern "C" const char* dgc_last_error(void) { return g_err.c_str(); }
 
-extern "C" int dgc_create(int nv, const double* vxy, int K, const int32_t* cells, const dgc_problem_desc* desc,
-                          dgc_handle* out) {
-  if (!out || !desc) return fail(DGC_ERR_ARG, "null argument");
-  *out = nullptr;
+namespace {
+
+int check_desc(const dgc_problem_desc* desc) {
   if (desc->physics < DGC_ADVECTION || desc->physics > DGC_LAPLACE)
     return fail(DGC_ERR_ARG, "unknown physics %d", desc->physics);
-  if (desc->precision != DGC_F64 && desc->precision != DGC_F32)
+  if (desc->precision != DGC_F64 && desc->precision != DGC_F32 && desc->precision != DGC_F32C)
     return fail(DGC_ERR_ARG, "unknown precision %d", desc->precision);
+  if (desc->precision == DGC_F32C && desc->physics == DGC_LAPLACE)
+    return fail(DGC_ERR_UNSUPPORTED, "the compensated FP32 state is offered for advection and Maxwell handles");
   if (desc->order < 1 || desc->order > dgc::kMaxOrder)
     return fail(DGC_ERR_ARG, "order %d outside [1, %d]", desc->order, dgc::kMaxOrder);
   if (desc->physics == DGC_ADVECTION && (desc->bc < DGC_BC_SINSIN || desc->bc > DGC_BC_ZERO))
     return fail(DGC_ERR_ARG, "unknown advection boundary kind %d", desc->bc);
   if (desc->physics == DGC_ADVECTION && desc->bc == DGC_BC_GAUSS && !(desc->gw > 0.0))
     return fail(DGC_ERR_ARG, "gaussian width must be positive");
-  auto* h = new dgc_handle_s();
-  h->desc = *desc;
-  std::string err;
-  if (!dgc::build_ref_element(desc->order, h->re, err)) {
-    delete h;
-    return fail(DGC_ERR_ARG, "%s", err.c_str());
-  }
-  // half-edge matching on the GPU from 16384 cells (DGC_GPU_TOPOLOGY_MIN overrides)
-  int64_t gpu_topo_min = 16384;
-  if (const char* e = std::getenv("DGC_GPU_TOPOLOGY_MIN")) gpu_topo_min = std::atoll(e);
-  if (!dgc::build_mesh(vxy, nv, cells, K, h->re, h->mesh, err, (int64_t)K >= gpu_topo_min)) {
-    delete h;
-    return fail(DGC_ERR_MESH, "%s", err.c_str());
-  }
+  return DGC_OK;
+}
+
+// the device side of a handle whose reference element and mesh are built
+int finish_create(dgc_handle_s* h, int K, dgc_handle* out) {
+  const dgc_problem_desc* desc = &h->desc;
   h->K = K;
   h->N = desc->order;
   h->Np = h->re.Np;
@@ -214,7 +253,63 @@ extern "C" int dgc_create(int nv, const double* vxy, int K, const int32_t* cells
   return DGC_OK;
 }
 
+}  // namespace
+
+extern "C" int dgc_create(int nv, const double* vxy, int K, const int32_t* cells, const dgc_problem_desc* desc,
+                          dgc_handle* out) {
+  if (!out || !desc) return fail(DGC_ERR_ARG, "null argument");
+  *out = nullptr;
+  if (int rc = check_desc(desc)) return rc;
+  auto* h = new dgc_handle_s();
+  h->desc = *desc;
+  std::string err;
+  if (!dgc::build_ref_element(desc->order, h->re, err)) {
+    delete h;
+    return fail(DGC_ERR_ARG, "%s", err.c_str());
+  }
+  // half-edge matching on the GPU from 16384 cells (DGC_GPU_TOPOLOGY_MIN overrides)
+  int64_t gpu_topo_min = 16384;
+  if (const char* e = std::getenv("DGC_GPU_TOPOLOGY_MIN")) gpu_topo_min = std::atoll(e);
+  if (!dgc::build_mesh(vxy, nv, cells, K, h->re, h->mesh, err, (int64_t)K >= gpu_topo_min)) {
+    delete h;
+    return fail(DGC_ERR_MESH, "%s", err.c_str());
+  }
+  return finish_create(h, K, out);
+}
+
+extern "C" int dgc_create_from_arrays(int K, const double* invJ, const double* J, const double* faceJ,
+                                      const int32_t* nb_cell, const int32_t* nb_face, int num_boundary_nodes,
+                                      const double* bx, const double* by, const double* nx, const double* ny,
+                                      const dgc_problem_desc* desc, dgc_handle* out) {
+  if (!out || !desc || !invJ || !J || !faceJ || !nb_cell || !nb_face || !nx || !ny ||
+      (num_boundary_nodes > 0 && (!bx || !by)))
+    return fail(DGC_ERR_ARG, "null argument");
+  *out = nullptr;
+  if (int rc = check_desc(desc)) return rc;
+  auto* h = new dgc_handle_s();
+  h->desc = *desc;
+  std::string err;
+  if (!dgc::build_ref_element(desc->order, h->re, err)) {
+    delete h;
+    return fail(DGC_ERR_ARG, "%s", err.c_str());
+  }
+  if (!dgc::build_mesh_from_arrays(K, h->re, invJ, J, faceJ, nb_cell, nb_face, num_boundary_nodes, bx, by, nx, ny,
+                                   h->mesh, err)) {
+    delete h;
+    return fail(DGC_ERR_MESH, "%s", err.c_str());
+  }
+  return finish_create(h, K, out);
+}
+
 namespace dgc {
+
+// the stage kernel of the handle's precision and variant: launch (info NULL)
+// or describe it
+cudaError_t rhs_dispatch_any(const dgc_handle_s* h, const dgk::RhsParams& p, cudaStream_t s, dgk::LaunchInfo* info) {
+  if (h->prec == DGC_F64) return dgk::rhs_dispatch<double>(h->N, h->desc.physics, h->rhs_variant, p, h->sm_count, s, info);
+  if (h->prec == DGC_F32C) return dgk::rhs_x2_dispatch(h->N, h->desc.physics, p, h->sm_count, s, info);
+  return dgk::rhs_dispatch<float>(h->N, h->desc.physics, h->rhs_variant, p, h->sm_count, s, info);
+}
 
 int device_init(dgc_handle_s* h) {
   CK(cudaGetDevice(&h->device));
@@ -250,11 +345,7 @@ int device_init(dgc_handle_s* h) {
   if (rc != DGC_OK) return rc;
   if (h->desc.physics != DGC_LAPLACE) {
     dgk::LaunchInfo li;
-    cudaError_t e = h->prec == DGC_F64
-                        ? dgk::rhs_dispatch<double>(h->N, h->desc.physics, h->rhs_variant, dgk::RhsParams{},
-                                                    h->sm_count, 0, &li)
-                        : dgk::rhs_dispatch<float>(h->N, h->desc.physics, h->rhs_variant, dgk::RhsParams{},
-                                                   h->sm_count, 0, &li);
+    const cudaError_t e = rhs_dispatch_any(h, dgk::RhsParams{}, 0, &li);
     if (e != cudaSuccess) return cuda_fail(e, "configure rhs kernel");
     h->rhs_info = li;
   }
@@ -278,6 +369,7 @@ void device_free(dgc_handle_s* h) {
   }
   cudaFree(h->d_tc_b);
   cudaFree(h->d_blk_b);
+  cudaFree(h->d_blk_bs);
   ipdg_free(h);
 }
 
@@ -301,7 +393,7 @@ extern "C" int dgc_get_info(dgc_handle h, dgc_info* o) {
   o->num_fields = h->Nf;
   o->precision = h->prec;
   o->state_len = (int64_t)h->K * h->Nf * h->NpP;
-  o->scalar_bytes = h->prec == DGC_F64 ? 8 : 4;
+  o->scalar_bytes = h->prec == DGC_F32 ? 4 : 8;
   o->num_boundary_faces = h->mesh.num_bfaces;
   o->min_edge = h->mesh.min_edge;
   o->min_altitude = h->mesh.min_altitude;
@@ -316,6 +408,8 @@ extern "C" int dgc_get_info(dgc_handle h, dgc_info* o) {
 extern "C" int dgc_node_coordinates(dgc_handle h, double* x, double* y) {
   if (!h || !x || !y) return fail(DGC_ERR_ARG, "null argument");
   const dgc::MeshData& m = h->mesh;
+  if (m.cells.empty())
+    return fail(DGC_ERR_UNSUPPORTED, "the handle was created from geometry arrays and has no vertex coordinates");
   for (int k = 0; k < h->K; ++k) {
     const int32_t* c = &m.cells[3 * (size_t)k];
     for (int j = 0; j < h->Np; ++j) {
@@ -368,7 +462,9 @@ static int layout_convert(dgc_handle h, int layout, const void* src, void* dst, 
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const size_t n = (size_t)h->K * h->Nf * h->NpP;
   const int grid = (int)std::min<size_t>((n + 255) / 256, (size_t)h->sm_count * 16);
-  if (h->prec == DGC_F64)
+  if (h->prec == DGC_F32C)
+    k_layout_x2<<<grid, 256, 0, s>>>(h->K, h->Nf, h->Np, h->NpP, layout, to_native, src, dst);
+  else if (h->prec == DGC_F64)
     k_layout<double><<<grid, 256, 0, s>>>(h->K, h->Nf, h->Np, h->NpP, layout, to_native,
                                           static_cast<const double*>(src), static_cast<double*>(dst));
   else
@@ -387,6 +483,7 @@ extern "C" int dgc_from_native(dgc_handle h, int layout, const void* src, void* 
 
 extern "C" int dgc_axpy(dgc_handle h, double a, const void* x, const void* y, void* out, void* stream) {
   if (!h || !x || !y || !out) return fail(DGC_ERR_ARG, "null argument");
+  if (h->prec == DGC_F32C) return fail(DGC_ERR_UNSUPPORTED, "axpy is not offered for compensated FP32 states");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const size_t n = (size_t)h->K * h->Nf * h->NpP;
   const int grid = (int)std::min<size_t>((n + 255) / 256, (size_t)h->sm_count * 8);
@@ -410,7 +507,7 @@ dgk::RhsParams base_params(dgc_handle h) {
   p.bxy = h->d_bxy;
   p.mats = h->prec == DGC_F64 ? h->d_mats64[0] : h->d_mats32[0];
   p.mats_tc = h->prec == DGC_F32 ? h->d_tc_b : nullptr;
-  p.mats_blk = h->prec == DGC_F32 ? h->d_blk_b : nullptr;
+  p.mats_blk = h->prec == DGC_F32 ? h->d_blk_b : (h->prec == DGC_F32C ? h->d_blk_bs : nullptr);
   p.ax = h->desc.ax;
   p.ay = h->desc.ay;
   p.gx0 = h->desc.gx0;
@@ -422,10 +519,7 @@ dgk::RhsParams base_params(dgc_handle h) {
 }
 
 int launch(dgc_handle h, const dgk::RhsParams& p, cudaStream_t s) {
-  cudaError_t e =
-      h->prec == DGC_F64
-          ? dgk::rhs_dispatch<double>(h->N, h->desc.physics, h->rhs_variant, p, h->sm_count, s, nullptr)
-          : dgk::rhs_dispatch<float>(h->N, h->desc.physics, h->rhs_variant, p, h->sm_count, s, nullptr);
+  const cudaError_t e = dgc::rhs_dispatch_any(h, p, s, nullptr);
   if (e != cudaSuccess) return cuda_fail(e, "rhs kernel launch");
   ++h->launches;
   return DGC_OK;
@@ -459,6 +553,8 @@ extern "C" int dgc_rhs(dgc_handle h, const void* q, double t, void* out, void* s
 extern "C" int dgc_rk4_step(dgc_handle h, void* q, double t, double dt, void* const* work, void* stream) {
   if (!h || !q || !work || !work[0] || !work[1] || !work[2]) return fail(DGC_ERR_ARG, "null argument");
   if (int rc = check_time_dependent(h)) return rc;
+  if (h->prec == DGC_F32C)
+    return fail(DGC_ERR_UNSUPPORTED, "classical RK4 is not offered for compensated FP32 states (use LSERK4)");
   void* ya = work[0];
   void* yb = work[1];
   void* acc = work[2];
@@ -685,10 +781,7 @@ namespace {
 
 int refresh_rhs_info(dgc_handle h) {
   dgk::LaunchInfo li;
-  cudaError_t e = h->prec == DGC_F64 ? dgk::rhs_dispatch<double>(h->N, h->desc.physics, h->rhs_variant,
-                                                                 dgk::RhsParams{}, h->sm_count, 0, &li)
-                                     : dgk::rhs_dispatch<float>(h->N, h->desc.physics, h->rhs_variant,
-                                                                dgk::RhsParams{}, h->sm_count, 0, &li);
+  const cudaError_t e = dgc::rhs_dispatch_any(h, dgk::RhsParams{}, 0, &li);
   if (e != cudaSuccess) return cuda_fail(e, "configure rhs kernel");
   h->rhs_info = li;
   return DGC_OK;
@@ -733,7 +826,7 @@ void cache_store(const std::string& key, int v) {
 
 extern "C" int dgc_num_variants(dgc_handle h) {
   if (!h) return fail(DGC_ERR_ARG, "null handle");
-  if (h->desc.physics == DGC_LAPLACE) return 1;
+  if (h->desc.physics == DGC_LAPLACE || h->prec == DGC_F32C) return 1;
   return dgk::rhs_num_variants(h->prec == DGC_F32, h->N);
 }
 
@@ -764,7 +857,7 @@ extern "C" int dgc_autotune(dgc_handle h, int reps, double* times_ms, int* chose
   }
   if (reps <= 0) reps = 10;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  const size_t bytes = (size_t)h->K * h->Nf * h->NpP * (h->prec == DGC_F64 ? 8 : 4);
+  const size_t bytes = dgc::state_bytes(h);
   void *qa = nullptr, *qb = nullptr, *res = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   const int keep = h->rhs_variant;

@@ -87,7 +87,7 @@ struct RhsConfig {
   static constexpr int ESTR = Nf * O::NpP;                                      // state stride per element
   // dynamic shared memory layout (bytes)
   static constexpr uint32_t oBar = 0;
-  static constexpr uint32_t oMats = 16;
+  static constexpr uint32_t oMats = 32;  // room for the three barriers of the batched kernel's other tile code
   static constexpr uint32_t oQ = oMats + MatLayout<R, N>::kBytes;
   static constexpr uint32_t oGeom = (oQ + TE * ESTR * sizeof(R) + 15) / 16 * 16;
   static constexpr uint32_t oNbr = oGeom + TE * 16 * sizeof(R);

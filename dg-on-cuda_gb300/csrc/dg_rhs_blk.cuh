@@ -64,15 +64,21 @@ __device__ __forceinline__ float f4c(const float4& v, int i) {
   return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
 }
 
+// Tiles t0, t0 + tstep, ... < tend of the stage p: the operator copy, then a
+// double-buffered tile loop.  smem holds BlkConfig's layout with its three
+// mbarriers (initialised by the caller) at offset 0; ph[0], ph[1] are the
+// phases of the tile-buffer barriers, ph[2] that of the operator barrier, kept
+// by the caller across calls.  Every thread must have finished with smem
+// before the call; the call ends in a CTA barrier.  False if a wait expired
+// (uniform across the CTA).
 template <int N, int P, int EPT_, int MAP_>
-__global__ void __launch_bounds__(BlkConfig<N, P, EPT_, MAP_>::kThreads, BlkConfig<N, P, EPT_, MAP_>::kMinBlocks)
-    dg_rhs_blk_kernel(const RhsParams p) {
+__device__ __forceinline__ bool blk_tiles(const RhsParams& p, unsigned char* smem, uint32_t (&ph)[3], int t0,
+                                          int tstep, int tend) {
   using C = BlkConfig<N, P, EPT_, MAP_>;
   constexpr int Np = C::Np, NpP = C::NpP, NFACE = C::NFACE, Nfp = Order<N>::Nfp;
   constexpr int EPT = C::EPT, NG = C::NG, NTE = C::NTE, TE = C::TE, NF = C::Nf, ESTR = C::ESTR;
   constexpr int FSTR = C::FSTR, NT = C::kThreads;
 
-  extern __shared__ __align__(128) unsigned char smem[];
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem + C::oBar);  // [0], [1]: tile buffers, [2]: operators
   const float* sB = reinterpret_cast<const float*>(smem + C::oMats);
   float* sF = reinterpret_cast<float*>(smem + C::oFlux);
@@ -88,17 +94,10 @@ __global__ void __launch_bounds__(BlkConfig<N, P, EPT_, MAP_>::kThreads, BlkConf
   // element slot and 4-node group of this thread
   const int slot = C::MAP == 0 ? tid / NG : ((tid >> 5) / NG) * 32 + (tid & 31);
   const int grp = C::MAP == 0 ? tid - (tid / NG) * NG : (tid >> 5) % NG;
-  const int ntiles = (p.K + TE - 1) / TE;
   const float* qin = static_cast<const float*>(p.q_in);
   const double tnow = p.t_dev ? *p.t_dev + p.t : p.t;
   const float cax = p.fax, cay = p.fay, cca = p.fca, ccb = p.fcb, cdt = p.fdt;
 
-  if (tid == 0) {
-    mbar_init(&bar[0], 1);
-    mbar_init(&bar[1], 1);
-    mbar_init(&bar[2], 1);
-    fence_barrier_init();
-  }
   // the padding columns of the flux rows are never written by the face phase
   for (int x = tid; x < TE * NF * FSTR; x += NT) sF[x] = 0.0f;
   __syncthreads();
@@ -115,22 +114,23 @@ __global__ void __launch_bounds__(BlkConfig<N, P, EPT_, MAP_>::kThreads, BlkConf
   };
 
   if (tid == 0) {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     mbar_arrive_expect_tx(&bar[2], C::kMat);
     bulk_g2s(const_cast<float*>(sB), p.mats_blk, C::kMat, &bar[2]);
-    if ((int)blockIdx.x < ntiles) issue(blockIdx.x, 0);
+    if (t0 < tend) issue(t0, 0);
   }
-  if (!__syncthreads_and(mbar_wait(&bar[2], 0, p.status))) return;
+  if (!__syncthreads_and(mbar_wait(&bar[2], ph[2], p.status))) return false;
+  ph[2] ^= 1;
 
-  uint32_t ph[2] = {0, 0};
   int it = 0;
-  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
+  for (int tile = t0; tile < tend; tile += tstep, ++it) {
     const int b = it & 1;
     const int k0 = tile * TE, ne = min(TE, p.K - k0);
-    const int nxt = tile + gridDim.x;
+    const int nxt = tile + tstep;
     // buffer b^1 was last read in the previous iteration, which ended in a
     // CTA barrier, so it (and its mbarrier) can be refilled now
-    if (tid == 0 && nxt < ntiles) issue(nxt, b ^ 1);
-    if (!__syncthreads_and(mbar_wait(&bar[b], ph[b], p.status))) return;
+    if (tid == 0 && nxt < tend) issue(nxt, b ^ 1);
+    if (!__syncthreads_and(mbar_wait(&bar[b], ph[b], p.status))) return false;
     ph[b] ^= 1;
     const float* sQ = bufQ(b);
     const float* sA = bufA(b);
@@ -337,6 +337,24 @@ __global__ void __launch_bounds__(BlkConfig<N, P, EPT_, MAP_>::kThreads, BlkConf
     }
     __syncthreads();
   }
+  return true;
+}
+
+template <int N, int P, int EPT_, int MAP_>
+__global__ void __launch_bounds__(BlkConfig<N, P, EPT_, MAP_>::kThreads, BlkConfig<N, P, EPT_, MAP_>::kMinBlocks)
+    dg_rhs_blk_kernel(const RhsParams p) {
+  using C = BlkConfig<N, P, EPT_, MAP_>;
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + C::oBar);
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    mbar_init(&bar[2], 1);
+    fence_barrier_init();
+  }
+  __syncthreads();
+  uint32_t ph[3] = {0, 0, 0};
+  blk_tiles<N, P, EPT_, MAP_>(p, smem, ph, blockIdx.x, gridDim.x, (p.K + C::TE - 1) / C::TE);
 }
 
 }  // namespace dgk

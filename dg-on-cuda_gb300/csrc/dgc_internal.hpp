@@ -33,6 +33,7 @@ struct dgc_handle_s {
   void* d_mats32[2] = {nullptr, nullptr};
   void* d_tc_b = nullptr;     // FP32 tensor-core operand [Dr | Ds | LIFT] (strong form, split TF32)
   void* d_blk_b = nullptr;    // FP32 operand of the register-blocked kernel (weak form, rows padded to NpP)
+  void* d_blk_bs = nullptr;   // the same rows in the strong form (compensated-state kernel, DGC_F32C)
   int* d_status = nullptr;    // device-side error word
   double* d_time = nullptr;   // simulation time for graph-replayed steps
   dgk::LaunchInfo rhs_info;
@@ -49,7 +50,14 @@ struct dgc_handle_s {
 
 namespace dgc {
 
+// bytes of one state vector of the handle (DGC_F32C: the hi and lo vectors)
+inline size_t state_bytes(const dgc_handle_s* h) {
+  return (size_t)h->K * h->Nf * h->NpP * (h->prec == DGC_F32 ? 4 : 8);
+}
+
 int set_error(int code, const char* msg);
+// the stage kernel of the handle's precision and variant (capi.cu)
+cudaError_t rhs_dispatch_any(const dgc_handle_s* h, const dgk::RhsParams& p, cudaStream_t s, dgk::LaunchInfo* info);
 int upload_operators(dgc_handle_s* h, int form);
 int device_init(dgc_handle_s* h);
 void device_free(dgc_handle_s* h);

@@ -139,6 +139,7 @@ namespace {
 int check_scalar_handle(dgc_handle h) {
   if (!h) return set_error(DGC_ERR_ARG, "null handle");
   if (h->Nf != 1) return set_error(DGC_ERR_UNSUPPORTED, "grad / div act on scalar-field (advection, laplace) handles");
+  if (h->prec == DGC_F32C) return set_error(DGC_ERR_UNSUPPORTED, "grad / div are not offered for compensated FP32 handles");
   return DGC_OK;
 }
 

@@ -66,7 +66,7 @@ extern "C" int dgc_write_data_file(const char* path, int64_t n, const double* x,
 
 extern "C" int dgc_save_state(dgc_handle h, const char* path, const void* q, double t, void* stream) {
   if (!h || !path || !q) return set_error(DGC_ERR_ARG, "null argument");
-  const size_t bytes = (size_t)h->K * h->Nf * h->NpP * (h->prec == DGC_F64 ? 8 : 4);
+  const size_t bytes = dgc::state_bytes(h);
   std::vector<unsigned char> host(bytes);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   cudaError_t e = cudaMemcpyAsync(host.data(), q, bytes, cudaMemcpyDeviceToHost, s);
@@ -102,7 +102,7 @@ extern "C" int dgc_load_state(dgc_handle h, const char* path, void* q, double* t
   if (hd.physics != h->desc.physics || hd.order != h->N || hd.np_padded != h->NpP || hd.num_fields != h->Nf ||
       hd.precision != h->prec || hd.num_cells != h->K)
     return set_error(DGC_ERR_ARG, "checkpoint was written for another discretisation");
-  const size_t bytes = (size_t)hd.state_len * (h->prec == DGC_F64 ? 8 : 4);
+  const size_t bytes = (size_t)hd.state_len * (h->prec == DGC_F32 ? 4 : 8);
   std::vector<unsigned char> host(bytes);
   if (std::fread(host.data(), 1, bytes, fc.f) != bytes) return set_error(DGC_ERR_ARG, "checkpoint truncated");
   if (fnv1a(host.data(), bytes) != hd.checksum) return set_error(DGC_ERR_ARG, "checkpoint checksum mismatch");

@@ -53,6 +53,8 @@ cudaError_t rhs_dispatch(int N, int P, int variant, const RhsParams& p, int sm_c
                          LaunchInfo* info);
 // number of tile-shape variants compiled for (precision, order)
 int rhs_num_variants(int prec_f32, int N);
+// the compensated-state stage kernel (dg_rhs_x2.cuh), defined in rhs_x2.cu
+cudaError_t rhs_x2_dispatch(int N, int P, const RhsParams& p, int sm_count, cudaStream_t s, LaunchInfo* info);
 
 }  // namespace dgk
 
@@ -61,6 +63,7 @@ int rhs_num_variants(int prec_f32, int N);
 #include "dg_rhs_tct.cuh"
 #include "dg_rhs_tcp.cuh"
 #include "dg_rhs_v2.cuh"
+#include "dg_rhs_x2.cuh"
 
 namespace dgk {
 

@@ -410,7 +410,13 @@ bool build_mesh(const double* vxy, int nv, const int32_t* cells, int K, const Re
           m.bxy.push_back(l2 * m.vy[c[0]] + l3 * m.vy[c[1]] + l1 * m.vy[c[2]]);
         }
       }
+  fill_penalty(m, re);
+  return true;
+}
+
+void fill_penalty(MeshData& m, const RefElement& re) {
   // laplace penalty tau_f = (N+1)^2 / h_f, h_f = smaller altitude onto the face
+  const int K = m.K;
   m.tau.assign((size_t)4 * K, 0.0);
   const double n1 = (re.N + 1.0) * (re.N + 1.0);
   for (int k = 0; k < K; ++k)
@@ -424,6 +430,67 @@ bool build_mesh(const double* vxy, int nv, const int32_t* cells, int K, const Re
       }
       m.tau[(size_t)4 * k + f] = n1 / h;
     }
+}
+
+bool build_mesh_from_arrays(int K, const RefElement& re, const double* invJ, const double* J, const double* faceJ,
+                            const int32_t* nb_cell, const int32_t* nb_face, int num_boundary_nodes, const double* bx,
+                            const double* by, const double* nx, const double* ny, MeshData& m, std::string& err) {
+  char buf[200];
+  auto bad = [&](const char* fmt, long a, long b) {
+    std::snprintf(buf, sizeof buf, fmt, a, b);
+    err = buf;
+    return false;
+  };
+  if (K <= 0 || K >= (1 << 29)) return bad("cell count %ld outside [1, 2^29) (%ld)", K, 0);
+  const int Nfp = re.Nfp;
+  m = MeshData();
+  m.K = K;
+  m.N = re.N;
+  m.Np = re.Np;
+  m.Nfp = Nfp;
+  m.geom.assign((size_t)K * kGeomStride, 0.0);
+  m.nbr.assign((size_t)4 * K, 0);
+  m.min_edge = 1e300;
+  m.min_altitude = 1e300;
+  int offset = 0;
+  for (int k = 0; k < K; ++k) {
+    double* g = &m.geom[(size_t)k * kGeomStride];
+    for (int i = 0; i < 4; ++i) g[G_RX + i] = invJ[4 * (size_t)k + i];
+    g[G_J] = J[k];
+    if (!(J[k] > 0.0)) return bad("cell %ld: J is not positive (%ld)", k, 0);
+    for (int f = 0; f < 3; ++f) {
+      const size_t i = 3 * (size_t)k + f;
+      g[G_FJ0 + f] = faceJ[i];
+      g[G_NX0 + f] = nx[i];
+      g[G_NY0 + f] = ny[i];
+      if (!(faceJ[i] > 0.0)) return bad("cell %ld face %ld: faceJ is not positive", k, f);
+      const double len = 2.0 * faceJ[i];
+      m.min_edge = std::min(m.min_edge, len);
+      m.min_altitude = std::min(m.min_altitude, 4.0 * J[k] / len);
+      const int32_t c = nb_cell[i], e = nb_face[i];
+      if (c < 0 || c >= K) return bad("cell %ld: neighbour cell %ld out of range", k, c);
+      if (c == k) {
+        // boundary face: nb_face is the running offset into the boundary nodes
+        if (e != offset) return bad("cell %ld: boundary node offset %ld out of sequence", k, e);
+        m.nbr[4 * (size_t)k + f] = -(1 + m.num_bfaces);
+        ++m.num_bfaces;
+        offset += Nfp;
+      } else {
+        if (e < 0 || e > 2) return bad("cell %ld: neighbour face %ld out of range", k, e);
+        const size_t j = 3 * (size_t)c + e;
+        if (nb_cell[j] != k || nb_face[j] != f) return bad("cells %ld and %ld: interface map not symmetric", k, c);
+        m.nbr[4 * (size_t)k + f] = (c << 2) | e;
+      }
+    }
+  }
+  if (offset != num_boundary_nodes)
+    return bad("boundary node count %ld does not match the interfaces (%ld)", num_boundary_nodes, offset);
+  m.bxy.resize((size_t)2 * offset);
+  for (int b = 0; b < offset; ++b) {
+    m.bxy[2 * (size_t)b] = bx[b];
+    m.bxy[2 * (size_t)b + 1] = by[b];
+  }
+  fill_penalty(m, re);
   return true;
 }
 

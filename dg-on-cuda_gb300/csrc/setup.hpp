@@ -107,6 +107,18 @@ struct MeshData {
 bool build_mesh(const double* vxy, int nv, const int32_t* cells, int K, const RefElement& re,
                 MeshData& out, std::string& err, bool gpu_topology = false);
 
+// The same MeshData from the reference's flattened arrays
+// (simple_discretization_2d::fill_cell_mappings / fill_cell_interfaces /
+// fill_boundary_nodes / fill_outward_normals, src/simple_discretization_2d.h:
+// 112-218): the geometry is taken as given; boundary faces are the faces that
+// map to their own cell, with the running boundary-node offset in nb_face.
+// No vertex coordinates or connectivity (vx, vy, cells stay empty).
+bool build_mesh_from_arrays(int K, const RefElement& re, const double* invJ, const double* J, const double* faceJ,
+                            const int32_t* nb_cell, const int32_t* nb_face, int num_boundary_nodes, const double* bx,
+                            const double* by, const double* nx, const double* ny, MeshData& m, std::string& err);
+// the laplace penalty per face from the geometry and neighbours of m
+void fill_penalty(MeshData& m, const RefElement& re);
+
 // twin[3 k + f] = (k' << 2 | f') of the twin half-edge, or -1 on the boundary
 // (csrc/topology.cu)
 bool gpu_match_half_edges(const int32_t* cells, int K, std::vector<int32_t>& twin, std::string& err);

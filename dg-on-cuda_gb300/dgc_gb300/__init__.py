@@ -19,7 +19,7 @@ PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 LIB_PATH = os.path.join(PKG, "lib", "libdgc_gb300.so")
 
 ADVECTION, MAXWELL_TM, MAXWELL_TE, LAPLACE = 0, 1, 2, 3
-F64, F32 = 0, 1
+F64, F32, F32C = 0, 1, 2  # F32C: FP32 arithmetic, compensated (hi + lo) FP32 state
 BC_SINSIN, BC_GAUSS, BC_ZERO = 0, 1, 2
 TAU_ONE, TAU_SCALED = 0, 1
 LAYOUT_NATIVE, LAYOUT_REF_CPU, LAYOUT_REF_GPU = 0, 1, 2
@@ -83,6 +83,8 @@ def lib():
             L = C.CDLL(LIB_PATH)
             L.dgc_last_error.restype = C.c_char_p
             L.dgc_create.argtypes = [C.c_int, _dp, C.c_int, _ip, C.POINTER(ProblemDesc), C.POINTER(_vp)]
+            L.dgc_create_from_arrays.argtypes = [C.c_int, _dp, _dp, _dp, _ip, _ip, C.c_int, C.c_void_p,
+                                                 C.c_void_p, _dp, _dp, C.POINTER(ProblemDesc), C.POINTER(_vp)]
             L.dgc_destroy.argtypes = [_vp]
             L.dgc_get_info.argtypes = [_vp, C.POINTER(Info)]
             L.dgc_node_coordinates.argtypes = [_vp, _dp, _dp]
@@ -250,6 +252,31 @@ class Discretization:
         self.desc = ProblemDesc(physics, order, precision, ax, ay, bc, gx0, gy0, gw, tau, int(dirichlet))
         h = _vp()
         _check(lib().dgc_create(xy.size // 2, xy, cells.size // 3, cells, C.byref(self.desc), C.byref(h)))
+        self._adopt(h, precision)
+
+    @classmethod
+    def from_arrays(cls, arrays, physics, order: int, precision: int = F64, ax: float = 1.0, ay: float = 1.0,
+                    bc: int = BC_SINSIN, gx0: float = -0.3, gy0: float = 0.0, gw: float = 0.02,
+                    tau: int = TAU_SCALED, dirichlet: bool = True):
+        """Handle from the reference's flattened discretisation arrays (a mapping with
+        invJ, J, faceJ, nbCell, nbFace, bx, by, nx, ny as simple_discretization_2d's
+        fill_* functions produce them), through dgc_create_from_arrays."""
+        if isinstance(physics, str):
+            physics = PHYSICS[physics]
+        self = cls.__new__(cls)
+        f = lambda k: np.ascontiguousarray(arrays[k], dtype=np.float64).reshape(-1)  # noqa: E731
+        i = lambda k: np.ascontiguousarray(arrays[k], dtype=np.int32).reshape(-1)   # noqa: E731
+        J = f("J")
+        bx, by = f("bx"), f("by")
+        self.desc = ProblemDesc(physics, order, precision, ax, ay, bc, gx0, gy0, gw, tau, int(dirichlet))
+        h = _vp()
+        _check(lib().dgc_create_from_arrays(J.size, f("invJ"), J, f("faceJ"), i("nbCell"), i("nbFace"), bx.size,
+                                            bx.ctypes.data, by.ctypes.data, f("nx"), f("ny"),
+                                            C.byref(self.desc), C.byref(h)))
+        self._adopt(h, precision)
+        return self
+
+    def _adopt(self, h, precision: int) -> None:
         self._h = h
         info = Info()
         _check(lib().dgc_get_info(self._h, C.byref(info)))
@@ -271,7 +298,7 @@ class Discretization:
         self.K, self.N, self.Np, self.NpP = info.num_cells, info.order, info.np, info.np_padded
         self.Nfp, self.Nf = info.nfp, info.num_fields
         self.state_len = info.state_len
-        self.precision = F64
+        self.precision = info.precision
         return self
 
     def __del__(self):
@@ -288,6 +315,17 @@ class Discretization:
     def torch_dtype(self):
         import torch
         return torch.float64 if self.precision == F64 else torch.float32
+
+    @property
+    def state_elems(self) -> int:
+        """Elements of torch_dtype in one native state buffer (F32C: hi and lo vectors)."""
+        return 2 * self.state_len if self.precision == F32C else self.state_len
+
+    @property
+    def ref_dtype(self):
+        """dtype of the reference-layout arrays dgc_to_native / dgc_from_native exchange."""
+        import torch
+        return torch.float32 if self.precision == F32 else torch.float64
 
     def node_xy(self):
         x = np.zeros(self.K * self.Np)
@@ -348,7 +386,7 @@ class Discretization:
     def empty_state(self, zero: bool = True):
         import torch
         f = torch.zeros if zero else torch.empty
-        return f(self.state_len, dtype=self.torch_dtype, device="cuda")
+        return f(self.state_elems, dtype=self.torch_dtype, device="cuda")
 
     def to_native(self, src, layout: int = LAYOUT_REF_CPU, out=None, stream=None):
         out = self.empty_state() if out is None else out
@@ -358,14 +396,14 @@ class Discretization:
     def from_native(self, q, layout: int = LAYOUT_REF_CPU, out=None, stream=None):
         import torch
         if out is None:
-            out = torch.empty(self.Nf * self.K * self.Np, dtype=self.torch_dtype, device="cuda")
+            out = torch.empty(self.Nf * self.K * self.Np, dtype=self.ref_dtype, device="cuda")
         _check(lib().dgc_from_native(self._h, layout, _ptr(q), _ptr(out), _stream(stream)))
         return out
 
     def upload(self, q_ref_cpu: np.ndarray, stream=None):
         """Host array in the reference CPU layout [field][cell][node] -> native device state."""
         import torch
-        src = torch.from_numpy(np.ascontiguousarray(q_ref_cpu).reshape(-1)).to(self.torch_dtype).cuda()
+        src = torch.from_numpy(np.ascontiguousarray(q_ref_cpu).reshape(-1)).to(self.ref_dtype).cuda()
         return self.to_native(src, LAYOUT_REF_CPU, stream=stream)
 
     def download(self, q, stream=None) -> np.ndarray:

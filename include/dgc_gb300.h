@@ -50,7 +50,17 @@ typedef enum dgc_physics {
   DGC_LAPLACE = 3      /* strong-form LDG/IPDG laplace_2d (src/laplace_2d.h:130-251) */
 } dgc_physics;
 
-typedef enum dgc_precision { DGC_F64 = 0, DGC_F32 = 1 } dgc_precision;
+/* DGC_F32C (advection / Maxwell handles): FP32 arithmetic with the state
+ * carried as a compensated pair hi + lo of FP32 values.  A state buffer holds
+ * 2 x state_len floats (the hi vector, then the lo vector; 8 bytes per entry
+ * in all); residual registers are plain FP32 vectors of state_len floats
+ * (a buffer of the state's size also serves).  The stage kernel evaluates the
+ * strong form with jump-based surface terms, so the round-off floor of long
+ * runs sits well below that of DGC_F32 (no reference counterpart: the
+ * reference runs FP64 only).  dgc_to_native / dgc_from_native take and give
+ * FP64 arrays in the reference layouts for these handles.  Classical RK4,
+ * axpy, batches and grad / div are not offered for them. */
+typedef enum dgc_precision { DGC_F64 = 0, DGC_F32 = 1, DGC_F32C = 2 } dgc_precision;
 
 /* advection inflow values: the exact translated solution */
 typedef enum dgc_bc {
@@ -107,6 +117,23 @@ typedef struct dgc_info {
  * both give the same result. */
 int dgc_create(int num_vertices, const double* vertex_xy, int num_cells, const int32_t* cells,
                const dgc_problem_desc* desc, dgc_handle* out);
+
+/* The same handle from the reference's flattened discretisation arrays, as
+ * simple_discretization_2d's fill_cell_mappings (invJ [K][4] = rx, ry, sx, sy;
+ * J [K]; faceJ [K][3]), fill_cell_interfaces (nb_cell, nb_face [K][3]: the
+ * twin (cell, face), or for a boundary face the cell itself and the running
+ * offset into the boundary nodes), fill_boundary_nodes (bx, by, the
+ * num_boundary_nodes = boundary faces x (N+1) coordinates) and
+ * fill_outward_normals (nx, ny [K][3]) produce them
+ * (src/simple_discretization_2d.h:112-218), i.e. what the examples' host
+ * code hands to create_device_object (examples/advection_2d/
+ * k_advection_2d.cuh:32-50).  The geometry is used as given (bit for bit);
+ * the interface map must be symmetric.  Such a handle has no vertex
+ * coordinates: dgc_node_coordinates returns DGC_ERR_UNSUPPORTED. */
+int dgc_create_from_arrays(int num_cells, const double* invJ, const double* J, const double* faceJ,
+                           const int32_t* nb_cell, const int32_t* nb_face, int num_boundary_nodes, const double* bx,
+                           const double* by, const double* nx, const double* ny, const dgc_problem_desc* desc,
+                           dgc_handle* out);
 
 /* Replaces destroy_simple_discretization_2d_on_device / destroy_device_object
  * (src/d_simple_discretization_2d.cuh:133-152). */

@@ -113,3 +113,21 @@ def test_jittered_mesh_properties():
     assert onb.sum() == 4 * 32
     m2 = meshes.jittered_square(32, 5)
     assert np.array_equal(m.xy, m2.xy)
+
+
+def test_create_from_arrays_rejects_inconsistent_interfaces(L):
+    """The reference-array path validates the interface map before it touches a
+    GPU: an asymmetric twin or an out-of-sequence boundary offset is refused."""
+    d = dict(np.load(os.path.join(GOLDEN, "ref_jit4_N2.npz")))
+    K = d["J"].size
+    cell = d["nbCell"].reshape(K, 3).copy()
+    k, f = next((k, f) for k in range(K) for f in range(3) if cell[k, f] != k)
+    cell[k, f] = (cell[k, f] + 1) % K if (cell[k, f] + 1) % K != k else (cell[k, f] + 2) % K
+    bad = dict(d, nbCell=cell.reshape(-1))
+    with pytest.raises(dg.DgcError, match="interface map|boundary node"):
+        dg.Discretization.from_arrays(bad, "advection", 2)
+    face = d["nbFace"].reshape(K, 3).copy()
+    kb, fb = next((k, f) for k in range(K) for f in range(3) if d["nbCell"].reshape(K, 3)[k, f] == k and face[k, f] > 0)
+    face[kb, fb] += 1
+    with pytest.raises(dg.DgcError, match="offset"):
+        dg.Discretization.from_arrays(dict(d, nbFace=face.reshape(-1)), "advection", 2)

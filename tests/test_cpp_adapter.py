@@ -1,6 +1,7 @@
 """The header-only C++ adapter (include/dgc_gb300.hpp) compiles against the
 C ABI with the host compiler, and on a GPU reproduces the reference's rk4 call
-shape bit-for-bit-close to the fused step."""
+shape bit-for-bit-close to the fused step, and the kernel_adapter phases of the
+Poisson example bit for bit as dgc_laplace_apply."""
 import os
 import subprocess
 
@@ -34,3 +35,4 @@ def test_adapter_reference_rk4_matches_fused():
     r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
     assert r.returncode == 0, r.stdout + r.stderr
     assert '"lserk4_result_buffer_ok": true' in r.stdout
+    assert '"execute_phase_vs_laplace_apply_relerr": 0.000e+00' in r.stdout

@@ -1,8 +1,10 @@
 """Batched persistent launches (dgc_batch_*): many independent FP32 advection /
 Maxwell problems with mixed orders and mesh sizes, one launch per LSERK4
-stage.  A batched step runs the same tile code as the per-instance variant-0
-kernel, so results must be bitwise equal to per-instance dgc_lserk4_step, and
-the per-instance results agree with the oracle at the FP32 tolerance."""
+stage.  A batched step runs the tile code of each handle's variant (variant 0,
+or the register-blocked one-element-per-thread variant: 5 at orders 1..6, 1
+at orders 7, 8), so results must be bitwise equal to per-instance
+dgc_lserk4_step with that variant, and the per-instance results agree with the
+oracle at the FP32 tolerance."""
 import numpy as np
 import pytest
 
@@ -40,16 +42,23 @@ def make(case):
     return D, o, p, dt
 
 
-def test_batched_steps_equal_per_instance_steps():
+def blk_variant(N):
+    return 5 if N <= 6 else 1
+
+
+@pytest.mark.parametrize("codes", ["v0", "blocked", "mixed"])
+def test_batched_steps_equal_per_instance_steps(codes):
     insts = [make(c) for c in CASES]
+    for i, (D, *_) in enumerate(insts):
+        blocked = codes == "blocked" or (codes == "mixed" and i % 2 == 1)
+        D.set_variant(blk_variant(D.N) if blocked else 0)
     t0 = [0.05 * i for i in range(len(insts))]
     q0 = [o.exact(p, t) for (D, o, p, dt), t in zip(insts, t0)]
     B = dg.Batch([D for D, _, _, _ in insts])
     dts = [dt for *_, dt in insts]
-    # reference: per-instance steps with variant 0
+    # reference: per-instance steps with each handle's variant
     ref = []
     for (D, o, p, dt), q, t in zip(insts, q0, t0):
-        D.set_variant(0)
         a, b, r = D.upload(q), D.empty_state(), D.empty_state()
         for s in range(3):
             D.lserk4_step(a, b, r, t + s * dt, dt)

@@ -11,8 +11,8 @@
   autotuned stage kernel and with the tensor-core pipeline (variant 9).
 * IPDG Poisson, jittered 256x256 mesh (K = 131072), N = 4, tau = (N+1)^2/h:
   the mixed-precision solution's residual recomputed on the CPU with the
-  oracle's operator (FP64) is at the solver's 1e-10, and its error against
-  sin(pi x) sin(pi y) matches the FP64 PCG solution's.
+  oracle's operator (FP64) is at the solver's 1e-10, and it agrees with the
+  FP64 PCG solution and with sin(pi x) sin(pi y) to the same tolerance.
 """
 import numpy as np
 import pytest
@@ -139,6 +139,9 @@ def test_poisson_k131072_n4_mixed_solution_residual_on_cpu():
     r = bo - o.spd(sol[dg.SOLVE_MIXED_IR], tau_mode=1)
     assert np.linalg.norm(r) <= 2e-10 * np.linalg.norm(bo)
     ex = (np.sin(np.pi * x) * np.sin(np.pi * y)).reshape(-1)
+    # at this resolution the discretisation error (~1e-12) is below the solves'
+    # algebraic error, so both solutions sit within the 1e-10 tolerance of the
+    # exact solution and of each other
     e_mixed, e_fp64 = relerr(sol[dg.SOLVE_MIXED_IR], ex), relerr(sol[dg.SOLVE_FP64_PCG], ex)
-    assert abs(e_mixed - e_fp64) <= 1e-6 * e_fp64 + 1e-12
-    assert relerr(sol[dg.SOLVE_MIXED_IR], sol[dg.SOLVE_FP64_PCG]) < 1e-8
+    assert e_mixed < 1e-10 and e_fp64 < 1e-10, (e_mixed, e_fp64)
+    assert relerr(sol[dg.SOLVE_MIXED_IR], sol[dg.SOLVE_FP64_PCG]) < 1e-10

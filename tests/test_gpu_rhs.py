@@ -229,3 +229,28 @@ def test_argument_errors():
         D.lserk4_step(q, q, D.empty_state(), 0.0, 0.1)
     with pytest.raises(dg.DgcError):
         dg.Discretization(meshes.jittered_square(2, 0), "maxwell_te", 9)
+
+
+@pytest.mark.parametrize("case", ["jit4_N4", "coarse_N3", "cells4_N2", "coarse_N6"])
+def test_create_from_reference_arrays_matches_reference(case):
+    """dgc_create_from_arrays with the reference's own fill_* arrays (the goldens
+    hold what simple_discretization_2d produced): RHS and RK4 steps of both
+    examples against the reference at 1e-12."""
+    d = np.load(os.path.join(GOLDEN, f"ref_{case}.npz"))
+    N = int(case.split("_N")[1])
+    D = dg.Discretization.from_arrays(d, "advection", N, dg.F64, ax=1.0, ay=1.0, bc=dg.BC_SINSIN)
+    u0 = D.upload(d["adv_u0"])
+    assert relerr(D.download(D.rhs(u0, 0.05)), d["adv_rhs"]) < TOL64
+    dt = float(d["dt"][0])
+    work = [D.empty_state() for _ in range(3)]
+    q = u0.clone()
+    for i in range(10):
+        D.rk4_step(q, i * dt, dt, work)
+    assert relerr(D.download(q), d["adv_rk4_10"]) < TOL64
+    M = dg.Discretization.from_arrays(d, "maxwell_tm", N, dg.F64)
+    q0 = M.upload(d["mx_q0"])
+    assert relerr(M.download(M.rhs(q0, 0.0)), d["mx_rhs"]) < TOL64
+    with pytest.raises(dg.DgcError, match="vertex coordinates"):
+        M.node_xy()
+    D.check()
+    M.check()
