@@ -167,7 +167,8 @@ class ClockSampler:
 
 
 # committed ncu summaries of the stage-kernel variants on this workload
-PROFILES = {5: "dg_rhs_blk_maxwell_te_n6_fp32.md", 9: "dg_rhs_tcp_maxwell_te_n6_fp32.md"}
+PROFILES = {5: "dg_rhs_blk_maxwell_te_n6_fp32.md", 9: "dg_rhs_tcp_maxwell_te_n6_fp32.md",
+            "x2": "dg_rhs_x2_maxwell_te_n6_fp32c.md"}
 
 
 def read_traffic(variant):
@@ -511,6 +512,8 @@ def measure_batched(dg, meshes):
     qb = [D.empty_state() for D, *_ in insts]
     rs = [D.empty_state() for D, *_ in insts]
     B.lserk4_run(qa, qb, rs, [0.0] * len(insts), dts, 4, graph=True)  # warm-up (even: back in qa)
+    for (D, q, *_), a in zip(insts, qa):                              # both arms start from the same state
+        a.copy_(D.upload(q))
     torch.cuda.synchronize()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     l0 = B.launch_count()
@@ -529,8 +532,8 @@ def measure_batched(dg, meshes):
     sr = [D.empty_state() for D, *_ in insts]
     for (D, *_), a, b, r, dt in zip(insts, sa, sb, sr, dts):
         D.lserk4_run(a, b, r, 0.0, dt, 4, graph=True)                  # warm-up, graph capture
-    sa = [D.upload(q) for D, q, *_ in insts]
-    sr = [D.empty_state() for D, *_ in insts]
+    for (D, q, *_), a in zip(insts, sa):                               # same buffers: the graphs are reused
+        a.copy_(D.upload(q))
     torch.cuda.synchronize()
     seq_fin = []
     ev0.record()
@@ -675,6 +678,41 @@ def measure_fp64(dg, m, q_init, dt, flush, stream, steps, dofs):
     ms = float(np.mean([x.elapsed_time(y) for x, y in evs]))
     D64.check()
     return D64, {"value": dofs * 5 / (ms * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": ms, "steps": steps}
+
+
+def measure_fp32c(dg, m, q_init, dt, flush, stream, steps, dofs):
+    """The workload with the compensated FP32 state (DGC_F32C): per-step time of
+    the 5 stage launches (L2 flushed before each step), GDOF/s and the stage
+    kernel's roofline.  Algorithmic bytes per element: hi and lo state read and
+    written, residual read and written (6 Nf Np x 4 B) + 14 FP32 geometric
+    factors + 3 int32 neighbours."""
+    import torch
+    D = dg.Discretization(m, "maxwell_te", ORDER, dg.F32C)
+    a, b, r = D.upload(q_init), D.empty_state(), D.empty_state()
+    for _ in range(3):
+        D.lserk4_step(a, b, r, 0.0, dt)
+        a, b = b, a
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(6)] for _ in range(steps)]
+    for it in range(steps):
+        flush.fill_(float(it))
+        evs[it][0].record(stream)
+        for st in range(5):
+            D.lserk4_stage(st, a if st % 2 == 0 else b, b if st % 2 == 0 else a, r, 0.0, dt)
+            evs[it][st + 1].record(stream)
+        a, b = b, a
+    torch.cuda.synchronize()
+    D.check()
+    step_ms = float(np.mean([e[0].elapsed_time(e[5]) for e in evs]))
+    stage_ms = float(np.mean([[e[s].elapsed_time(e[s + 1]) for s in range(5)] for e in evs]))
+    elem_bytes = 6 * 3 * D.Np * 4 + 14 * 4 + 3 * 4
+    peak, peak_kind = measured_peak()
+    achieved = elem_bytes * D.K / (stage_ms * 1e-3) / 1e9
+    return {"value": dofs * 5 / (step_ms * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": step_ms, "steps": steps,
+            "kernel": "dgk::dg_rhs_x2_kernel<6,PHYS_TE> (LSERK4 stage)",
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_source": peak_kind, "launch_ms": stage_ms,
+                         "alg_bytes_per_element": elem_bytes, "alg_bytes_per_launch": elem_bytes * D.K,
+                         "traffic": read_traffic("x2")}}
 
 
 def measure_accuracy(dg, D32, D64, q_init, x, y, dt):
@@ -893,8 +931,20 @@ def main():
                             else "unbound (GPU NUMA node not found)")
     D64, fp64 = (None, None) if args.no_fp64 else measure_fp64(dg, m, q_init, dt, flush, stream,
                                                                 max(3, min(args.steps, 10)), dofs)
+    fp32c = None if args.no_fp64 else measure_fp32c(dg, m, q_init, dt, flush, stream,
+                                                    max(3, min(args.steps, 10)), dofs)
+    equal_error = None
+    if rank == 0 and not args.no_equal_error:
+        equal_error = measure_equal_error(dg, meshes)
     accuracy = None
-    if rank == 0 and D64 is not None and not args.no_accuracy:
+    if rank == 0 and equal_error is not None and not args.no_accuracy:
+        # the sweep's run of this very workload (mesh, order, dt rule, T = 1)
+        row = next(r for r in equal_error["rows"] if r["n"] == NSIDE and r["order"] == ORDER)
+        accuracy = {"T": 1.0, "steps": row["steps"], "from": "equal_error sweep, same mesh / order / dt",
+                    "rel_l2_fp32_vs_exact": row["fp32"]["rel_l2"], "rel_l2_fp64_vs_exact": row["fp64"]["rel_l2"],
+                    "rel_l2_fp32c_vs_exact": row["fp32c"]["rel_l2"],
+                    "gdofs_graphed_run": {k: row[k]["gdofs"] for k in ("fp64", "fp32", "fp32c")}}
+    elif rank == 0 and D64 is not None and not args.no_accuracy:
         accuracy = measure_accuracy(dg, D32, D64, q_init, x, y, dt)
     poisson = None
     if rank == 0 and not args.no_poisson:
@@ -908,9 +958,6 @@ def main():
     stokes = None
     if rank == 0 and not args.no_stokes:
         stokes = measure_stokes(dg, meshes)
-    equal_error = None
-    if rank == 0 and not args.no_equal_error:
-        equal_error = measure_equal_error(dg, meshes)
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         csteps = 10
@@ -924,7 +971,7 @@ def main():
                 "warmup": args.warmup, "ms_per_step": my_ms, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config_dict(ws),
                 "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu,
-                "clocks": clocks, "fp64_plain": fp64,
+                "clocks": clocks, "fp64_plain": fp64, "fp32c": fp32c,
                 "speedup_mixed_vs_fp64": (value / ws / fp64["value"]) if fp64 else None,
                 "accuracy": accuracy, "poisson": poisson, "batched": batched, "learned_precond": learned,
                 "stokes": stokes, "equal_error": equal_error, "wall_s_timed_region": wall}
