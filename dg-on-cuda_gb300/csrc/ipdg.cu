@@ -306,7 +306,7 @@ struct IpdgState {
   // workspace: FP64 and FP32 vector sets
   double* w64[10] = {};
   float* w32[10] = {};
-  dgk::CgScalars* cg = nullptr;   // [2]: fp64 solve, fp32 inner solve
+  dgk::CgScalars* cg = nullptr;   // [3]: fp64 solve, fp32 inner solve, standalone FP32 applies (never done)
   double* dots = nullptr;         // scratch dot products
   dgk::CgScalars* h_cg = nullptr; // pinned host mirror
   double* h_dots = nullptr;
@@ -535,8 +535,8 @@ int ipdg_init(dgc_handle_s* h) {
     CKI(cudaMemset(st->w64[i], 0, n * 8));
     CKI(cudaMemset(st->w32[i], 0, n * 4));
   }
-  CKI(cudaMalloc(&st->cg, 2 * sizeof(dgk::CgScalars)));
-  CKI(cudaMemset(st->cg, 0, 2 * sizeof(dgk::CgScalars)));
+  CKI(cudaMalloc(&st->cg, 3 * sizeof(dgk::CgScalars)));
+  CKI(cudaMemset(st->cg, 0, 3 * sizeof(dgk::CgScalars)));
   CKI(cudaMalloc(&st->dots, 64));
   CKI(cudaMallocHost(&st->h_cg, 2 * sizeof(dgk::CgScalars)));
   CKI(cudaMallocHost(&st->h_dots, 64));
@@ -734,7 +734,28 @@ int true_residual(dgc_handle_s* h, const double* b64, const double* x64, double*
 
 int ipdg_spd_apply_f32(dgc_handle_s* h, const float* u, float* out, cudaStream_t s) {
   if (int rc = check_laplace(h)) return rc;
-  return apply<float>(h, dgk::IK_DIV_SPD, u, out, nullptr, nullptr, s);
+  IpdgState* st = h->ipdg;
+  if (st->bcdir) return apply<float>(h, dgk::IK_DIV_SPD, u, out, nullptr, nullptr, s);
+  // uniform boundary types: the register-blocked passes of the FP32 CG
+  // iteration with beta = 0 (the grad pass copies u to the direction slot W_T,
+  // the div pass writes S u), on a CG scalar record that never stops
+  dgk::IpdgParams p = base<float>(h);
+  p.cg = st->cg + 2;
+  p.first = 1;
+  p.slot = 0;
+  p.u = u;
+  p.p_old = u;
+  p.p = wv<float>(h, W_T);
+  p.qx = wv<float>(h, W_QX);
+  p.qy = wv<float>(h, W_QY);
+  cudaError_t e = dgk::ipdg_blk_launch(h->N, dgk::IB_GRAD, p, h->sm_count, s);
+  if (e != cudaSuccess) return cuda_err(e, "ipdg blocked kernel launch");
+  p.du_src = wv<float>(h, W_T);
+  p.out = out;
+  e = dgk::ipdg_blk_launch(h->N, dgk::IB_DIV, p, h->sm_count, s);
+  if (e != cudaSuccess) return cuda_err(e, "ipdg blocked kernel launch");
+  h->launches += 2;
+  return DGC_OK;
 }
 
 }  // namespace dgc
