@@ -467,6 +467,88 @@ def measure_learned(dg, meshes):
 BATCH_INSTANCES, BATCH_SEED, BATCH_STEPS = 96, 777, 10
 
 
+def batch_specs():
+    """The batched workload's instances, drawn from BATCH_SEED: n log-uniform in
+    [8, 160] squares per side, N uniform in {2..8}, physics uniform over advection
+    (random direction, Gaussian pulse at a random centre) and Maxwell TE / TM."""
+    rng = np.random.default_rng(BATCH_SEED)
+    out = []
+    for i in range(BATCH_INSTANCES):
+        n = int(round(np.exp(rng.uniform(np.log(8), np.log(160)))))
+        N = int(rng.integers(2, 9))
+        kind = ["advection", "maxwell_te", "maxwell_tm"][int(rng.integers(0, 3))]
+        sp = {"n": n, "N": N, "kind": kind, "seed": BATCH_SEED + i}
+        if kind == "advection":
+            th = rng.uniform(0, 2 * np.pi)
+            sp.update(ax=float(np.cos(th)), ay=float(np.sin(th)), gx0=float(rng.uniform(-0.5, 0.5)),
+                      gy0=float(rng.uniform(-0.5, 0.5)))
+        out.append(sp)
+    return out
+
+
+def batch_initial(sp, x, y):
+    """Initial state of a batch instance in the reference CPU layout [field][cell][node]."""
+    if sp["kind"] == "advection":
+        return np.exp(-((x - sp["gx0"]) ** 2 + (y - sp["gy0"]) ** 2) / 0.02)[None]
+    q = np.zeros((3,) + x.shape)
+    # TE: Hz = cos cos; TM: Ez = sin sin (both PEC cavity modes)
+    q[2] = (np.cos(np.pi * x) * np.cos(np.pi * y) if sp["kind"] == "maxwell_te"
+            else np.sin(np.pi * x) * np.sin(np.pi * y))
+    return q
+
+
+def _cpu_batch_worker(specs):
+    """One host process: one LSERK4 step of each given instance with the oracle
+    (the serial C port of the reference CPU operator, FP64); returns (DOF-stage
+    evaluations, seconds of the steps alone)."""
+    import oracle
+    from dgc_gb300 import meshes
+    work, sec = 0.0, 0.0
+    kinds = {"advection": oracle.ADVECTION, "maxwell_te": oracle.MAXWELL_TE, "maxwell_tm": oracle.MAXWELL_TM}
+    for sp in specs:
+        m = meshes.jittered_square(sp["n"], sp["seed"])
+        o = oracle.Oracle(m.xy, m.cells, sp["N"])
+        if sp["kind"] == "advection":
+            p = oracle.problem(oracle.ADVECTION, sp["ax"], sp["ay"], oracle.BC_GAUSS, sp["gx0"], sp["gy0"], 0.02)
+        else:
+            p = oracle.problem(kinds[sp["kind"]])
+        x, y = o.node_xy()
+        q = batch_initial(sp, x, y).reshape(-1)
+        dt = 0.5 * meshes.min_edge_length(m) / (sp["N"] + 1) ** 2
+        t0 = time.perf_counter()
+        o.lserk4_step(p, 0.0, dt, q, np.zeros_like(q))
+        sec += time.perf_counter() - t0
+        work += q.size * 5
+    return work, sec
+
+
+def cpu_batched_baseline():
+    """The batched workload on the host cores: one process per core (spawned, so
+    no CUDA state is inherited), the instances dealt out longest first, one LSERK4
+    step of each.  Aggregate GDOF/s over the slowest process's step time, and the
+    same work on one core."""
+    import multiprocessing as mp
+    specs = batch_specs()
+    cores = os.cpu_count() or 1
+    cost = lambda sp: 2 * sp["n"] ** 2 * ((sp["N"] + 1) * (sp["N"] + 2) // 2) ** 2 * (1 if sp["kind"] == "advection" else 3)  # noqa: E731,E501
+    bins = [[] for _ in range(cores)]
+    load = [0.0] * cores
+    for sp in sorted(specs, key=cost, reverse=True):
+        j = int(np.argmin(load))
+        bins[j].append(sp)
+        load[j] += cost(sp)
+    with mp.get_context("spawn").Pool(cores) as pool:
+        res = pool.map(_cpu_batch_worker, [b for b in bins if b])
+    work = sum(r[0] for r in res)
+    span = max(r[1] for r in res)
+    serial = sum(r[1] for r in res)
+    return {"value": work / span / 1e9, "unit": UNIT, "cores": cores, "kind": "port",
+            "single_core_gdofs": work / serial / 1e9,
+            "sample": f"one LSERK4 step of each of the {len(specs)} instances (serial C port of the reference CPU "
+                      f"operator, FP64), one spawned process per core, instances dealt longest first; "
+                      f"host {cpu_model()}"}
+
+
 def measure_batched(dg, meshes):
     """96 independent FP32 instances (advection with a random velocity direction
     and Gaussian pulse, or a Maxwell TE / TM cavity mode) on jittered meshes with
@@ -478,27 +560,17 @@ def measure_batched(dg, meshes):
     after instance, each with its own autotuned variant, its steps replayed
     from its own CUDA graph.  Aggregate GDOF/s of both."""
     import torch
-    rng = np.random.default_rng(BATCH_SEED)
     insts = []
-    for i in range(BATCH_INSTANCES):
-        n = int(round(np.exp(rng.uniform(np.log(8), np.log(160)))))
-        N = int(rng.integers(2, 9))
-        kind = ["advection", "maxwell_te", "maxwell_tm"][int(rng.integers(0, 3))]
-        m = meshes.jittered_square(n, BATCH_SEED + i)
+    for sp in batch_specs():
+        N, kind = sp["N"], sp["kind"]
+        m = meshes.jittered_square(sp["n"], sp["seed"])
         if kind == "advection":
-            th = rng.uniform(0, 2 * np.pi)
-            ax, ay = float(np.cos(th)), float(np.sin(th))
-            D = dg.Discretization(m, kind, N, dg.F32, ax=ax, ay=ay, bc=dg.BC_GAUSS,
-                                  gx0=float(rng.uniform(-0.5, 0.5)), gy0=float(rng.uniform(-0.5, 0.5)), gw=0.02)
-            x, y = D.node_xy()
-            q = np.exp(-((x - D.desc.gx0) ** 2 + (y - D.desc.gy0) ** 2) / 0.02)[None]
+            D = dg.Discretization(m, kind, N, dg.F32, ax=sp["ax"], ay=sp["ay"], bc=dg.BC_GAUSS,
+                                  gx0=sp["gx0"], gy0=sp["gy0"], gw=0.02)
         else:
             D = dg.Discretization(m, kind, N, dg.F32)
-            x, y = D.node_xy()
-            q = np.zeros((3,) + x.shape)
-            # TE: Hz = cos cos; TM: Ez = sin sin (both PEC cavity modes)
-            q[2] = (np.cos(np.pi * x) * np.cos(np.pi * y) if kind == "maxwell_te"
-                    else np.sin(np.pi * x) * np.sin(np.pi * y))
+        x, y = D.node_xy()
+        q = batch_initial(sp, x, y)
         tuned, times = D.autotune(reps=5)
         blk = 5 if N <= 6 else 1
         batch_v = blk if times[blk] < times[0] else 0
@@ -952,6 +1024,8 @@ def main():
     batched = None
     if rank == 0 and not args.no_batched:
         batched = measure_batched(dg, meshes)
+        if ws == 1 and not args.no_cpu_baseline:
+            batched["cpu_baseline"] = cpu_batched_baseline()
     learned = None
     if rank == 0 and not args.no_learned:
         learned = measure_learned(dg, meshes)
