@@ -30,6 +30,7 @@
 
 #include "dgc_gb300.h"
 #include "dgc_internal.hpp"
+#include "mpnn_tc.cuh"
 
 namespace dgk {
 
@@ -69,14 +70,6 @@ __device__ __forceinline__ void block_add(double v, double* out) {
   }
 }
 
-// face neighbours of graph node e (sample s = e / K): up to 3 node indices, -1 on the boundary
-__device__ __forceinline__ void neighbours(const int4* __restrict__ nbr, int K, int64_t e, int64_t (&j)[3]) {
-  const int64_t s = e / K;
-  const int4 n4 = __ldg(nbr + (e - s * K));
-  const int c[3] = {n4.x, n4.y, n4.z};
-#pragma unroll
-  for (int f = 0; f < 3; ++f) j[f] = c[f] >= 0 ? s * K + (c[f] >> 2) : -1;
-}
 
 // h0 = Win x + bin; 4 nodes x 64 channels per 256 threads, groups strided over the grid
 __global__ void __launch_bounds__(256) k_fwd_in(int64_t n, int npi, const __nv_bfloat16* __restrict__ Win,
@@ -653,9 +646,12 @@ int forward(dgc_mpnn m, int64_t n, const float* x, float* y, float* ha, float* h
   CKM(cudaGetLastError());
   for (int l = 0; l < L.L; ++l) {
     float* nxt = store ? m->hs[l + 1] : (cur == ha ? hb : ha);
-    const int tiles = (int)std::min<int64_t>((n + dgk::kTileN - 1) / dgk::kTileN, (int64_t)m->sm_count * 2);
-    dgk::k_fwd_layer<<<tiles, 256, dgk::kLayerSmem, s>>>(n, K, nbr, m->w16 + L.oWs(l), m->w16 + L.oWn(l),
-                                                         m->w16 + L.ob(l), cur, store ? m->as[l] : nullptr, nxt);
+    // tensor-core layer (mpnn_tc.cuh): persistent CTAs over 128-node tiles, 2 per SM
+    const int tiles = (int)std::min<int64_t>((n + dgk::MpnnTc::kRows - 1) / dgk::MpnnTc::kRows,
+                                             (int64_t)m->sm_count * 2);
+    dgk::k_fwd_layer_tc<<<tiles, dgk::MpnnTc::kThreads, dgk::MpnnTc::kSmem, s>>>(
+        n, K, nbr, m->w16 + L.oWs(l), m->w16 + L.oWn(l), m->w16 + L.ob(l), cur, store ? m->as[l] : nullptr, nxt,
+        m->h->d_status);
     CKM(cudaGetLastError());
     cur = nxt;
   }
@@ -754,6 +750,8 @@ extern "C" int dgc_mpnn_create(dgc_handle h, int layers, uint64_t seed, dgc_mpnn
   if (e != cudaSuccess) return fail(mcuda(e, "mpnn set-up"));
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(dgk::k_fwd_layer, cudaFuncAttributeMaxDynamicSharedMemorySize, dgk::kLayerSmem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(dgk::k_fwd_layer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, dgk::MpnnTc::kSmem);
   if (e != cudaSuccess) return fail(mcuda(e, "mpnn set-up"));
   dgk::k_to_bf16<<<grid_for(m, P, 256), 256>>>(P, m->w, m->w16);
   if ((e = cudaGetLastError()) != cudaSuccess) return fail(mcuda(e, "mpnn set-up"));

@@ -65,6 +65,26 @@ def test_forward_loss_and_gradients_match_numpy(kind):
     assert relerr(y, y_ref) < 1e-5
 
 
+def test_forward_many_tiles_matches_numpy():
+    # K = 2048 nodes per sample, 3 samples: 48 tiles of the 128-node tensor-core
+    # layer, a ragged last tile, 4 layers with random (non-zero) weights
+    m = meshes.jittered_square(32, 23)
+    N, L = 3, 4
+    D = dg.Discretization(m, "laplace", N, dg.F64, tau=dg.TAU_SCALED, dirichlet=True)
+    net = dg.MPNN(D, layers=L, seed=4)
+    K, Np, npi = D.K, D.Np, D.NpP
+    nbr = dg.host_mesh(m, N)[1]
+    rng = np.random.default_rng(6)
+    w = (rng.standard_normal(net.num_params) * 0.15).astype(np.float32)
+    net.set_weights(w)
+    x = rng.standard_normal((K, npi)).astype(np.float32)
+    x[:, Np:] = 0.0
+    y = net.forward(torch.from_numpy(x).cuda().reshape(-1)).cpu().numpy().reshape(K, npi)
+    y_ref = mpnn_ref.forward(w, x.astype(np.float64), nbr, K, npi, L)[0]
+    assert relerr(y, y_ref) < 1e-5
+    D.check()
+
+
 def test_weights_round_trip_and_adam_step_moves_weights():
     m = meshes.jittered_square(3, 2)
     D = dg.Discretization(m, "laplace", 3, dg.F64, tau=dg.TAU_SCALED, dirichlet=True)
