@@ -677,17 +677,18 @@ def run_reference(args):
     print(json.dumps(line))
 
 
-E2E_SETS = 8   # device buffer sets the end-to-end loop rotates through (3 x 11 MB each)
+E2E_STREAMS = 3  # CUDA streams the end-to-end loop issues its independent steps on
+E2E_SETS = 9     # device buffer sets it rotates through (3 x 11 MB each; a multiple of E2E_STREAMS)
 
 
 def measure_e2e(D32, bufs, res, flush, stream, t, dt, steps, ws, dofs, barrier):
     """End to end through the C ABI with pinned host buffers, every step: H2D of
     the step's input state, one LSERK4 step (dgc_lserk4_step), D2H of the new
     state.  Steps are independent (each starts from the host state), so they are
-    issued on two CUDA streams: one step's copies overlap the other's kernels,
-    as a host application streaming states through the library would run it.
-    The device buffers rotate through E2E_SETS sets (264 MB in all, more than
-    L2), so every step's kernels read their inputs from DRAM.  The same calls on
+    issued round robin on E2E_STREAMS CUDA streams: one step's copies overlap the
+    others' kernels, as a host application streaming states through the library
+    would run it.  The device buffers rotate through E2E_SETS sets (297 MB in all,
+    more than L2), so every step's kernels read their inputs from DRAM.  The same calls on
     one stream, one step after another with an L2 flush between steps, are
     reported as `serial`."""
     import torch
@@ -697,17 +698,18 @@ def measure_e2e(D32, bufs, res, flush, stream, t, dt, steps, ws, dofs, barrier):
     h_state.copy_(bufs[0].cpu())
     # pinned as well (empty_like would not pin it): a pageable target is staged
     # through a bounce buffer and page-faults on its first write
-    h_out = [torch.empty(n, dtype=torch.float32, pin_memory=True) for _ in range(2)]
+    h_out = [torch.empty(n, dtype=torch.float32, pin_memory=True) for _ in range(E2E_STREAMS)]
     sets = [(D32.empty_state(), D32.empty_state(), D32.empty_state()) for _ in range(E2E_SETS)]
-    streams = [torch.cuda.Stream(), torch.cuda.Stream()]
+    streams = [torch.cuda.Stream() for _ in range(E2E_STREAMS)]
 
     def one(i):
-        st = streams[i % 2]
+        # step i and step i + E2E_SETS share a buffer set and a host output: same stream
+        st = streams[i % E2E_STREAMS]
         qi, qo, rr = sets[i % E2E_SETS]
         with torch.cuda.stream(st):
             qi.copy_(h_state, non_blocking=True)
             D32.lserk4_step(qi, qo, rr, t, dt, stream=st.cuda_stream)
-            h_out[i % 2].copy_(qo, non_blocking=True)
+            h_out[i % E2E_STREAMS].copy_(qo, non_blocking=True)
 
     for i in range(4):  # warm-up: the same calls, untimed
         one(i)
@@ -740,7 +742,7 @@ def measure_e2e(D32, bufs, res, flush, stream, t, dt, steps, ws, dofs, barrier):
     return {"value": replicas.job_throughput(dofs * 5, ms * 1e-3, ws) / 1e9, "unit": UNIT,
             "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes, "ms_per_step": ms,
             "path": "dgc_lserk4_step via ctypes, pinned host state in and out every step, independent steps "
-                    f"on two streams, {E2E_SETS} device buffer sets (inputs larger than L2)",
+                    f"on {E2E_STREAMS} streams, {E2E_SETS} device buffer sets (inputs larger than L2)",
             "serial": {"value": replicas.job_throughput(dofs * 5, ms_serial * 1e-3, ws) / 1e9,
                        "ms_per_step": ms_serial,
                        "ms_per_step_min_median_max": [float(per.min()), float(np.median(per)),

@@ -17,7 +17,8 @@
 //     matrices of 8 rows x 16 bytes: element (row, k) at byte
 //     (row / 8) * 2048 + (k / 8) * 128 + (row % 8) * 16 + (k % 8) * 2);
 //   * two threads per tile row gather h_e and the neighbour rows (float4
-//     loads), sum, split and store the three X parts in the same layout;
+//     loads, two 8-channel chunks in flight at a time), sum, split and store
+//     the three X parts in the same layout;
 //   * one thread issues 8 K steps x 3 MMAs (M = 128, N = 64, K = 16) into 64
 //     TMEM columns and commits to an mbarrier (bounded wait);
 //   * the epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 (its rows),
@@ -40,7 +41,8 @@ struct MpnnTc {
   static constexpr uint32_t kBBytes = (kN / 8) * kSbo;     // 16 KB
   static constexpr uint32_t kABytes = (kRows / 8) * kSbo;  // 32 KB per split
   static constexpr uint32_t oBar = 0;               // mbarrier (8 B) + TMEM address (4 B)
-  static constexpr uint32_t oB = 128;
+  static constexpr uint32_t oBias = 16;             // 64 FP32 biases
+  static constexpr uint32_t oB = 384;
   static constexpr uint32_t oA = oB + kBBytes;
   static constexpr uint32_t kSmem = oA + 3 * kABytes;
   static constexpr uint32_t kTmemCols = 64;
@@ -103,6 +105,7 @@ __global__ void __launch_bounds__(MpnnTc::kThreads, 2)
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + C::oBar + 8);
   unsigned char* sB = smem + C::oB;
   unsigned char* sA = smem + C::oA;
+  float* sBias = reinterpret_cast<float*>(smem + C::oBias);
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
 
   if (t == 0) {
@@ -117,6 +120,7 @@ __global__ void __launch_bounds__(MpnnTc::kThreads, 2)
     const __nv_bfloat16* src = (k0 < C::kN ? Ws + c * C::kN + k0 : Wn + c * C::kN + (k0 - C::kN));
     *reinterpret_cast<uint4*>(sB + tc_off(c, k0)) = *reinterpret_cast<const uint4*>(src);
   }
+  if (t < C::kN) sBias[t] = __bfloat162float(bl[t]);
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
@@ -126,9 +130,6 @@ __global__ void __launch_bounds__(MpnnTc::kThreads, 2)
   const int row = t & 127, half = t >> 7;
   // epilogue: rows of the warp's lane quadrant, its half of the channels
   const int erow = (warp & 3) * 32 + lane, ecol = (warp >> 2) * 32;
-  float bias[32];
-#pragma unroll
-  for (int j = 0; j < 32; ++j) bias[j] = __bfloat162float(bl[ecol + j]);
   uint32_t phase = 0;
   bool ok = true;
   for (int64_t n0 = (int64_t)blockIdx.x * C::kRows; n0 < n && ok; n0 += (int64_t)gridDim.x * C::kRows) {
@@ -137,29 +138,48 @@ __global__ void __launch_bounds__(MpnnTc::kThreads, 2)
       const int64_t e = n0 + row;
       int64_t j[3] = {-1, -1, -1};
       if (e < n) neighbours(nbr, K, e, j);
+      // two chunks of 8 channels at a time, every load of both issued before use
 #pragma unroll 1
-      for (int cc = 0; cc < 4; ++cc) {
-        const int c0 = (half * 4 + cc) * 8;  // channels c0 .. c0 + 7
-        float hv[8], mv[8];
+      for (int cp = 0; cp < 2; ++cp) {
+        float4 hl[2][2], ml[2][3][2];
 #pragma unroll
-        for (int i = 0; i < 8; ++i) hv[i] = mv[i] = 0.0f;
-        if (e < n) {
-          const float4* hp = reinterpret_cast<const float4*>(h + e * C::kN + c0);
-          const float4 a = hp[0], b = hp[1];
-          hv[0] = a.x; hv[1] = a.y; hv[2] = a.z; hv[3] = a.w; hv[4] = b.x; hv[5] = b.y; hv[6] = b.z; hv[7] = b.w;
+        for (int u = 0; u < 2; ++u) {
+          const int c0 = (half * 4 + cp * 2 + u) * 8;  // channels c0 .. c0 + 7
+          const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+          hl[u][0] = hl[u][1] = z4;
+          if (e < n) {
+            const float4* hp = reinterpret_cast<const float4*>(h + e * C::kN + c0);
+            hl[u][0] = hp[0];
+            hl[u][1] = hp[1];
+          }
 #pragma unroll
-          for (int f = 0; f < 3; ++f)
+          for (int f = 0; f < 3; ++f) {
+            ml[u][f][0] = ml[u][f][1] = z4;
             if (j[f] >= 0) {
               const float4* mp = reinterpret_cast<const float4*>(h + j[f] * C::kN + c0);
-              const float4 u = mp[0], w = mp[1];
-              mv[0] += u.x; mv[1] += u.y; mv[2] += u.z; mv[3] += u.w;
-              mv[4] += w.x; mv[5] += w.y; mv[6] += w.z; mv[7] += w.w;
+              ml[u][f][0] = mp[0];
+              ml[u][f][1] = mp[1];
             }
+          }
         }
-        split3_store(hv, sA + tc_off(row, c0), sA + C::kABytes + tc_off(row, c0),
-                     sA + 2 * C::kABytes + tc_off(row, c0));
-        split3_store(mv, sA + tc_off(row, C::kN + c0), sA + C::kABytes + tc_off(row, C::kN + c0),
-                     sA + 2 * C::kABytes + tc_off(row, C::kN + c0));
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          const int c0 = (half * 4 + cp * 2 + u) * 8;
+          const float hv[8] = {hl[u][0].x, hl[u][0].y, hl[u][0].z, hl[u][0].w,
+                               hl[u][1].x, hl[u][1].y, hl[u][1].z, hl[u][1].w};
+          float mv[8];
+#pragma unroll
+          for (int q = 0; q < 2; ++q) {
+            mv[4 * q] = (ml[u][0][q].x + ml[u][1][q].x) + ml[u][2][q].x;
+            mv[4 * q + 1] = (ml[u][0][q].y + ml[u][1][q].y) + ml[u][2][q].y;
+            mv[4 * q + 2] = (ml[u][0][q].z + ml[u][1][q].z) + ml[u][2][q].z;
+            mv[4 * q + 3] = (ml[u][0][q].w + ml[u][1][q].w) + ml[u][2][q].w;
+          }
+          split3_store(hv, sA + tc_off(row, c0), sA + C::kABytes + tc_off(row, c0),
+                       sA + 2 * C::kABytes + tc_off(row, c0));
+          split3_store(mv, sA + tc_off(row, C::kN + c0), sA + C::kABytes + tc_off(row, C::kN + c0),
+                       sA + 2 * C::kABytes + tc_off(row, C::kN + c0));
+        }
       }
     }
     // generic-proxy stores of X -> visible to the tensor core's async proxy
@@ -196,8 +216,9 @@ __global__ void __launch_bounds__(MpnnTc::kThreads, 2)
       if (e < n) {
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
-          const float4 a = make_float4(v[4 * q] + bias[4 * q], v[4 * q + 1] + bias[4 * q + 1],
-                                       v[4 * q + 2] + bias[4 * q + 2], v[4 * q + 3] + bias[4 * q + 3]);
+          const float4 bq = *reinterpret_cast<const float4*>(sBias + ecol + 4 * q);
+          const float4 a = make_float4(v[4 * q] + bq.x, v[4 * q + 1] + bq.y, v[4 * q + 2] + bq.z,
+                                       v[4 * q + 3] + bq.w);
           if (a_out) *reinterpret_cast<float4*>(a_out + e * C::kN + ecol + 4 * q) = a;
           const float4 hh = *reinterpret_cast<const float4*>(h + e * C::kN + ecol + 4 * q);
           *reinterpret_cast<float4*>(hn + e * C::kN + ecol + 4 * q) =
