@@ -689,7 +689,8 @@ def measure_e2e(D32, bufs, res, flush, stream, t, dt, steps, ws, dofs, barrier):
     issued round robin on E2E_STREAMS CUDA streams: one step's copies overlap the
     others' kernels, as a host application streaming states through the library
     would run it.  The device buffers rotate through E2E_SETS sets (297 MB in all,
-    more than L2), so every step's kernels read their inputs from DRAM.  The same calls on
+    more than L2), so nothing a step reads stays in L2 from an earlier step except
+    what its own host-to-device copy has just written.  The same calls on
     one stream, one step after another with an L2 flush between steps, are
     reported as `serial`."""
     import torch

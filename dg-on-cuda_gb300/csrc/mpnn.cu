@@ -96,100 +96,6 @@ __global__ void __launch_bounds__(256) k_fwd_in(int64_t n, int npi, const __nv_b
   }
 }
 
-// One message-passing layer, a_out (pre-activations) optional.  Persistent
-// CTAs of 256 threads: the layer's weights are staged once as FP32
-// Wt[i][c] (i < 64: Ws, i >= 64: Wn), then per tile of 64 graph nodes the rows
-// [h | sum of neighbour h] are loaded with coalesced float4 loads into padded
-// node-major shared rows and each thread accumulates 4 nodes x 4 channels
-// (16 FMAs per two 16-byte shared loads, no bank conflicts).
-constexpr int kTileN = 64;
-constexpr int kXS = 2 * kW + 4;  // padded shared row: [h (64) | m (64) | pad]
-constexpr int kLayerSmem = (2 * kW * kW + kTileN * kXS) * 4;
-
-__device__ __forceinline__ float4 f4add(float4 a, float4 b) {
-  return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
-}
-
-__global__ void __launch_bounds__(256, 2) k_fwd_layer(int64_t n, int K, const int4* __restrict__ nbr,
-                                                      const __nv_bfloat16* __restrict__ Ws,
-                                                      const __nv_bfloat16* __restrict__ Wn,
-                                                      const __nv_bfloat16* __restrict__ bl,
-                                                      const float* __restrict__ h, float* __restrict__ a_out,
-                                                      float* __restrict__ hn) {
-  extern __shared__ float4 smem4[];
-  float* Wt = reinterpret_cast<float*>(smem4);  // [2 kW][kW]
-  float* X = Wt + 2 * kW * kW;                  // [kTileN][kXS]
-  const int t = threadIdx.x;
-  // weights: thread reads 8 consecutive inputs of one output channel, writes a column segment
-  for (int q = t; q < 2 * kW * (kW / 8); q += 256) {
-    const int mat = q / (kW * (kW / 8)), r = q % (kW * (kW / 8));
-    const int c = r % kW, i0 = (r / kW) * 8;
-    const __nv_bfloat16* src = (mat == 0 ? Ws : Wn) + c * kW + i0;
-    const uint4 raw = *reinterpret_cast<const uint4*>(src);
-    const __nv_bfloat16* v = reinterpret_cast<const __nv_bfloat16*>(&raw);
-#pragma unroll
-    for (int j = 0; j < 8; ++j) Wt[(mat * kW + i0 + j) * kW + c] = bf(v[j]);
-  }
-  const int cg = t & 15, ng = t >> 4;  // channels 4 cg .. 4 cg + 3, tile nodes 4 ng .. 4 ng + 3
-  float bias[4];
-#pragma unroll
-  for (int j = 0; j < 4; ++j) bias[j] = bf(bl[cg * 4 + j]);
-  const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
-  for (int64_t n0 = (int64_t)blockIdx.x * kTileN; n0 < n; n0 += (int64_t)gridDim.x * kTileN) {
-    __syncthreads();  // weights staged / previous tile's rows consumed
-    for (int q = t; q < kTileN * (kW / 4); q += 256) {
-      const int r = q / (kW / 4), c4 = q % (kW / 4);
-      const int64_t e = n0 + r;
-      float4 hv = zero, mv = zero;
-      if (e < n) {
-        hv = *reinterpret_cast<const float4*>(h + e * kW + c4 * 4);
-        int64_t j[3];
-        neighbours(nbr, K, e, j);
-#pragma unroll
-        for (int f = 0; f < 3; ++f)
-          if (j[f] >= 0) mv = f4add(mv, *reinterpret_cast<const float4*>(h + j[f] * kW + c4 * 4));
-      }
-      *reinterpret_cast<float4*>(X + r * kXS + c4 * 4) = hv;
-      *reinterpret_cast<float4*>(X + r * kXS + kW + c4 * 4) = mv;
-    }
-    __syncthreads();
-    float acc[4][4];
-#pragma unroll
-    for (int a = 0; a < 4; ++a)
-#pragma unroll
-      for (int j = 0; j < 4; ++j) acc[a][j] = bias[j];
-#pragma unroll 2
-    for (int i = 0; i < 2 * kW; i += 4) {
-      float4 xv[4];
-#pragma unroll
-      for (int a = 0; a < 4; ++a) xv[a] = *reinterpret_cast<const float4*>(X + (ng * 4 + a) * kXS + i);
-#pragma unroll
-      for (int ii = 0; ii < 4; ++ii) {
-        const float4 w = *reinterpret_cast<const float4*>(Wt + (i + ii) * kW + cg * 4);
-#pragma unroll
-        for (int a = 0; a < 4; ++a) {
-          const float xs = ii == 0 ? xv[a].x : ii == 1 ? xv[a].y : ii == 2 ? xv[a].z : xv[a].w;
-          acc[a][0] = fmaf(xs, w.x, acc[a][0]);
-          acc[a][1] = fmaf(xs, w.y, acc[a][1]);
-          acc[a][2] = fmaf(xs, w.z, acc[a][2]);
-          acc[a][3] = fmaf(xs, w.w, acc[a][3]);
-        }
-      }
-    }
-#pragma unroll
-    for (int a = 0; a < 4; ++a) {
-      const int64_t e = n0 + ng * 4 + a;
-      if (e < n) {
-        const float4 av = make_float4(acc[a][0], acc[a][1], acc[a][2], acc[a][3]);
-        if (a_out) *reinterpret_cast<float4*>(a_out + e * kW + cg * 4) = av;
-        const float4 hh = *reinterpret_cast<const float4*>(X + (ng * 4 + a) * kXS + cg * 4);
-        *reinterpret_cast<float4*>(hn + e * kW + cg * 4) =
-            make_float4(hh.x + fmaxf(av.x, 0.f), hh.y + fmaxf(av.y, 0.f), hh.z + fmaxf(av.z, 0.f),
-                        hh.w + fmaxf(av.w, 0.f));
-      }
-    }
-  }
-}
 
 // y = Wout h + bout; min(256 / npi, 16) nodes x npi outputs per block
 __global__ void __launch_bounds__(256) k_fwd_out(int64_t n, int npi, const __nv_bfloat16* __restrict__ Wout,
@@ -748,8 +654,6 @@ extern "C" int dgc_mpnn_create(dgc_handle h, int layers, uint64_t seed, dgc_mpnn
   if (e == cudaSuccess) e = cudaMemset(m->am, 0, P * 4);
   if (e == cudaSuccess) e = cudaMemset(m->av, 0, P * 4);
   if (e != cudaSuccess) return fail(mcuda(e, "mpnn set-up"));
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(dgk::k_fwd_layer, cudaFuncAttributeMaxDynamicSharedMemorySize, dgk::kLayerSmem);
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(dgk::k_fwd_layer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, dgk::MpnnTc::kSmem);
   if (e != cudaSuccess) return fail(mcuda(e, "mpnn set-up"));

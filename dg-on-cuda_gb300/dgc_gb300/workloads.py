@@ -17,7 +17,7 @@ skip count can be read off.
     stage_fp32   the autotuned FP32 stage kernel of the same workload
     batch        dg_batch_kernel: 24 seeded instances (advection / Maxwell TE / TM,
                  n in [8, 160], N in 2..8), each on its faster batch tile code
-    mpnn_fwd     k_fwd_layer: the 4-layer, width-64 network over a jittered
+    mpnn_fwd     k_fwd_layer_tc: the 4-layer, width-64 network over a jittered
                  128x128 mesh (K = 32768), N = 4
     bj_apply     k_bj_apply<float>: block-Jacobi application inside the two-level
                  mixed PCG, jittered 256x256 mesh (K = 131072), N = 4
@@ -102,7 +102,7 @@ def mpnn_fwd(reps: int):
     w[:] = np.random.default_rng(1).standard_normal(w.size).astype(np.float32) * 0.05
     net.set_weights(w)
     xin = torch.randn(D.K * D.NpP, dtype=torch.float32, device="cuda")
-    print(f"kernel: k_fwd_layer, warm-up forward passes 3, measured {reps}", flush=True)
+    print(f"kernel: k_fwd_layer_tc, warm-up forward passes 3, measured {reps}", flush=True)
     for _ in range(3):
         net.forward(xin)
     _sync()
