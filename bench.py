@@ -830,6 +830,48 @@ def measure_accuracy(dg, D32, D64, q_init, x, y, dt):
             "fp32_run_s": t32, "fp64_run_s": t64}
 
 
+def measure_advection(dg, meshes):
+    """The advection workload: jittered 32x32 mesh (K = 2048), N = 4, a = (1, 0.5),
+    Gaussian pulse exp(-((x+0.3)^2 + y^2)/0.02) with its exact translation as
+    inflow data, LSERK4 with dt = 0.5 min(h) / ((N+1)^2 |a|) to T = 0.5.  The L2
+    error against the exact pulse from the GPU (FP64 and compensated FP32,
+    graphed runs, device time of the whole run) and from the oracle (the serial
+    C port of the reference CPU operator, FP64, host time)."""
+    import torch
+    import oracle
+    N, T, ax, ay = 4, 0.5, 1.0, 0.5
+    m = meshes.jittered_square(32, SEED)
+    o = oracle.Oracle(m.xy, m.cells, N)
+    p = oracle.problem(oracle.ADVECTION, ax, ay, oracle.BC_GAUSS)
+    q0, ex = o.exact(p, 0.0), o.exact(p, T)
+    out = {"workload": "advection_gauss_k2048_n4_lserk4_t0.5", "num_cells": int(m.cells.shape[0]), "order": N}
+    stream = torch.cuda.current_stream()
+    for tag, prec in (("fp64", dg.F64), ("fp32c", dg.F32C)):
+        D = dg.Discretization(m, "advection", N, prec, ax=ax, ay=ay, bc=dg.BC_GAUSS)
+        dt0 = 0.5 * D.info.min_edge / ((N + 1) ** 2 * np.hypot(ax, ay))
+        ns = int(np.ceil(T / dt0))
+        qa, qb, r = D.upload(q0), D.empty_state(), D.empty_state()
+        D.lserk4_run(qa, qb, r, 0.0, T / ns, 20, graph=True)            # warm-up, graph capture
+        qa.copy_(D.upload(q0))
+        r.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fin = D.lserk4_run(qa, qb, r, 0.0, T / ns, ns, graph=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        D.check()
+        ms = e0.elapsed_time(e1)
+        out["steps"] = ns
+        out[tag] = {"rel_l2_vs_exact": float(np.linalg.norm(D.download(fin) - ex) / np.linalg.norm(ex)),
+                    "ms_to_t": ms, "gdofs": D.Np * D.K * 5 * ns / (ms * 1e-3) / 1e9}
+    t0 = time.perf_counter()
+    qo, _ = o.run(p, 1, 0.0, T / out["steps"], out["steps"], q0)   # scheme 1: LSERK4
+    cpu_s = time.perf_counter() - t0
+    out["oracle_cpu"] = {"rel_l2_vs_exact": float(np.linalg.norm(qo - ex) / np.linalg.norm(ex)), "seconds": cpu_s,
+                         "cores": 1}
+    return out
+
+
 EQ_MESHES = (16, 32, 64, 128)
 EQ_ORDERS = (2, 3, 4, 5, 6)
 EQ_TARGETS = (1e-4, 1e-5, 1e-6, 1e-7)
@@ -922,6 +964,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-instances comparison")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-preconditioner comparison")
     ap.add_argument("--no-stokes", action="store_true", help="skip the Stokes dual-splitting timing")
+    ap.add_argument("--no-advection", action="store_true", help="skip the advection (K = 2048) accuracy line")
     ap.add_argument("--no-equal-error", action="store_true", help="skip the accuracy-against-time sweep")
     ap.add_argument("--learned-full", action="store_true",
                     help="run only the learned-preconditioner workload over its whole 1600 / 400 sequence "
@@ -1061,6 +1104,9 @@ def main():
     learned = None
     if rank == 0 and not args.no_learned:
         learned = measure_learned(dg, meshes)
+    advection = None
+    if rank == 0 and not args.no_advection:
+        advection = measure_advection(dg, meshes)
     stokes = None
     if rank == 0 and not args.no_stokes:
         stokes = measure_stokes(dg, meshes)
@@ -1080,7 +1126,7 @@ def main():
                 "clocks": clocks, "fp64_plain": fp64, "fp32c": fp32c,
                 "speedup_mixed_vs_fp64": (value / ws / fp64["value"]) if fp64 else None,
                 "accuracy": accuracy, "poisson": poisson, "batched": batched, "learned_precond": learned,
-                "stokes": stokes, "equal_error": equal_error, "wall_s_timed_region": wall}
+                "stokes": stokes, "advection": advection, "equal_error": equal_error, "wall_s_timed_region": wall}
         print(json.dumps(line))
     if ws > 1:
         import torch.distributed as tdist
