@@ -319,7 +319,7 @@ def smooth_rhs(x, y, index: int, modes: int = 24):
 
 
 def measure_learned(dg, meshes, n_train=LEARN_TRAIN_SAMPLE, n_held=LEARN_HELD_SAMPLE, n_fp64=LEARN_FP64_HELD,
-                    snapshots=LEARN_SNAPSHOTS, full=False):
+                    snapshots=LEARN_SNAPSHOTS, full=False, activation="relu"):
     """Learned preconditioner on IPDG Poisson (Dirichlet, jittered 128x128 mesh,
     K = 32768, N = 4), in two-level form: M r = Binv r + P A_c^-1 P^T r + network,
     the coarse space a smoothed aggregation of LEARN_AGGREGATE cells.  Residual /
@@ -344,6 +344,8 @@ def measure_learned(dg, meshes, n_train=LEARN_TRAIN_SAMPLE, n_held=LEARN_HELD_SA
     D.block_jacobi()
     c = float(np.sqrt(D.K * D.Np))
     net = dg.MPNN(D, layers=4, seed=LEARN_SEED)
+    if activation == "linear":   # a fixed linear correction: flexible CG sees a fixed preconditioner
+        net.set_activation(dg.MPNN_ACT_LINEAR)
     bj = dg.MPNN(D, layers=1, seed=0)               # zero output layer: M(r) = Binv r + coarse
     # two-level form: the coarse space (smoothed aggregation) removes the smooth
     # mesh-wide error that a 4-hop network cannot see; the network learns the rest
@@ -450,7 +452,7 @@ def measure_learned(dg, meshes, n_train=LEARN_TRAIN_SAMPLE, n_held=LEARN_HELD_SA
                 "wall_s_p95": float(np.percentile(ts, 95)), "wall_s_total": float(np.sum(ts)),
                 "max_final_relres": float(max(r[2] for r in rows))}
 
-    out = {"workload": f"ipdg_poisson_dirichlet_k{D.K}_n{LEARN_ORDER}_learned_precond",
+    out = {"workload": f"ipdg_poisson_dirichlet_k{D.K}_n{LEARN_ORDER}_learned_precond", "activation": activation,
            "num_cells": D.K, "order": LEARN_ORDER, "rtol": 1e-10,
            "sequence": {"solves": LEARN_TRAIN + LEARN_HELD, "train": LEARN_TRAIN, "held_out": LEARN_HELD,
                         "rhs": "24 Fourier modes, amplitudes ~ N(0, |k|^-2), seeded per solve"},
@@ -966,6 +968,8 @@ def main():
     ap.add_argument("--no-stokes", action="store_true", help="skip the Stokes dual-splitting timing")
     ap.add_argument("--no-advection", action="store_true", help="skip the advection (K = 2048) accuracy line")
     ap.add_argument("--no-equal-error", action="store_true", help="skip the accuracy-against-time sweep")
+    ap.add_argument("--learned-activation", default="relu", choices=["relu", "linear"],
+                    help="hidden-layer activation of the learned preconditioner's network")
     ap.add_argument("--learned-full", action="store_true",
                     help="run only the learned-preconditioner workload over its whole 1600 / 400 sequence "
                          "(about a quarter of an hour) and print its section as one JSON line")
@@ -979,7 +983,7 @@ def main():
         from dgc_gb300 import meshes
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         out = measure_learned(dg, meshes, n_train=LEARN_TRAIN, n_held=LEARN_HELD, n_fp64=40,
-                              snapshots=(4, 16, 64), full=True)
+                              snapshots=(4, 16, 64), full=True, activation=args.learned_activation)
         print(json.dumps({"learned_precond_full": out}))
         return None
 
@@ -1103,7 +1107,7 @@ def main():
             batched["cpu_baseline"] = cpu_batched_baseline()
     learned = None
     if rank == 0 and not args.no_learned:
-        learned = measure_learned(dg, meshes)
+        learned = measure_learned(dg, meshes, activation=args.learned_activation)
     advection = None
     if rank == 0 and not args.no_advection:
         advection = measure_advection(dg, meshes)

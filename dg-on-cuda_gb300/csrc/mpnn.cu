@@ -234,11 +234,11 @@ __global__ void k_gather(int64_t n, int K, const int4* __restrict__ nbr, const f
   }
 }
 
-// g = dh * (a > 0)
+// g = dh * (a > 0), or g = dh for the linear network
 __global__ void k_relu_bwd(int64_t n, const float* __restrict__ dh, const float* __restrict__ a,
-                           float* __restrict__ g) {
+                           float* __restrict__ g, int linear) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    g[i] = a[i] > 0.0f ? dh[i] : 0.0f;
+    g[i] = (linear || a[i] > 0.0f) ? dh[i] : 0.0f;
 }
 
 // gW[o][i] += sum_e gout[e][o] xin[e][i], gb[o] += sum_e gout[e][o]; nout, nin <= 64.
@@ -431,6 +431,7 @@ struct dgc_mpnn_s {
   float *y = nullptr, *dy = nullptr, *dh0 = nullptr, *dh1 = nullptr, *g = nullptr, *m = nullptr;
   float *sd = nullptr, *tm = nullptr, *st = nullptr;  // energy loss: S d, masked t, S t
   int loss_kind = DGC_MPNN_LOSS_ENERGY;
+  int linear = 0;                // DGC_MPNN_ACT_LINEAR: no ReLU, biases held at zero
   bool coarse = false;           // add the handle's coarse-space correction to Binv r
   double* scal = nullptr;        // training: [0] loss, [1..] per-sample target norms; solver: dot products
   double* h_scal = nullptr;      // pinned
@@ -572,7 +573,7 @@ int forward(dgc_mpnn m, int64_t n, const float* x, float* y, float* ha, float* h
     dgk::k_nbr_sum<<<grid_for(m, n * (dgk::kW / 4), 256), 256, 0, s>>>(n, K, nbr, cur, m->msum);
     dgk::k_fwd_layer_tc<<<tiles, dgk::MpnnTc::kThreads, dgk::MpnnTc::kSmem, s>>>(
         n, m->w16 + L.oWs(l), m->w16 + L.oWn(l), m->w16 + L.ob(l), cur, m->msum, store ? m->as[l] : nullptr, nxt,
-        m->h->d_status);
+        m->linear, m->h->d_status);
     CKM(cudaGetLastError());
     cur = nxt;
   }
@@ -738,6 +739,29 @@ extern "C" int dgc_mpnn_forward(dgc_mpnn m, const float* x, float* y, void* stre
   return forward(m, m->h->K, x, y, m->ph0, m->ph1, false, static_cast<cudaStream_t>(stream));
 }
 
+// zero the bias entries of a parameter-sized vector (weights or gradients)
+static int zero_biases(dgc_mpnn m, float* v, cudaStream_t s) {
+  const auto& L = m->lay;
+  CKM(cudaMemsetAsync(v + L.obin, 0, dgk::kW * 4, s));
+  for (int l = 0; l < L.L; ++l) CKM(cudaMemsetAsync(v + L.ob(l), 0, dgk::kW * 4, s));
+  CKM(cudaMemsetAsync(v + L.obout, 0, (size_t)L.npi * 4, s));
+  return DGC_OK;
+}
+
+extern "C" int dgc_mpnn_set_activation(dgc_mpnn m, int kind) {
+  if (!m) return merr(DGC_ERR_ARG, "null network");
+  if (kind != DGC_MPNN_ACT_RELU && kind != DGC_MPNN_ACT_LINEAR) return merr(DGC_ERR_ARG, "unknown activation");
+  m->linear = kind == DGC_MPNN_ACT_LINEAR;
+  if (m->linear) {
+    if (int rc = zero_biases(m, m->w, 0)) return rc;
+    const auto& L = m->lay;
+    dgk::k_to_bf16<<<grid_for(m, L.total, 256), 256>>>(L.total, m->w, m->w16);
+    CKM(cudaGetLastError());
+    CKM(cudaDeviceSynchronize());
+  }
+  return DGC_OK;
+}
+
 extern "C" int dgc_mpnn_train_step(dgc_mpnn m, const float* x, const float* t, int S, float lr, float* loss,
                                    float* grad_out, void* stream) {
   if (!m || !x || !t || S <= 0) return merr(DGC_ERR_ARG, "null argument or no samples");
@@ -780,7 +804,7 @@ extern "C" int dgc_mpnn_train_step(dgc_mpnn m, const float* x, const float* t, i
   float* dh = m->dh0;
   float* dhp = m->dh1;
   for (int l = L.L - 1; l >= 0; --l) {
-    dgk::k_relu_bwd<<<grid_for(m, n * dgk::kW, 256), 256, 0, s>>>(n * dgk::kW, dh, m->as[l], m->g);
+    dgk::k_relu_bwd<<<grid_for(m, n * dgk::kW, 256), 256, 0, s>>>(n * dgk::kW, dh, m->as[l], m->g, m->linear);
     dgk::k_grad_dense<<<grid_for(m, n, 32), 256, 0, s>>>(n, dgk::kW, dgk::kW, m->g, m->hs[l], m->grad + L.oWs(l),
                                                          m->grad + L.ob(l));
     dgk::k_gather<<<grid_for(m, n * dgk::kW, 256), 256, 0, s>>>(n, K, nbr, m->hs[l], m->m);
@@ -794,6 +818,9 @@ extern "C" int dgc_mpnn_train_step(dgc_mpnn m, const float* x, const float* t, i
   dgk::k_grad_dense<<<grid_for(m, n, 32), 256, 0, s>>>(n, dgk::kW, npi, dh, x, m->grad + L.oWin, m->grad + L.obin);
   CKM(cudaGetLastError());
   m->h->launches += 3 + 5 * L.L;  // output grads, 5 per layer, input grads
+  if (m->linear) {  // the biases stay at zero: the network remains a linear map
+    if (int rc = zero_biases(m, m->grad, s)) return rc;
+  }
   if (grad_out) CKM(cudaMemcpyAsync(grad_out, m->grad, L.total * 4, cudaMemcpyDeviceToDevice, s));
   if (lr > 0.0f) {
     ++m->step;

@@ -3,7 +3,7 @@
 //
 // Per graph node e the layer computes
 //   a_e = Ws h_e + Wn m_e + b,   m_e = sum of h over the face neighbours of e,
-//   h'_e = h_e + relu(a_e),
+//   h'_e = h_e + relu(a_e)   (or h_e + a_e for the linear network),
 // i.e. for a tile of 128 nodes the product D[128 x 64] = X[128 x 128] W^T with
 // X = [h | m] (FP32) and W = [Ws | Wn] (64 x 128, BF16 copies of the FP32
 // master weights).  W is exact in BF16; X is not, so X is split into three
@@ -123,7 +123,7 @@ __global__ void __launch_bounds__(MpnnTc::kThreads, 2)
     k_fwd_layer_tc(int64_t n, const __nv_bfloat16* __restrict__ Ws, const __nv_bfloat16* __restrict__ Wn,
                    const __nv_bfloat16* __restrict__ bl, const float* __restrict__ h,
                    const float* __restrict__ msum, float* __restrict__ a_out, float* __restrict__ hn,
-                   int* __restrict__ status) {
+                   int linear, int* __restrict__ status) {
   using C = MpnnTc;
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem + C::oBar);
@@ -230,8 +230,9 @@ __global__ void __launch_bounds__(MpnnTc::kThreads, 2)
           if (a_out) *reinterpret_cast<float4*>(a_out + e * C::kN + ecol + 4 * q) = a;
           const float4 hh = *reinterpret_cast<const float4*>(h + e * C::kN + ecol + 4 * q);
           *reinterpret_cast<float4*>(hn + e * C::kN + ecol + 4 * q) =
-              make_float4(hh.x + fmaxf(a.x, 0.f), hh.y + fmaxf(a.y, 0.f), hh.z + fmaxf(a.z, 0.f),
-                          hh.w + fmaxf(a.w, 0.f));
+              linear ? make_float4(hh.x + a.x, hh.y + a.y, hh.z + a.z, hh.w + a.w)
+                     : make_float4(hh.x + fmaxf(a.x, 0.f), hh.y + fmaxf(a.y, 0.f), hh.z + fmaxf(a.z, 0.f),
+                                   hh.w + fmaxf(a.w, 0.f));
         }
       }
     }

@@ -25,6 +25,7 @@ TAU_ONE, TAU_SCALED = 0, 1
 LAYOUT_NATIVE, LAYOUT_REF_CPU, LAYOUT_REF_GPU = 0, 1, 2
 OP_DR_WEAK, OP_DS_WEAK, OP_LIFT, OP_DR_STRONG, OP_DS_STRONG, OP_MASS, OP_V = range(7)
 MPNN_LOSS_L2, MPNN_LOSS_ENERGY = 0, 1
+MPNN_ACT_RELU, MPNN_ACT_LINEAR = 0, 1
 PHYSICS = {"advection": ADVECTION, "maxwell_tm": MAXWELL_TM, "maxwell_te": MAXWELL_TE, "laplace": LAPLACE}
 
 
@@ -157,6 +158,7 @@ def lib():
             L.dgc_mpnn_train_step.argtypes = [_vp, _vp, _vp, C.c_int, C.c_float, C.POINTER(C.c_float), _vp, _vp]
             L.dgc_mpnn_forward.argtypes = [_vp, _vp, _vp, _vp]
             L.dgc_mpnn_set_loss.argtypes = [_vp, C.c_int]
+            L.dgc_mpnn_set_activation.argtypes = [_vp, C.c_int]
             L.dgc_mpnn_set_coarse.argtypes = [_vp, C.c_int, _vp]
             L.dgc_coarse_build.argtypes = [_vp, C.c_int, _vp]
             L.dgc_coarse_apply.argtypes = [_vp, _vp, _vp, C.c_int, _vp]
@@ -708,6 +710,10 @@ class MPNN:
         """MPNN_LOSS_ENERGY (default: |d|_S^2 / |t|_S^2) or MPNN_LOSS_L2 (|d|^2 / |t|^2)."""
         _check(lib().dgc_mpnn_set_loss(self._h, kind))
 
+
+    def set_activation(self, kind: int):
+        """MPNN_ACT_RELU (default) or MPNN_ACT_LINEAR (no ReLU, biases zero and held there)."""
+        _check(lib().dgc_mpnn_set_activation(self._h, kind))
     def get_weights(self) -> np.ndarray:
         w = np.zeros(self.num_params, dtype=np.float32)
         _check(lib().dgc_mpnn_get_weights(self._h, w.ctypes.data))

@@ -382,6 +382,13 @@ int dgc_mpnn_set_weights(dgc_mpnn m, const float* host_in);
  *   DGC_MPNN_LOSS_L2: mean_s |d_s|^2 / |t_s|^2. */
 enum { DGC_MPNN_LOSS_L2 = 0, DGC_MPNN_LOSS_ENERGY = 1 };
 int dgc_mpnn_set_loss(dgc_mpnn m, int kind);
+/* Activation of the hidden layers: DGC_MPNN_ACT_RELU (default) or
+ * DGC_MPNN_ACT_LINEAR (no ReLU, and every bias set to and held at zero during
+ * training).  The linear network is a fixed linear map of its input, and with
+ * it the preconditioner's correction (|r|/c) net(c r/|r|) = net(r) is linear in
+ * r, so flexible CG sees a fixed preconditioner. */
+enum { DGC_MPNN_ACT_RELU = 0, DGC_MPNN_ACT_LINEAR = 1 };
+int dgc_mpnn_set_activation(dgc_mpnn m, int kind);
 /* Loss and gradients on `samples` field pairs (device, FP32, native layout,
  * samples x K x NpP each): x the network inputs, t the targets.  grad_out
  * (device, num_params floats) receives d loss / d weights (may be NULL);

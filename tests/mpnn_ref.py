@@ -50,8 +50,8 @@ def neighbour_sum(h, nbr, K):
     return m
 
 
-def forward(w, x, nbr, K, npi, L):
-    """x: (S*K, npi) -> y (S*K, npi) and the activations."""
+def forward(w, x, nbr, K, npi, L, linear=False):
+    """x: (S*K, npi) -> y (S*K, npi) and the activations (linear: no ReLU)."""
     P = unpack(w, npi, L)
     hs = [x @ P["Win"].T + P["bin"]]
     acts = []
@@ -60,17 +60,18 @@ def forward(w, x, nbr, K, npi, L):
         m = neighbour_sum(h, nbr, K)
         a = h @ P["Ws"][l].T + m @ P["Wn"][l].T + P["b"][l]
         acts.append(a)
-        hs.append(h + np.maximum(a, 0.0))
+        hs.append(h + (a if linear else np.maximum(a, 0.0)))
     y = hs[-1] @ P["Wout"].T + P["bout"]
     return y, hs, acts, P
 
 
-def loss_and_grad(w, x, t, nbr, K, npi, np_valid, L, spd=None):
+def loss_and_grad(w, x, t, nbr, K, npi, np_valid, L, spd=None, linear=False):
     """Loss = mean over samples of |y - t|^2 / |t|^2 on valid nodes, or with
     spd (a symmetric operator on one (K, npi) field, padding zero) the energy
-    form d.S d / t.S t; returns (loss, flat gradient)."""
+    form d.S d / t.S t; returns (loss, flat gradient).  linear: the network
+    without ReLU, whose bias gradients are zero (the biases are held at zero)."""
     S = x.shape[0] // K
-    y, hs, acts, P = forward(w, x, nbr, K, npi, L)
+    y, hs, acts, P = forward(w, x, nbr, K, npi, L, linear)
     mask = np.zeros(npi)
     mask[:np_valid] = 1.0
     dy = np.zeros_like(y)
@@ -93,7 +94,7 @@ def loss_and_grad(w, x, t, nbr, K, npi, np_valid, L, spd=None):
     gWs, gWn, gb = [None] * L, [None] * L, [None] * L
     for l in range(L - 1, -1, -1):
         h = hs[l]
-        gg = dh * (acts[l] > 0.0)
+        gg = dh if linear else dh * (acts[l] > 0.0)
         m = neighbour_sum(h, nbr, K)
         gWs[l] = gg.T @ h
         gWn[l] = gg.T @ m
@@ -105,4 +106,7 @@ def loss_and_grad(w, x, t, nbr, K, npi, np_valid, L, spd=None):
     for l in range(L):
         flat += [gWs[l].ravel(), gWn[l].ravel(), gb[l]]
     flat += [g["Wout"].ravel(), g["bout"]]
+    if linear:  # bin, the per-layer b and bout
+        for i in [1] + [4 + 3 * l for l in range(L)] + [len(flat) - 1]:
+            flat[i] = np.zeros_like(flat[i])
     return loss, np.concatenate(flat)

@@ -25,10 +25,12 @@ def relerr(a, b):
     return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
 
 
+@pytest.mark.parametrize("act", ["relu", "linear"])
 @pytest.mark.parametrize("kind", ["l2", "energy"])
-def test_forward_loss_and_gradients_match_numpy(kind):
+def test_forward_loss_and_gradients_match_numpy(kind, act):
     m = meshes.jittered_square(4, 21)   # K = 32
     N, L, S = 2, 2, 2
+    linear = act == "linear"
     D = dg.Discretization(m, "laplace", N, dg.F64, tau=dg.TAU_SCALED, dirichlet=True)
     net = dg.MPNN(D, layers=L, seed=3)
     net.set_loss(dg.MPNN_LOSS_L2 if kind == "l2" else dg.MPNN_LOSS_ENERGY)
@@ -43,6 +45,10 @@ def test_forward_loss_and_gradients_match_numpy(kind):
     assert not np.any(w[-(npi * 64 + npi):])   # the output layer starts at zero
     w = (rng.standard_normal(w.size) * 0.2).astype(np.float32)   # every block then carries gradient
     net.set_weights(w)
+    if linear:
+        net.set_activation(dg.MPNN_ACT_LINEAR)   # zeroes the biases
+        w = net.get_weights()
+        assert not np.any(w[npi * 64:npi * 64 + 64])   # bin
     xd = torch.from_numpy(x).cuda().reshape(-1)
     td = torch.from_numpy(t).cuda().reshape(-1)
     loss, grad = net.train_step(xd, td, lr=0.0, want_grad=True)
@@ -51,18 +57,27 @@ def test_forward_loss_and_gradients_match_numpy(kind):
         return D.spd(torch.from_numpy(np.ascontiguousarray(v).reshape(-1)).cuda()).cpu().numpy().reshape(K, npi)
 
     loss_ref, grad_ref = mpnn_ref.loss_and_grad(w, x.astype(np.float64), t.astype(np.float64), nbr, K, npi, Np, L,
-                                                spd=spd if kind == "energy" else None)
+                                                spd=spd if kind == "energy" else None, linear=linear)
     assert abs(loss - loss_ref) / loss_ref < 1e-5
     assert relerr(grad.cpu().numpy(), grad_ref) < 1e-4
     # per-parameter-block agreement (every block carries gradient)
     g = grad.cpu().numpy()
     o = 0
     for size in [64 * npi, 64] + [64 * 64, 64 * 64, 64] * L + [npi * 64, npi]:
-        assert relerr(g[o:o + size], grad_ref[o:o + size]) < 1e-3, o
+        if linear and size in (64, npi) and not np.any(grad_ref[o:o + size]):
+            assert not np.any(g[o:o + size]), o      # bias gradients held at zero
+        else:
+            assert relerr(g[o:o + size], grad_ref[o:o + size]) < 1e-3, o
         o += size
     y = net.forward(torch.from_numpy(x[:K]).cuda().reshape(-1)).cpu().numpy().reshape(K, npi)
-    y_ref = mpnn_ref.forward(w, x[:K].astype(np.float64), nbr, K, npi, L)[0]
+    y_ref = mpnn_ref.forward(w, x[:K].astype(np.float64), nbr, K, npi, L, linear)[0]
     assert relerr(y, y_ref) < 1e-5
+    if linear:  # a linear map: net(2x - x') = 2 net(x) - net(x')
+        x2 = rng.standard_normal((K, npi)).astype(np.float32)
+        x2[:, Np:] = 0.0
+        f = lambda v: net.forward(torch.from_numpy(np.ascontiguousarray(v)).cuda().reshape(-1)).cpu().numpy()  # noqa
+        lhs = f((2.0 * x[:K] - x2).astype(np.float32))
+        assert relerr(lhs, 2.0 * f(x[:K]) - f(x2)) < 1e-5
 
 
 def test_forward_many_tiles_matches_numpy():
