@@ -52,7 +52,6 @@ STAGE_KERNELS = {
     7: "dgk::dg_rhs_blk_kernel<6,PHYS_TE,1> (warp-uniform operator loads)",
     8: "dgk::dg_rhs_tct_kernel<6,PHYS_TE> (tcgen05, A in TMEM, split TF32)",
     9: "dgk::dg_rhs_tcp_kernel<6,PHYS_TE> (tcgen05, A in TMEM, warp-specialized pipeline)",
-    10: "dgk::dg_rhs_blk_kernel<6,PHYS_TE,1,2> (warp-uniform operator loads, residual read in the epilogue)",
 }
 
 

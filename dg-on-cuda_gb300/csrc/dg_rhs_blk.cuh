@@ -21,10 +21,7 @@
 //      covers ~32/NG elements and reads NG different operator chunks);
 //   1: a warp holds one node group of 32 consecutive elements, so every
 //      operator load is warp-uniform (a broadcast) and the 32 element rows of
-//      a state load fall in distinct banks when NG is odd;
-//   2: mapping 1 in a lean form: the LSERK residual is read in the epilogue
-//      instead of being bulk-copied with the tile, which frees the shared
-//      memory for a fourth CTA per SM (registers capped accordingly).
+//      a state load fall in distinct banks when NG is odd.
 // Tiles are double-buffered: the bulk copy of the next tile (state, residual,
 // geometry, neighbours) is in flight while the current one is computed.
 #pragma once
@@ -37,12 +34,11 @@ template <int N, int P, int EPT_, int MAP_ = 0>
 struct BlkConfig {
   using O = Order<N>;
   static constexpr int Np = O::Np, NpP = O::NpP, NFACE = O::Nface;
-  static constexpr int EPT = EPT_, MAP = MAP_ == 0 ? 0 : 1;  // thread mapping
-  static constexpr bool kLean = MAP_ == 2;
+  static constexpr int EPT = EPT_, MAP = MAP_;
   static constexpr int NG = NpP / 4;                 // 4-node groups per element
   static constexpr int RW = (8 / NG) > 0 ? 8 / NG : 1;  // MAP 1: rows of 32 elements per CTA
   static constexpr int kThreads = MAP == 0 ? 256 : NG * 32 * RW;
-  static constexpr int kMinBlocks = EPT == 2 ? 2 : (kLean ? 4 : 3);
+  static constexpr int kMinBlocks = EPT == 2 ? 2 : 3;
   static constexpr int NTE = MAP == 0 ? kThreads / NG : 32 * RW;  // element slots per CTA
   static constexpr int TE = NTE * EPT;               // elements per tile
   static constexpr int Nf = PhysTraits<P>::Nf;
@@ -53,7 +49,7 @@ struct BlkConfig {
   static constexpr uint32_t kMat = KB * NpP * 4;
   // the LSERK residual tile is prefetched with the state tile when the extra
   // buffers keep the CTA count per SM (one element per thread)
-  static constexpr bool kAuxTile = EPT == 1 && !kLean;
+  static constexpr bool kAuxTile = EPT == 1;
   static constexpr uint32_t kQ = TE * ESTR * 4, kA = kAuxTile ? kQ : 0, kG = TE * 16 * 4, kN = TE * 16;
   static constexpr uint32_t kBuf = kQ + kA + kG + kN;  // one tile buffer: state | residual | geometry | neighbours
   static constexpr uint32_t oBar = 0;

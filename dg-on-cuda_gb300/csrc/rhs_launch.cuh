@@ -247,12 +247,10 @@ cudaError_t rhs_blk(const RhsParams* p, int sm_count, cudaStream_t s, LaunchInfo
 // (dg_rhs_blk_kernel, mapping 0), 7 = 4-node x 1 element blocks with
 // warp-uniform operator loads (mapping 1), 8 = tensor cores with the A operand
 // in TMEM (dg_rhs_tct_kernel), 9 = its warp-specialized pipelined form
-// (dg_rhs_tcp_kernel, Maxwell; advection runs variant 8), 10 = mapping 1 in
-// its lean form (residual read in the epilogue, 4 CTAs per SM).  Orders 7, 8:
-// 0 = dg_rhs_kernel, 1, 2, 3 = dg_rhs_blk_kernel (EPT 1, EPT 2, mapping 1),
-// 4 = the lean mapping-1 form.
-constexpr int kF32Variants = 11;
-constexpr int kF32VariantsHigh = 5;
+// (dg_rhs_tcp_kernel, Maxwell; advection runs variant 8).  Orders 7, 8: 0 =
+// dg_rhs_kernel, 1, 2, 3 = dg_rhs_blk_kernel (EPT 1, EPT 2, mapping 1).
+constexpr int kF32Variants = 10;
+constexpr int kF32VariantsHigh = 4;
 
 template <int N, int P>
 cudaError_t rhs_f32_variant(int v, const RhsParams* p, int sm, cudaStream_t s, LaunchInfo* info) {
@@ -265,12 +263,10 @@ cudaError_t rhs_f32_variant(int v, const RhsParams* p, int sm, cudaStream_t s, L
     if (v == 7) return rhs_blk<N, P, 1, 1>(p, sm, s, info);
     if (v == 8) return rhs_tct<N, P>(p, sm, s, info);
     if (v == 9) return rhs_tcp<N, P>(p, sm, s, info);
-    if (v == 10) return rhs_blk<N, P, 1, 2>(p, sm, s, info);
   } else {
     if (v == 1) return rhs_blk<N, P, 1, 0>(p, sm, s, info);
     if (v == 2) return rhs_blk<N, P, 2, 0>(p, sm, s, info);
     if (v == 3) return rhs_blk<N, P, 1, 1>(p, sm, s, info);
-    if (v == 4) return rhs_blk<N, P, 1, 2>(p, sm, s, info);
   }
   return cudaErrorInvalidValue;
 }

@@ -39,7 +39,7 @@ def test_every_variant_matches_oracle(N, phys, kind):
     q0 = o.exact(p, 0.07)
     ref = o.rhs(p, 0.07, q0)
     nv = D.num_variants()
-    assert nv == (11 if N <= 6 else 5)
+    assert nv == (10 if N <= 6 else 4)
     q = D.upload(q0)
     for v in range(nv):
         D.set_variant(v)
