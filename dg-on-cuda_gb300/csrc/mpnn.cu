@@ -442,9 +442,6 @@ struct dgc_mpnn_s {
   static constexpr int kMaxWindow = 8;
   double* pv[kMaxWindow + 1] = {};  // direction ring p_i, i mod (window + 1)
   double* qv[kMaxWindow + 1] = {};  // S p_i
-  // neighbour sums m of the layer inputs (forward), for up to msum_cap graph nodes
-  float* msum = nullptr;
-  int64_t msum_cap = 0;
 };
 
 namespace {
@@ -525,16 +522,6 @@ int ensure_train(dgc_mpnn m, int S) {
   return ensure_scal(m, 1 + 3 * S);
 }
 
-int ensure_msum(dgc_mpnn m, int64_t n) {
-  if (n <= m->msum_cap) return DGC_OK;
-  cudaFree(m->msum);
-  m->msum = nullptr;
-  m->msum_cap = 0;
-  CKM(zalloc(&m->msum, (size_t)n * dgk::kW));
-  m->msum_cap = n;
-  return DGC_OK;
-}
-
 int ensure_apply(dgc_mpnn m) {
   if (m->px) return DGC_OK;
   const size_t nW = (size_t)m->h->K * dgk::kW, nY = field_len(m);
@@ -562,7 +549,6 @@ int forward(dgc_mpnn m, int64_t n, const float* x, float* y, float* ha, float* h
   const int4* nbr = reinterpret_cast<const int4*>(m->h->d_nbr);
   const int K = m->h->K;
   float* cur = store ? m->hs[0] : ha;
-  if (int rc = ensure_msum(m, n)) return rc;
   dgk::k_fwd_in<<<grid_for(m, n, 4), 256, 0, s>>>(n, L.npi, m->w16 + L.oWin, m->w16 + L.obin, x, cur);
   CKM(cudaGetLastError());
   for (int l = 0; l < L.L; ++l) {
@@ -570,9 +556,8 @@ int forward(dgc_mpnn m, int64_t n, const float* x, float* y, float* ha, float* h
     // tensor-core layer (mpnn_tc.cuh): persistent CTAs over 128-node tiles, 2 per SM
     const int tiles = (int)std::min<int64_t>((n + dgk::MpnnTc::kRows - 1) / dgk::MpnnTc::kRows,
                                              (int64_t)m->sm_count * 2);
-    dgk::k_nbr_sum<<<grid_for(m, n * (dgk::kW / 4), 256), 256, 0, s>>>(n, K, nbr, cur, m->msum);
     dgk::k_fwd_layer_tc<<<tiles, dgk::MpnnTc::kThreads, dgk::MpnnTc::kSmem, s>>>(
-        n, m->w16 + L.oWs(l), m->w16 + L.oWn(l), m->w16 + L.ob(l), cur, m->msum, store ? m->as[l] : nullptr, nxt,
+        n, K, nbr, m->w16 + L.oWs(l), m->w16 + L.oWn(l), m->w16 + L.ob(l), cur, store ? m->as[l] : nullptr, nxt,
         m->linear, m->h->d_status);
     CKM(cudaGetLastError());
     cur = nxt;
@@ -580,7 +565,7 @@ int forward(dgc_mpnn m, int64_t n, const float* x, float* y, float* ha, float* h
   const int per = std::min(256 / L.npi, 16);
   dgk::k_fwd_out<<<grid_for(m, n, per), 256, 0, s>>>(n, L.npi, m->w16 + L.oWout, m->w16 + L.obout, cur, y);
   CKM(cudaGetLastError());
-  m->h->launches += 2 * L.L + 2;
+  m->h->launches += L.L + 2;
   return DGC_OK;
 }
 
@@ -683,7 +668,7 @@ extern "C" int dgc_mpnn_destroy(dgc_mpnn m) {
   if (!m) return DGC_OK;
   for (float* p : {m->w, m->grad, m->am, m->av, m->y, m->dy, m->dh0, m->dh1, m->g, m->m, m->sd, m->tm, m->st,
                    m->px, m->ph0, m->ph1,
-                   m->py, m->msum})
+                   m->py})
     cudaFree(p);
   for (auto p : m->hs) cudaFree(p);
   for (auto p : m->as) cudaFree(p);

@@ -12,22 +12,22 @@
 // accumulating products per K step.  The result matches the FP32 SIMT form of
 // the same layer to FP32 accumulation round-off.
 //
-// The neighbour sums m are formed first by k_nbr_sum (one thread per node and
-// 4 channels, a gather from L2), so that the tile kernel reads two contiguous
-// rows per node and has no dependent index load in front of its data loads.
-//
 // CTA: 256 threads, one 128-node tile at a time (persistent over tiles).
 //   * W is staged once per CTA in shared memory (K-major, no swizzle, core
 //     matrices of 8 rows x 16 bytes: element (row, k) at byte
 //     (row / 8) * 2048 + (k / 8) * 128 + (row % 8) * 16 + (k % 8) * 2);
-//   * two threads per tile row load h_e and m_e (all 16 float4 loads of the
-//     thread in flight at once), split and store the three X parts in the
-//     same layout;
+//   * two threads per tile row gather h_e and the neighbour rows (float4
+//     loads, two 8-channel chunks in flight at a time), sum, split and store
+//     the three X parts in the same layout;
 //   * one thread issues 8 K steps x 3 MMAs (M = 128, N = 64, K = 16) into 64
 //     TMEM columns and commits to an mbarrier (bounded wait);
 //   * the epilogue: warp w reads TMEM lanes 32 (w % 4) .. + 31 (its rows),
 //     columns 32 (w / 4) .. + 31, adds the bias, writes a (optional) and h'.
 // Shared memory 112 KB + barriers: 2 CTAs per SM; TMEM 64 columns per CTA.
+// (Forming the neighbour sums in a separate gather kernel first, so that this
+// kernel reads two contiguous rows per node, was measured: 22.5 us for this
+// kernel plus the gather, 6 % slower per network application than the fused
+// gather here.)
 #pragma once
 
 #include <cuda_bf16.h>
@@ -98,31 +98,10 @@ __device__ __forceinline__ void split3_store(const float (&v)[8], unsigned char*
   *reinterpret_cast<uint4*>(a2) = *reinterpret_cast<const uint4*>(p[2]);
 }
 
-// m_e = sum of h over the face neighbours of e (the three summands in face
-// order), one float4 of channels per thread
-__global__ void __launch_bounds__(256) k_nbr_sum(int64_t n, int K, const int4* __restrict__ nbr,
-                                                 const float* __restrict__ h, float* __restrict__ m) {
-  constexpr int kC4 = MpnnTc::kN / 4;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n * kC4; i += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t e = i / kC4;
-    const int c4 = (int)(i - e * kC4);
-    int64_t j[3];
-    neighbours(nbr, K, e, j);
-    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-#pragma unroll
-    for (int f = 0; f < 3; ++f)
-      if (j[f] >= 0) {
-        const float4 v = __ldg(reinterpret_cast<const float4*>(h + j[f] * MpnnTc::kN) + c4);
-        acc.x += v.x; acc.y += v.y; acc.z += v.z; acc.w += v.w;
-      }
-    reinterpret_cast<float4*>(m + e * MpnnTc::kN)[c4] = acc;
-  }
-}
-
 __global__ void __launch_bounds__(MpnnTc::kThreads, 2)
-    k_fwd_layer_tc(int64_t n, const __nv_bfloat16* __restrict__ Ws, const __nv_bfloat16* __restrict__ Wn,
-                   const __nv_bfloat16* __restrict__ bl, const float* __restrict__ h,
-                   const float* __restrict__ msum, float* __restrict__ a_out, float* __restrict__ hn,
+    k_fwd_layer_tc(int64_t n, int K, const int4* __restrict__ nbr, const __nv_bfloat16* __restrict__ Ws,
+                   const __nv_bfloat16* __restrict__ Wn, const __nv_bfloat16* __restrict__ bl,
+                   const float* __restrict__ h, float* __restrict__ a_out, float* __restrict__ hn,
                    int linear, int* __restrict__ status) {
   using C = MpnnTc;
   extern __shared__ __align__(128) unsigned char smem[];
@@ -161,33 +140,50 @@ __global__ void __launch_bounds__(MpnnTc::kThreads, 2)
     // ---- X = [h | m] of the tile, split into three BF16 parts
     {
       const int64_t e = n0 + row;
-      // all four 8-channel chunks of h_e and m_e in flight at once
-      float4 hl[4][2], ml[4][2];
-      const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+      int64_t j[3] = {-1, -1, -1};
+      if (e < n) neighbours(nbr, K, e, j);
+      // two chunks of 8 channels at a time, every load of both issued before use
+#pragma unroll 1
+      for (int cp = 0; cp < 2; ++cp) {
+        float4 hl[2][2], ml[2][3][2];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const int c0 = (half * 4 + u) * 8;  // channels c0 .. c0 + 7
-        hl[u][0] = hl[u][1] = ml[u][0] = ml[u][1] = z4;
-        if (e < n) {
-          const float4* hp = reinterpret_cast<const float4*>(h + e * C::kN + c0);
-          const float4* mp = reinterpret_cast<const float4*>(msum + e * C::kN + c0);
-          hl[u][0] = hp[0];
-          hl[u][1] = hp[1];
-          ml[u][0] = mp[0];
-          ml[u][1] = mp[1];
+        for (int u = 0; u < 2; ++u) {
+          const int c0 = (half * 4 + cp * 2 + u) * 8;  // channels c0 .. c0 + 7
+          const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+          hl[u][0] = hl[u][1] = z4;
+          if (e < n) {
+            const float4* hp = reinterpret_cast<const float4*>(h + e * C::kN + c0);
+            hl[u][0] = hp[0];
+            hl[u][1] = hp[1];
+          }
+#pragma unroll
+          for (int f = 0; f < 3; ++f) {
+            ml[u][f][0] = ml[u][f][1] = z4;
+            if (j[f] >= 0) {
+              const float4* mp = reinterpret_cast<const float4*>(h + j[f] * C::kN + c0);
+              ml[u][f][0] = mp[0];
+              ml[u][f][1] = mp[1];
+            }
+          }
         }
-      }
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const int c0 = (half * 4 + u) * 8;
-        const float hv[8] = {hl[u][0].x, hl[u][0].y, hl[u][0].z, hl[u][0].w,
-                             hl[u][1].x, hl[u][1].y, hl[u][1].z, hl[u][1].w};
-        const float mv[8] = {ml[u][0].x, ml[u][0].y, ml[u][0].z, ml[u][0].w,
-                             ml[u][1].x, ml[u][1].y, ml[u][1].z, ml[u][1].w};
-        split3_store(hv, sA + tc_off(row, c0), sA + C::kABytes + tc_off(row, c0),
-                     sA + 2 * C::kABytes + tc_off(row, c0));
-        split3_store(mv, sA + tc_off(row, C::kN + c0), sA + C::kABytes + tc_off(row, C::kN + c0),
-                     sA + 2 * C::kABytes + tc_off(row, C::kN + c0));
+        for (int u = 0; u < 2; ++u) {
+          const int c0 = (half * 4 + cp * 2 + u) * 8;
+          const float hv[8] = {hl[u][0].x, hl[u][0].y, hl[u][0].z, hl[u][0].w,
+                               hl[u][1].x, hl[u][1].y, hl[u][1].z, hl[u][1].w};
+          float mv[8];
+#pragma unroll
+          for (int q = 0; q < 2; ++q) {
+            mv[4 * q] = (ml[u][0][q].x + ml[u][1][q].x) + ml[u][2][q].x;
+            mv[4 * q + 1] = (ml[u][0][q].y + ml[u][1][q].y) + ml[u][2][q].y;
+            mv[4 * q + 2] = (ml[u][0][q].z + ml[u][1][q].z) + ml[u][2][q].z;
+            mv[4 * q + 3] = (ml[u][0][q].w + ml[u][1][q].w) + ml[u][2][q].w;
+          }
+          split3_store(hv, sA + tc_off(row, c0), sA + C::kABytes + tc_off(row, c0),
+                       sA + 2 * C::kABytes + tc_off(row, c0));
+          split3_store(mv, sA + tc_off(row, C::kN + c0), sA + C::kABytes + tc_off(row, C::kN + c0),
+                       sA + 2 * C::kABytes + tc_off(row, C::kN + c0));
+        }
       }
     }
     // generic-proxy stores of X -> visible to the tensor core's async proxy
