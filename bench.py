@@ -318,7 +318,7 @@ def smooth_rhs(x, y, index: int, modes: int = 24):
 
 
 def measure_learned(dg, meshes, n_train=LEARN_TRAIN_SAMPLE, n_held=LEARN_HELD_SAMPLE, n_fp64=LEARN_FP64_HELD,
-                    snapshots=LEARN_SNAPSHOTS, full=False, activation="relu"):
+                    snapshots=LEARN_SNAPSHOTS, full=False, activation="relu", correction="additive"):
     """Learned preconditioner on IPDG Poisson (Dirichlet, jittered 128x128 mesh,
     K = 32768, N = 4), in two-level form: M r = Binv r + P A_c^-1 P^T r + network,
     the coarse space a smoothed aggregation of LEARN_AGGREGATE cells.  Residual /
@@ -345,6 +345,8 @@ def measure_learned(dg, meshes, n_train=LEARN_TRAIN_SAMPLE, n_held=LEARN_HELD_SA
     net = dg.MPNN(D, layers=4, seed=LEARN_SEED)
     if activation == "linear":   # a fixed linear correction: flexible CG sees a fixed preconditioner
         net.set_activation(dg.MPNN_ACT_LINEAR)
+    if correction == "residual":  # the network acts on r' = r - S z0, the residual the two-level step leaves
+        net.set_correction(dg.MPNN_CORR_RESIDUAL)
     bj = dg.MPNN(D, layers=1, seed=0)               # zero output layer: M(r) = Binv r + coarse
     # two-level form: the coarse space (smoothed aggregation) removes the smooth
     # mesh-wide error that a 4-hop network cannot see; the network learns the rest
@@ -382,9 +384,11 @@ def measure_learned(dg, meshes, n_train=LEARN_TRAIN_SAMPLE, n_held=LEARN_HELD_SA
         for k in snapshots:
             xk, _ = D.pcg(b, rtol=1e-30, maxit=k, check=False)
             r = b - D.spd(xk)
-            nr = float(torch.linalg.norm(r))
-            X.append((r * (c / nr)).float())
-            T.append(((xs - xk - bj.precondition(r)) * (c / nr)).float())
+            z0 = bj.precondition(r)
+            rin = r - D.spd(z0) if correction == "residual" else r
+            nr = float(torch.linalg.norm(rin))
+            X.append((rin * (c / nr)).float())
+            T.append(((xs - xk - z0) * (c / nr)).float())
     torch.cuda.synchronize()
     datagen_s = time.perf_counter() - t0
     sigma = float(torch.sqrt(torch.mean(torch.stack([torch.mean(t.double() ** 2) for t in T]))))
@@ -452,6 +456,7 @@ def measure_learned(dg, meshes, n_train=LEARN_TRAIN_SAMPLE, n_held=LEARN_HELD_SA
                 "max_final_relres": float(max(r[2] for r in rows))}
 
     out = {"workload": f"ipdg_poisson_dirichlet_k{D.K}_n{LEARN_ORDER}_learned_precond", "activation": activation,
+           "correction": correction,
            "num_cells": D.K, "order": LEARN_ORDER, "rtol": 1e-10,
            "sequence": {"solves": LEARN_TRAIN + LEARN_HELD, "train": LEARN_TRAIN, "held_out": LEARN_HELD,
                         "rhs": "24 Fourier modes, amplitudes ~ N(0, |k|^-2), seeded per solve"},
@@ -969,6 +974,8 @@ def main():
     ap.add_argument("--no-equal-error", action="store_true", help="skip the accuracy-against-time sweep")
     ap.add_argument("--learned-activation", default="relu", choices=["relu", "linear"],
                     help="hidden-layer activation of the learned preconditioner's network")
+    ap.add_argument("--learned-correction", default="additive", choices=["additive", "residual"],
+                    help="where the learned preconditioner's network acts: on r, or on r - S z0")
     ap.add_argument("--learned-full", action="store_true",
                     help="run only the learned-preconditioner workload over its whole 1600 / 400 sequence "
                          "(about a quarter of an hour) and print its section as one JSON line")
@@ -982,7 +989,8 @@ def main():
         from dgc_gb300 import meshes
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         out = measure_learned(dg, meshes, n_train=LEARN_TRAIN, n_held=LEARN_HELD, n_fp64=40,
-                              snapshots=(4, 16, 64), full=True, activation=args.learned_activation)
+                              snapshots=(4, 16, 64), full=True, activation=args.learned_activation,
+                              correction=args.learned_correction)
         print(json.dumps({"learned_precond_full": out}))
         return None
 
@@ -1106,7 +1114,8 @@ def main():
             batched["cpu_baseline"] = cpu_batched_baseline()
     learned = None
     if rank == 0 and not args.no_learned:
-        learned = measure_learned(dg, meshes, activation=args.learned_activation)
+        learned = measure_learned(dg, meshes, activation=args.learned_activation,
+                                  correction=args.learned_correction)
     advection = None
     if rank == 0 and not args.no_advection:
         advection = measure_advection(dg, meshes)

@@ -349,6 +349,31 @@ __global__ void k_scale_to_f32(int64_t n, int npi, int np, const double* __restr
     x[i] = (int)(i % npi) < np ? (float)(r[i] * scale) : 0.0f;
 }
 
+// residual-correction form: rp = r - S z0 on valid nodes (FP32; S z0 given in
+// FP32), and |rp|^2 accumulated in FP64 into *nrm
+__global__ void k_post_residual(int64_t n, int npi, int np, const double* __restrict__ r,
+                                const float* __restrict__ sz, float* __restrict__ rp, double* __restrict__ nrm) {
+  double acc = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float v = (int)(i % npi) < np ? (float)r[i] - sz[i] : 0.0f;
+    rp[i] = v;
+    acc += (double)v * (double)v;
+  }
+  block_add(acc, nrm);
+}
+
+// FP64 vector -> FP32 copy (padding nodes 0)
+__global__ void k_to_f32_valid(int64_t n, int npi, int np, const double* __restrict__ x, float* __restrict__ y) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = (int)(i % npi) < np ? (float)x[i] : 0.0f;
+}
+
+// x *= scale in place
+__global__ void k_scale_f32(int64_t n, float scale, float* __restrict__ x) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    x[i] *= scale;
+}
+
 // z = bj + scale * y (padding nodes 0)
 __global__ void k_precond_combine(int64_t n, int npi, int np, const double* __restrict__ bj,
                                   const float* __restrict__ y, double scale, double* __restrict__ z) {
@@ -432,12 +457,13 @@ struct dgc_mpnn_s {
   float *sd = nullptr, *tm = nullptr, *st = nullptr;  // energy loss: S d, masked t, S t
   int loss_kind = DGC_MPNN_LOSS_ENERGY;
   int linear = 0;                // DGC_MPNN_ACT_LINEAR: no ReLU, biases held at zero
+  int post = 0;                  // DGC_MPNN_CORR_RESIDUAL: the network acts on r - S z0
   bool coarse = false;           // add the handle's coarse-space correction to Binv r
   double* scal = nullptr;        // training: [0] loss, [1..] per-sample target norms; solver: dot products
   double* h_scal = nullptr;      // pinned
   int scal_cap = 0;
   // preconditioner / flexible CG work (one field)
-  float *px = nullptr, *ph0 = nullptr, *ph1 = nullptr, *py = nullptr;
+  float *px = nullptr, *ph0 = nullptr, *ph1 = nullptr, *py = nullptr, *pt = nullptr;
   double *bj = nullptr, *r = nullptr, *z = nullptr;
   static constexpr int kMaxWindow = 8;
   double* pv[kMaxWindow + 1] = {};  // direction ring p_i, i mod (window + 1)
@@ -527,6 +553,7 @@ int ensure_apply(dgc_mpnn m) {
   const size_t nW = (size_t)m->h->K * dgk::kW, nY = field_len(m);
   CKM(zalloc(&m->px, nY));
   CKM(zalloc(&m->py, nY));
+  CKM(zalloc(&m->pt, nY));
   CKM(zalloc(&m->ph0, nW));
   CKM(zalloc(&m->ph1, nW));
   for (double** p : {&m->bj, &m->r, &m->z}) CKM(zalloc(p, nY));
@@ -602,9 +629,28 @@ int precondition(dgc_mpnn m, const double* r, double* z, cudaStream_t s, double 
     CKM(cudaMemsetAsync(z, 0, n * sizeof(double), s));
     return DGC_OK;
   }
-  // network input r c / |r| (unit RMS per valid node, c = sqrt(K Np)), output scaled back by |r| / c
+  // network input x c / |x| (unit RMS per valid node, c = sqrt(K Np)), output scaled back by |x| / c;
+  // x = r, or in the residual-correction form x = r - S z0 (S applied in FP32)
   const double c = std::sqrt((double)h->K * h->Np);
-  dgk::k_scale_to_f32<<<grid_for(m, n, 256), 256, 0, s>>>(n, m->lay.npi, h->Np, r, c / nr, m->px);
+  if (m->post) {
+    dgk::k_to_f32_valid<<<grid_for(m, n, 256), 256, 0, s>>>(n, m->lay.npi, h->Np, m->bj, m->pt);
+    CKM(cudaGetLastError());
+    if (int rc = dgc::ipdg_spd_apply_f32(h, m->pt, m->py, s)) return rc;
+    CKM(cudaMemsetAsync(m->scal, 0, sizeof(double), s));
+    dgk::k_post_residual<<<dot_grid(m, n), 256, 0, s>>>(n, m->lay.npi, h->Np, r, m->py, m->px, m->scal);
+    CKM(cudaGetLastError());
+    CKM(cudaMemcpyAsync(m->h_scal, m->scal, sizeof(double), cudaMemcpyDeviceToHost, s));
+    CKM(cudaStreamSynchronize(s));
+    nr = std::sqrt(m->h_scal[0]);
+    if (nr == 0.0) {
+      CKM(cudaMemcpyAsync(z, m->bj, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+      return DGC_OK;
+    }
+    dgk::k_scale_f32<<<grid_for(m, n, 256), 256, 0, s>>>(n, (float)(c / nr), m->px);
+    h->launches += 3;
+  } else {
+    dgk::k_scale_to_f32<<<grid_for(m, n, 256), 256, 0, s>>>(n, m->lay.npi, h->Np, r, c / nr, m->px);
+  }
   CKM(cudaGetLastError());
   if (int rc = forward(m, h->K, m->px, m->py, m->ph0, m->ph1, false, s)) return rc;
   dgk::k_precond_combine<<<grid_for(m, n, 256), 256, 0, s>>>(n, m->lay.npi, h->Np, m->bj, m->py, nr / c, z);
@@ -668,7 +714,7 @@ extern "C" int dgc_mpnn_destroy(dgc_mpnn m) {
   if (!m) return DGC_OK;
   for (float* p : {m->w, m->grad, m->am, m->av, m->y, m->dy, m->dh0, m->dh1, m->g, m->m, m->sd, m->tm, m->st,
                    m->px, m->ph0, m->ph1,
-                   m->py})
+                   m->py, m->pt})
     cudaFree(p);
   for (auto p : m->hs) cudaFree(p);
   for (auto p : m->as) cudaFree(p);
@@ -744,6 +790,14 @@ extern "C" int dgc_mpnn_set_activation(dgc_mpnn m, int kind) {
     CKM(cudaGetLastError());
     CKM(cudaDeviceSynchronize());
   }
+  return DGC_OK;
+}
+
+extern "C" int dgc_mpnn_set_correction(dgc_mpnn m, int kind) {
+  if (!m) return merr(DGC_ERR_ARG, "null network");
+  if (kind != DGC_MPNN_CORR_ADDITIVE && kind != DGC_MPNN_CORR_RESIDUAL)
+    return merr(DGC_ERR_ARG, "unknown correction form");
+  m->post = kind == DGC_MPNN_CORR_RESIDUAL;
   return DGC_OK;
 }
 

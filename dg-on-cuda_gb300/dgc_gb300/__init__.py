@@ -26,6 +26,7 @@ LAYOUT_NATIVE, LAYOUT_REF_CPU, LAYOUT_REF_GPU = 0, 1, 2
 OP_DR_WEAK, OP_DS_WEAK, OP_LIFT, OP_DR_STRONG, OP_DS_STRONG, OP_MASS, OP_V = range(7)
 MPNN_LOSS_L2, MPNN_LOSS_ENERGY = 0, 1
 MPNN_ACT_RELU, MPNN_ACT_LINEAR = 0, 1
+MPNN_CORR_ADDITIVE, MPNN_CORR_RESIDUAL = 0, 1
 PHYSICS = {"advection": ADVECTION, "maxwell_tm": MAXWELL_TM, "maxwell_te": MAXWELL_TE, "laplace": LAPLACE}
 
 
@@ -159,6 +160,7 @@ def lib():
             L.dgc_mpnn_forward.argtypes = [_vp, _vp, _vp, _vp]
             L.dgc_mpnn_set_loss.argtypes = [_vp, C.c_int]
             L.dgc_mpnn_set_activation.argtypes = [_vp, C.c_int]
+            L.dgc_mpnn_set_correction.argtypes = [_vp, C.c_int]
             L.dgc_mpnn_set_coarse.argtypes = [_vp, C.c_int, _vp]
             L.dgc_coarse_build.argtypes = [_vp, C.c_int, _vp]
             L.dgc_coarse_apply.argtypes = [_vp, _vp, _vp, C.c_int, _vp]
@@ -714,6 +716,10 @@ class MPNN:
     def set_activation(self, kind: int):
         """MPNN_ACT_RELU (default) or MPNN_ACT_LINEAR (no ReLU, biases zero and held there)."""
         _check(lib().dgc_mpnn_set_activation(self._h, kind))
+
+    def set_correction(self, kind: int):
+        """MPNN_CORR_ADDITIVE (default) or MPNN_CORR_RESIDUAL (the network acts on r - S z0)."""
+        _check(lib().dgc_mpnn_set_correction(self._h, kind))
     def get_weights(self) -> np.ndarray:
         w = np.zeros(self.num_params, dtype=np.float32)
         _check(lib().dgc_mpnn_get_weights(self._h, w.ctypes.data))

@@ -389,6 +389,16 @@ int dgc_mpnn_set_loss(dgc_mpnn m, int kind);
  * r, so flexible CG sees a fixed preconditioner. */
 enum { DGC_MPNN_ACT_RELU = 0, DGC_MPNN_ACT_LINEAR = 1 };
 int dgc_mpnn_set_activation(dgc_mpnn m, int kind);
+/* Where the network's correction enters the preconditioner.
+ * DGC_MPNN_CORR_ADDITIVE (default): M(r) = z0 + (|r|/c) net(c r/|r|).
+ * DGC_MPNN_CORR_RESIDUAL: the network acts on what the rest leaves,
+ *   M(r) = z0 + (|r'|/c) net(c r'/|r'|),  r' = r - S z0 (S in FP32),
+ * with z0 = Binv r (+ the coarse term when dgc_mpnn_set_coarse is on); train it
+ * on inputs r' c/|r'| and targets (e - z0) c/|r'|, the error left after z0,
+ * which is S^-1 r'.  Costs one FP32 apply of S and one host round trip more
+ * per application. */
+enum { DGC_MPNN_CORR_ADDITIVE = 0, DGC_MPNN_CORR_RESIDUAL = 1 };
+int dgc_mpnn_set_correction(dgc_mpnn m, int kind);
 /* Loss and gradients on `samples` field pairs (device, FP32, native layout,
  * samples x K x NpP each): x the network inputs, t the targets.  grad_out
  * (device, num_params floats) receives d loss / d weights (may be NULL);

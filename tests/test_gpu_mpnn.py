@@ -100,6 +100,33 @@ def test_forward_many_tiles_matches_numpy():
     D.check()
 
 
+def test_residual_correction_form_composes_as_documented():
+    # M(r) = z0 + (|r'|/c) net(c r'/|r'|), r' = r - S z0, z0 = Binv r; the FP32 S
+    # inside against the FP64 one here, hence the 1e-5 tolerance
+    m = meshes.jittered_square(12, 31)
+    D = dg.Discretization(m, "laplace", 3, dg.F64, tau=dg.TAU_SCALED, dirichlet=True)
+    net = dg.MPNN(D, layers=2, seed=8)
+    base = dg.MPNN(D, layers=1, seed=0)          # zero output layer: M(r) = Binv r
+    rng = np.random.default_rng(9)
+    w = (rng.standard_normal(net.num_params) * 0.1).astype(np.float32)
+    net.set_weights(w)
+    net.set_correction(dg.MPNN_CORR_RESIDUAL)
+    rv = np.zeros((D.K, D.NpP))
+    rv[:, :D.Np] = rng.standard_normal((D.K, D.Np))
+    r = torch.from_numpy(rv.reshape(-1)).cuda()
+    z = net.precondition(r).cpu().numpy()
+    z0 = base.precondition(r)
+    rp = (r - D.spd(z0)).cpu().numpy()
+    c = np.sqrt(D.K * D.Np)
+    nr = np.linalg.norm(rp)
+    y = net.forward(torch.from_numpy((rp * c / nr).astype(np.float32)).cuda()).double().cpu().numpy()
+    ref = z0.cpu().numpy() + y * nr / c
+    ref.reshape(D.K, D.NpP)[:, D.Np:] = 0.0
+    assert relerr(z, ref) < 1e-5
+    assert relerr(z, z0.cpu().numpy()) > 1e-3      # the network term is present
+    D.check()
+
+
 def test_weights_round_trip_and_adam_step_moves_weights():
     m = meshes.jittered_square(3, 2)
     D = dg.Discretization(m, "laplace", 3, dg.F64, tau=dg.TAU_SCALED, dirichlet=True)
