@@ -136,6 +136,17 @@ __device__ __forceinline__ bool mbar_wait_backoff(uint64_t* bar, uint32_t parity
   }
 }
 
+// Programmatic dependent launch.  A stage kernel launched with programmatic
+// stream serialization may start while the previous kernel of its stream is
+// still running; grid_dep_wait blocks the calling thread until that kernel has
+// completed and its memory operations are visible (a no-op for a kernel
+// launched without the attribute), so it precedes every access to data the
+// previous launch reads or writes.  grid_dep_launch lets the next kernel of the
+// stream be scheduled once every CTA of this grid has executed it or exited;
+// that kernel still waits for this one's completion before touching its data.
+__device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void grid_dep_launch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 template <typename R>
 struct Vec16;
 template <>

@@ -95,7 +95,6 @@ __device__ __forceinline__ bool blk_tiles(const RhsParams& p, unsigned char* sme
   const int slot = C::MAP == 0 ? tid / NG : ((tid >> 5) / NG) * 32 + (tid & 31);
   const int grp = C::MAP == 0 ? tid - (tid / NG) * NG : (tid >> 5) % NG;
   const float* qin = static_cast<const float*>(p.q_in);
-  const double tnow = p.t_dev ? *p.t_dev + p.t : p.t;
   const float cax = p.fax, cay = p.fay, cca = p.fca, ccb = p.fcb, cdt = p.fdt;
 
   // the padding columns of the flux rows are never written by the face phase
@@ -117,8 +116,12 @@ __device__ __forceinline__ bool blk_tiles(const RhsParams& p, unsigned char* sme
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     mbar_arrive_expect_tx(&bar[2], C::kMat);
     bulk_g2s(const_cast<float*>(sB), p.mats_blk, C::kMat, &bar[2]);
-    if (t0 < tend) issue(t0, 0);
   }
+  // the operators are set-up data; the state, the residual and the device
+  // time are the previous launch's output
+  grid_dep_wait();
+  const double tnow = p.t_dev ? *p.t_dev + p.t : p.t;
+  if (tid == 0 && t0 < tend) issue(t0, 0);
   if (!__syncthreads_and(mbar_wait(&bar[2], ph[2], p.status))) return false;
   ph[2] ^= 1;
 
@@ -346,6 +349,7 @@ __global__ void __launch_bounds__(BlkConfig<N, P, EPT_, MAP_>::kThreads, BlkConf
   using C = BlkConfig<N, P, EPT_, MAP_>;
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem + C::oBar);
+  grid_dep_launch();  // the next stage may be scheduled; it waits for this grid before its reads
   if (threadIdx.x == 0) {
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);

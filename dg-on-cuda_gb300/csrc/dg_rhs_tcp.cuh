@@ -96,6 +96,7 @@ __global__ void __launch_bounds__(512, 1) dg_rhs_tcp_kernel(const RhsParams p) {
   const float cax = p.fax, cay = p.fay, cca = p.fca, ccb = p.fcb, cdt = p.fdt;
   const bool aux_tile = p.mode == MODE_LSERK;
 
+  grid_dep_launch();  // the next stage may be scheduled; it waits for this grid before its reads
   if (tid == 0) {
     for (int s = 0; s < NB; ++s) {
       mbar_init(&bar[TB_DFULL + s], 1);
@@ -131,6 +132,7 @@ __global__ void __launch_bounds__(512, 1) dg_rhs_tcp_kernel(const RhsParams p) {
   if (warp == 15) {
     if (lane == 1) {
       // ============================================================== LOAD
+      grid_dep_wait();  // the state and the residual are the previous launch's output
       for (int i = 0; i < nt; ++i) {
         const int s = i % NB, k0 = tile_of(i) * TE, ne = min(TE, p.K - k0);
         if (i >= NB) wait(TB_DFREE + s, ((i - NB) / NB) & 1);  // epilogue of tile i - NB done
@@ -189,6 +191,7 @@ __global__ void __launch_bounds__(512, 1) dg_rhs_tcp_kernel(const RhsParams p) {
       if (e < ne) face_flux<N, P>(e, f, nbcur, bufQ(s), bufG(s), cur, gam(g), cax, cay);
       mbar_arrive(&bar[TB_GFULL + g]);
     };
+    grid_dep_wait();  // neighbour traces are read from the previous launch's output
     if (nt > 0) gather(0, bc, nbc);
     for (int i = 0; i < nt; i += 2) {
       step(i, bc, nbc, bx, nbx);
@@ -257,6 +260,7 @@ __global__ void __launch_bounds__(512, 1) dg_rhs_tcp_kernel(const RhsParams p) {
     const int j0 = 16 * half, jn = min(NpP - j0, 16);
     float* out = static_cast<float*>(p.out);
     float* aux = static_cast<float*>(p.aux);
+    grid_dep_wait();  // the previous launch reads the buffers written here
     for (int i = 0; i < nt; ++i) {
       const int s = i % NB, g = i & 1, k0 = tile_of(i) * TE, ne = min(TE, p.K - k0);
       wait(TB_DFULL + s, (i / NB) & 1);

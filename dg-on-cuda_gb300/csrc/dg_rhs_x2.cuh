@@ -108,9 +108,9 @@ __global__ void __launch_bounds__(X2Config<N, P>::kThreads, X2Config<N, P>::kMin
   const size_t nvec = (size_t)p.K * ESTR;
   const float* qhi = static_cast<const float*>(p.q_in);
   const float* qlo = qhi + nvec;
-  const double tnow = p.t_dev ? *p.t_dev + p.t : p.t;
   const float cax = p.fax, cay = p.fay, cca = p.fca, ccb = p.fcb, cdt = p.fdt;
 
+  grid_dep_launch();  // the next stage may be scheduled; it waits for this grid before its reads
   if (tid == 0) {
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
@@ -134,8 +134,12 @@ __global__ void __launch_bounds__(X2Config<N, P>::kThreads, X2Config<N, P>::kMin
   if (tid == 0) {
     mbar_arrive_expect_tx(&bar[2], C::kMat);
     bulk_g2s(const_cast<float*>(sB), p.mats_blk, C::kMat, &bar[2]);
-    if ((int)blockIdx.x < ntiles) issue(blockIdx.x, 0);
   }
+  // the operators are set-up data; the state, the residual and the device
+  // time are the previous launch's output
+  grid_dep_wait();
+  const double tnow = p.t_dev ? *p.t_dev + p.t : p.t;
+  if (tid == 0 && (int)blockIdx.x < ntiles) issue(blockIdx.x, 0);
   if (!__syncthreads_and(mbar_wait(&bar[2], 0, p.status))) return;
 
   uint32_t ph[2] = {0, 0};

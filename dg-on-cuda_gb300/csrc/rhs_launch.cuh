@@ -4,6 +4,8 @@
 #pragma once
 
 #include <algorithm>
+#include <cstdlib>
+#include <cstring>
 #include <mutex>
 
 #include "dg_rhs.cuh"
@@ -13,6 +15,35 @@ namespace dgk {
 struct LaunchInfo {
   int threads = 0, tile = 0, smem = 0, blocks_per_sm = 0;
 };
+
+// Launch of a stage kernel that calls grid_dep_wait before it touches the
+// previous launch's data (dg_rhs_blk_kernel, dg_rhs_tcp_kernel,
+// dg_rhs_x2_kernel): with programmatic stream serialization its CTAs are
+// scheduled, and run their set-up (barriers, operator copies, tensor memory),
+// while the previous kernel of the stream finishes.  DGC_STAGE_OVERLAP=0 in the
+// environment launches them without the attribute.
+inline bool stage_overlap_enabled() {
+  static const bool on = [] {
+    const char* v = std::getenv("DGC_STAGE_OVERLAP");
+    return !(v && std::strcmp(v, "0") == 0);
+  }();
+  return on;
+}
+
+inline cudaError_t launch_stage(void (*kern)(RhsParams), int grid, int threads, size_t smem, cudaStream_t s,
+                                const RhsParams& p) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3((unsigned)threads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = stage_overlap_enabled() ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kern, p);
+}
 
 template <typename R, int N, int P>
 cudaError_t rhs_configure(LaunchInfo* info) {
@@ -208,8 +239,7 @@ cudaError_t rhs_tcp(const RhsParams* p, int sm_count, cudaStream_t s, LaunchInfo
     if (!p->mats_tc) return cudaErrorInvalidValue;
     const int ntiles = (p->K + C::TE - 1) / C::TE;
     const int grid = std::min(ntiles, sm_count);
-    dg_rhs_tcp_kernel<N, P><<<grid, C::kThreads, C::kSmemLaunch, s>>>(*p);
-    return cudaGetLastError();
+    return launch_stage(dg_rhs_tcp_kernel<N, P>, grid, C::kThreads, C::kSmemLaunch, s, *p);
   }
 }
 
@@ -237,8 +267,7 @@ cudaError_t rhs_blk(const RhsParams* p, int sm_count, cudaStream_t s, LaunchInfo
   const int ntiles = (p->K + C::TE - 1) / C::TE;
   int grid = sm_count * (bps > 0 ? bps : 1);
   if (grid > ntiles) grid = ntiles;
-  dg_rhs_blk_kernel<N, P, EPT, MAP><<<grid, C::kThreads, C::kSmem, s>>>(*p);
-  return cudaGetLastError();
+  return launch_stage(dg_rhs_blk_kernel<N, P, EPT, MAP>, grid, C::kThreads, C::kSmem, s, *p);
 }
 
 // FP32 variants at orders 1..6: 0 = one thread per element-node (dg_rhs_kernel),

@@ -27,8 +27,7 @@ static cudaError_t rhs_x2(const RhsParams* p, int sm_count, cudaStream_t s, Laun
   const int ntiles = (p->K + C::TE - 1) / C::TE;
   int grid = sm_count * (bps > 0 ? bps : 1);
   if (grid > ntiles) grid = ntiles;
-  dg_rhs_x2_kernel<N, P><<<grid, C::kThreads, C::kSmem, s>>>(*p);
-  return cudaGetLastError();
+  return launch_stage(dg_rhs_x2_kernel<N, P>, grid, C::kThreads, C::kSmem, s, *p);
 }
 
 template <int N>
