@@ -44,7 +44,7 @@ struct BlkConfig {
   static constexpr int Nf = PhysTraits<P>::Nf;
   static constexpr int ESTR = Nf * NpP;              // state stride per element
   static constexpr int FSTR = (NFACE + 3) / 4 * 4;   // padded face-flux row
-  static constexpr int kItems = (TE * NFACE + kThreads - 1) / kThreads;
+  static constexpr int kFItems = (TE * O::Nfp + kThreads - 1) / kThreads;  // (element, face-node) items per thread
   static constexpr int KB = 2 * Np + NFACE;          // operator rows: Dr^T | Ds^T | LIFT^T
   static constexpr uint32_t kMat = KB * NpP * 4;
   // the LSERK residual tile is prefetched with the state tile when the extra
@@ -140,51 +140,51 @@ __device__ __forceinline__ bool blk_tiles(const RhsParams& p, unsigned char* sme
     const float* sG = bufG(b);
     const int4* sN = bufN(b);
 
-    // ---- face nodes: gather own / neighbour values first, then the fluxes
-    {
-      float av[C::kItems][NF], bv[C::kItems][NF];
-      int item[C::kItems];
+    // ---- face nodes: item (element e, face-node index d) takes node d of the
+    //      three faces of e; the own and neighbour values of all three are
+    //      gathered first, then the three fluxes formed
 #pragma unroll
-      for (int s = 0; s < C::kItems; ++s) {
-        const int x = tid + s * NT;
-        item[s] = x < ne * NFACE ? x : -1;
-        if (item[s] < 0) continue;
-        const int e = x / NFACE, fm = x - e * NFACE, f = fm / Nfp, d = fm - f * Nfp;
-        const int nb = f == 0 ? sN[e].x : (f == 1 ? sN[e].y : sN[e].z);
+    for (int s = 0; s < C::kFItems; ++s) {
+      const int x = tid + s * NT;
+      if (x >= ne * Nfp) break;
+      const int e = x / Nfp, d = x - e * Nfp;
+      const int4 nb4 = sN[e];
+      float av[3][NF], bv[3][NF];
+#pragma unroll
+      for (int f = 0; f < 3; ++f) {
+        const int nb = f == 0 ? nb4.x : (f == 1 ? nb4.y : nb4.z);
         const int nd = fmask<N>(f, d);
 #pragma unroll
-        for (int c = 0; c < NF; ++c) av[s][c] = sQ[e * ESTR + c * NpP + nd];
+        for (int c = 0; c < NF; ++c) av[f][c] = sQ[e * ESTR + c * NpP + nd];
         if (nb >= 0) {
           const int kn = nb >> 2, nd2 = fmask<N>(nb & 3, Nfp - 1 - d);
           if (kn >= k0 && kn < k0 + ne) {
 #pragma unroll
-            for (int c = 0; c < NF; ++c) bv[s][c] = sQ[(kn - k0) * ESTR + c * NpP + nd2];
+            for (int c = 0; c < NF; ++c) bv[f][c] = sQ[(kn - k0) * ESTR + c * NpP + nd2];
           } else {
             const float* qb = qin + (size_t)kn * ESTR + nd2;
 #pragma unroll
-            for (int c = 0; c < NF; ++c) bv[s][c] = __ldg(qb + c * NpP);
+            for (int c = 0; c < NF; ++c) bv[f][c] = __ldg(qb + c * NpP);
           }
         } else if (P == PHYS_ADV) {
           const int bf = -1 - nb;
           const double xx = p.bxy[((size_t)bf * Nfp + d) * 2], yy = p.bxy[((size_t)bf * Nfp + d) * 2 + 1];
-          bv[s][0] = (float)adv_exact(p, tnow, xx, yy);
+          bv[f][0] = (float)adv_exact(p, tnow, xx, yy);
         } else if (P == PHYS_TM) {  // PEC: H+ = H-, Ez+ = -Ez-
-          bv[s][0] = av[s][0]; bv[s][1] = av[s][1]; bv[s][2] = -av[s][2];
+          bv[f][0] = av[f][0]; bv[f][1] = av[f][1]; bv[f][2] = -av[f][2];
         } else {                    // PEC: E+ = -E-, Hz+ = Hz-
-          bv[s][0] = -av[s][0]; bv[s][1] = -av[s][1]; bv[s][2] = av[s][2];
+          bv[f][0] = -av[f][0]; bv[f][1] = -av[f][1]; bv[f][2] = av[f][2];
         }
       }
+      const float* g = sG + e * 16;
+      const float mJ = g[4];
 #pragma unroll
-      for (int s = 0; s < C::kItems; ++s) {
-        if (item[s] < 0) continue;
-        const int x = item[s];
-        const int e = x / NFACE, fm = x - e * NFACE, f = fm / Nfp;
-        const float* g = sG + e * 16;
+      for (int f = 0; f < 3; ++f) {
         const float nx = g[8 + f], ny = g[11 + f];
-        const float sc = g[5 + f] * g[4];  // -faceJ / J: the lift scale folded into the flux
-        const float* a = av[s];
-        const float* bb = bv[s];
-        float* fo = sF + e * NF * FSTR + fm;
+        const float sc = g[5 + f] * mJ;  // -faceJ / J: the lift scale folded into the flux
+        const float* a = av[f];
+        const float* bb = bv[f];
+        float* fo = sF + e * NF * FSTR + f * Nfp + d;
         if (P == PHYS_ADV) {
           const float an = cax * nx + cay * ny;
           fo[0] = ((an >= 0.0f) ? a[0] : bb[0]) * an * sc;
