@@ -94,6 +94,7 @@ __global__ void __launch_bounds__(256, 3) dg_batch_kernel(const BatchLaunch b) {
   // offset 0 of both tile layouts: barrier 0 (tiles of code 0, buffer 0 of
   // code 1), 1 (buffer 1 of code 1), 2 (operators of code 1)
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
+  grid_dep_launch();  // the next stage may be scheduled; it waits for this grid before its reads
   if (threadIdx.x == 0) {
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
@@ -101,6 +102,7 @@ __global__ void __launch_bounds__(256, 3) dg_batch_kernel(const BatchLaunch b) {
     fence_barrier_init();
   }
   __syncthreads();
+  grid_dep_wait();  // every instance's state and residual are the previous stage's output
   uint32_t ph[3] = {0, 0, 0};
   for (;;) {
     if (threadIdx.x == 0) s_item = (int)atomicAdd(b.head, 1u);
@@ -215,8 +217,7 @@ int launch_step(dgc_batch b, cudaStream_t s) {
   CKB(cudaMemsetAsync(b->d_head, 0, 5 * sizeof(unsigned int), s));
   for (int st = 0; st < 5; ++st) {
     dgk::BatchLaunch L{b->d_params + (size_t)st * n, b->d_kinds, b->d_items, b->nitems, b->d_head + st};
-    dgk::dg_batch_kernel<<<grid, 256, b->smem, s>>>(L);
-    CKB(cudaGetLastError());
+    CKB(dgk::launch_stage(dgk::dg_batch_kernel, grid, 256, b->smem, s, L));
     ++b->launches;
   }
   return DGC_OK;

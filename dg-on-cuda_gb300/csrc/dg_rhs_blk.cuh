@@ -12,8 +12,13 @@
 //   * the element's field values are read 4 columns at a time (float4), the
 //     operators as rows of the transposed matrices padded to NpP columns, so
 //     one float4 of Dr^T / Ds^T / LIFT^T row j covers the thread's 4 nodes;
-//   * 4 x Nf x EPT accumulators per operator; the face fluxes are stored
-//     already scaled by -faceJ/J so LIFT accumulates straight into rhs;
+//   * Maxwell: the curl of the first two fields is accumulated as one
+//     product pair Dr u + Ds v, u and v their combination with the element's
+//     (constant) rx, ry, sx, sy, next to Dr q2 and Ds q2 for the gradient of
+//     the third field: 3 x 4 x EPT accumulators and 4 FMAs per node and
+//     column instead of 6 (advection: Dr q and Ds q);
+//   * the face fluxes are stored already scaled by -faceJ/J so LIFT
+//     accumulates straight into rhs;
 //   * columns past Np are skipped at compile time (padding never enters a
 //     valid output) and padded output nodes are written as 0.
 // Two thread mappings (MAP):
@@ -140,6 +145,110 @@ __device__ __forceinline__ bool blk_tiles(const RhsParams& p, unsigned char* sme
     const float* sG = bufG(b);
     const int4* sN = bufN(b);
 
+    // ---- volume: nodes 4 grp .. 4 grp + 3 of elements slot, slot + NTE.  It
+    //      needs no face data, so it runs first and the face phase's neighbour
+    //      gathers of some warps overlap the volume products of others.
+    float rh[EPT][NF][4];
+    if (slot < NTE) {
+      const float* bR = sB + 4 * grp;           // Dr^T row j at bR + j NpP
+      const float* bS = bR + Np * NpP;          // Ds^T
+      if constexpr (P == PHYS_ADV) {
+        float ur[EPT][4], us[EPT][4];
+#pragma unroll
+        for (int l = 0; l < EPT; ++l)
+#pragma unroll
+          for (int n = 0; n < 4; ++n) ur[l][n] = us[l][n] = 0.0f;
+#pragma unroll
+        for (int j0 = 0; j0 < Np; j0 += 4) {
+          float4 a[EPT];
+#pragma unroll
+          for (int l = 0; l < EPT; ++l) a[l] = *reinterpret_cast<const float4*>(sQ + (slot + l * NTE) * ESTR + j0);
+#pragma unroll
+          for (int jj = 0; jj < 4; ++jj) {
+            if (j0 + jj >= Np) break;
+            const float4 br = *reinterpret_cast<const float4*>(bR + (j0 + jj) * NpP);
+            const float4 bs = *reinterpret_cast<const float4*>(bS + (j0 + jj) * NpP);
+#pragma unroll
+            for (int l = 0; l < EPT; ++l) {
+              const float v = f4c(a[l], jj);
+              ur[l][0] = fmaf(br.x, v, ur[l][0]); us[l][0] = fmaf(bs.x, v, us[l][0]);
+              ur[l][1] = fmaf(br.y, v, ur[l][1]); us[l][1] = fmaf(bs.y, v, us[l][1]);
+              ur[l][2] = fmaf(br.z, v, ur[l][2]); us[l][2] = fmaf(bs.z, v, us[l][2]);
+              ur[l][3] = fmaf(br.w, v, ur[l][3]); us[l][3] = fmaf(bs.w, v, us[l][3]);
+            }
+          }
+        }
+#pragma unroll
+        for (int l = 0; l < EPT; ++l) {
+          const float4 g0 = *reinterpret_cast<const float4*>(sG + (slot + l * NTE) * 16);  // rx ry sx sy
+#pragma unroll
+          for (int n = 0; n < 4; ++n) {
+            const float dx = g0.x * ur[l][n] + g0.z * us[l][n], dy = g0.y * ur[l][n] + g0.w * us[l][n];
+            rh[l][0][n] = cax * dx + cay * dy;
+          }
+        }
+      } else {
+        // Maxwell: the curl term of the third field is one product pair,
+        // Dr u + Ds v with u, v the geometric combinations of the first two
+        // fields (rx, ry, sx, sy are constant on an element):
+        //   TE  Hz' = Dx Ey - Dy Ex = Dr (rx Ey - ry Ex) + Ds (sx Ey - sy Ex),
+        //   TM  Ez' = Dy Hx - Dx Hy = Dr (ry Hx - rx Hy) + Ds (sy Hx - sx Hy);
+        // the gradient of the third field needs Dr q2 and Ds q2.
+        float gr[EPT][4], gs[EPT][4], cu[EPT][4];
+        float4 g0[EPT];
+#pragma unroll
+        for (int l = 0; l < EPT; ++l) {
+          g0[l] = *reinterpret_cast<const float4*>(sG + (slot + l * NTE) * 16);  // rx ry sx sy
+#pragma unroll
+          for (int n = 0; n < 4; ++n) gr[l][n] = gs[l][n] = cu[l][n] = 0.0f;
+        }
+#pragma unroll
+        for (int j0 = 0; j0 < Np; j0 += 4) {
+          float4 a[EPT][NF];
+#pragma unroll
+          for (int l = 0; l < EPT; ++l)
+#pragma unroll
+            for (int c = 0; c < NF; ++c)
+              a[l][c] = *reinterpret_cast<const float4*>(sQ + (slot + l * NTE) * ESTR + c * NpP + j0);
+#pragma unroll
+          for (int jj = 0; jj < 4; ++jj) {
+            if (j0 + jj >= Np) break;
+            const float4 br = *reinterpret_cast<const float4*>(bR + (j0 + jj) * NpP);
+            const float4 bs = *reinterpret_cast<const float4*>(bS + (j0 + jj) * NpP);
+#pragma unroll
+            for (int l = 0; l < EPT; ++l) {
+              const float q0 = f4c(a[l][0], jj), q1 = f4c(a[l][1], jj), v = f4c(a[l][2], jj);
+              const float u = (P == PHYS_TE) ? g0[l].x * q1 - g0[l].y * q0 : g0[l].y * q0 - g0[l].x * q1;
+              const float w = (P == PHYS_TE) ? g0[l].z * q1 - g0[l].w * q0 : g0[l].w * q0 - g0[l].z * q1;
+              gr[l][0] = fmaf(br.x, v, gr[l][0]); gs[l][0] = fmaf(bs.x, v, gs[l][0]);
+              gr[l][1] = fmaf(br.y, v, gr[l][1]); gs[l][1] = fmaf(bs.y, v, gs[l][1]);
+              gr[l][2] = fmaf(br.z, v, gr[l][2]); gs[l][2] = fmaf(bs.z, v, gs[l][2]);
+              gr[l][3] = fmaf(br.w, v, gr[l][3]); gs[l][3] = fmaf(bs.w, v, gs[l][3]);
+              cu[l][0] = fmaf(br.x, u, fmaf(bs.x, w, cu[l][0]));
+              cu[l][1] = fmaf(br.y, u, fmaf(bs.y, w, cu[l][1]));
+              cu[l][2] = fmaf(br.z, u, fmaf(bs.z, w, cu[l][2]));
+              cu[l][3] = fmaf(br.w, u, fmaf(bs.w, w, cu[l][3]));
+            }
+          }
+        }
+#pragma unroll
+        for (int l = 0; l < EPT; ++l) {
+          const float rx = g0[l].x, ry = g0[l].y, sx = g0[l].z, sy = g0[l].w;
+#pragma unroll
+          for (int n = 0; n < 4; ++n) {
+            if (P == PHYS_TM) {  // Hx' = Dy Ez, Hy' = -Dx Ez
+              rh[l][0][n] = ry * gr[l][n] + sy * gs[l][n];
+              rh[l][1][n] = -(rx * gr[l][n] + sx * gs[l][n]);
+            } else {             // Ex' = -Dy Hz, Ey' = Dx Hz
+              rh[l][0][n] = -(ry * gr[l][n] + sy * gs[l][n]);
+              rh[l][1][n] = rx * gr[l][n] + sx * gs[l][n];
+            }
+            rh[l][2][n] = cu[l][n];
+          }
+        }
+      }
+    }
+
     // ---- face nodes: item (element e, face-node index d) takes node d of the
     //      three faces of e; the own and neighbour values of all three are
     //      gathered first, then the three fluxes formed
@@ -203,65 +312,9 @@ __device__ __forceinline__ bool blk_tiles(const RhsParams& p, unsigned char* sme
     }
     __syncthreads();
 
-    // ---- volume + lift + epilogue: nodes 4 grp .. 4 grp + 3 of elements slot, slot + NTE
+    // ---- lift + epilogue
     if (slot < NTE) {
-      const float* bR = sB + 4 * grp;           // Dr^T row j at bR + j NpP
-      const float* bS = bR + Np * NpP;          // Ds^T
-      const float* bL = bR + 2 * Np * NpP;      // LIFT^T
-      float ur[EPT][NF][4], us[EPT][NF][4];
-#pragma unroll
-      for (int l = 0; l < EPT; ++l)
-#pragma unroll
-        for (int c = 0; c < NF; ++c)
-#pragma unroll
-          for (int n = 0; n < 4; ++n) ur[l][c][n] = us[l][c][n] = 0.0f;
-#pragma unroll
-      for (int j0 = 0; j0 < Np; j0 += 4) {
-        float4 a[EPT][NF];
-#pragma unroll
-        for (int l = 0; l < EPT; ++l)
-#pragma unroll
-          for (int c = 0; c < NF; ++c)
-            a[l][c] = *reinterpret_cast<const float4*>(sQ + (slot + l * NTE) * ESTR + c * NpP + j0);
-#pragma unroll
-        for (int jj = 0; jj < 4; ++jj) {
-          if (j0 + jj >= Np) break;
-          const float4 br = *reinterpret_cast<const float4*>(bR + (j0 + jj) * NpP);
-          const float4 bs = *reinterpret_cast<const float4*>(bS + (j0 + jj) * NpP);
-#pragma unroll
-          for (int l = 0; l < EPT; ++l)
-#pragma unroll
-            for (int c = 0; c < NF; ++c) {
-              const float v = f4c(a[l][c], jj);
-              ur[l][c][0] = fmaf(br.x, v, ur[l][c][0]); us[l][c][0] = fmaf(bs.x, v, us[l][c][0]);
-              ur[l][c][1] = fmaf(br.y, v, ur[l][c][1]); us[l][c][1] = fmaf(bs.y, v, us[l][c][1]);
-              ur[l][c][2] = fmaf(br.z, v, ur[l][c][2]); us[l][c][2] = fmaf(bs.z, v, us[l][c][2]);
-              ur[l][c][3] = fmaf(br.w, v, ur[l][c][3]); us[l][c][3] = fmaf(bs.w, v, us[l][c][3]);
-            }
-        }
-      }
-      // combine with the element's geometric factors
-      float rh[EPT][NF][4];
-#pragma unroll
-      for (int l = 0; l < EPT; ++l) {
-        const float4 g0 = *reinterpret_cast<const float4*>(sG + (slot + l * NTE) * 16);  // rx ry sx sy
-        const float rx = g0.x, ry = g0.y, sx = g0.z, sy = g0.w;
-#pragma unroll
-        for (int n = 0; n < 4; ++n) {
-          if (P == PHYS_ADV) {
-            const float dx = rx * ur[l][0][n] + sx * us[l][0][n], dy = ry * ur[l][0][n] + sy * us[l][0][n];
-            rh[l][0][n] = cax * dx + cay * dy;
-          } else if (P == PHYS_TM) {  // Hx' = Dy Ez, Hy' = -Dx Ez, Ez' = -Dx Hy + Dy Hx
-            rh[l][0][n] = ry * ur[l][2][n] + sy * us[l][2][n];
-            rh[l][1][n] = -(rx * ur[l][2][n] + sx * us[l][2][n]);
-            rh[l][2][n] = -(rx * ur[l][1][n] + sx * us[l][1][n]) + (ry * ur[l][0][n] + sy * us[l][0][n]);
-          } else {                    // Ex' = -Dy Hz, Ey' = Dx Hz, Hz' = Dx Ey - Dy Ex
-            rh[l][0][n] = -(ry * ur[l][2][n] + sy * us[l][2][n]);
-            rh[l][1][n] = rx * ur[l][2][n] + sx * us[l][2][n];
-            rh[l][2][n] = (rx * ur[l][1][n] + sx * us[l][1][n]) - (ry * ur[l][0][n] + sy * us[l][0][n]);
-          }
-        }
-      }
+      const float* bL = sB + 4 * grp + 2 * Np * NpP;  // LIFT^T row m at bL + m NpP
       // lift of the scaled face fluxes
 #pragma unroll
       for (int m0 = 0; m0 < NFACE; m0 += 4) {

@@ -58,7 +58,7 @@ struct X2Config {
   static constexpr int Nf = PhysTraits<P>::Nf;
   static constexpr int ESTR = Nf * NpP;
   static constexpr int FSTR = (NFACE + 3) / 4 * 4;
-  static constexpr int kItems = (TE * NFACE + kThreads - 1) / kThreads;
+  static constexpr int kFItems = (TE * O::Nfp + kThreads - 1) / kThreads;  // (element, face-node) items per thread
   static constexpr int KB = 2 * Np + NFACE;
   static constexpr uint32_t kMat = KB * NpP * 4;
   static constexpr uint32_t kQ = TE * ESTR * 4, kG = TE * 16 * 4, kN = TE * 16;
@@ -157,65 +157,76 @@ __global__ void __launch_bounds__(X2Config<N, P>::kThreads, X2Config<N, P>::kMin
     const int4* sN = bufN(b);
 
     // ---- face nodes: jumps d = q+ - q- from the hi and lo parts, then the
-    // strong-form flux differences, pre-scaled by -faceJ / J
+    // strong-form flux differences, pre-scaled by -faceJ / J.  Item (element
+    // e, face-node index dd) takes node dd of the three faces of e.
 #pragma unroll
-    for (int s = 0; s < C::kItems; ++s) {
+    for (int s = 0; s < C::kFItems; ++s) {
       const int x = tid + s * NT;
-      if (x >= ne * NFACE) continue;
-      const int e = x / NFACE, fm = x - e * NFACE, f = fm / Nfp, dd = fm - f * Nfp;
-      const int nb = f == 0 ? sN[e].x : (f == 1 ? sN[e].y : sN[e].z);
-      const int nd = fmask<N>(f, dd);
-      float ah[NF], al[NF], d[NF];
+      if (x >= ne * Nfp) break;
+      const int e = x / Nfp, dd = x - e * Nfp;
+      const int4 nb4 = sN[e];
+      float d[3][NF];
 #pragma unroll
-      for (int c = 0; c < NF; ++c) {
-        ah[c] = sH[e * ESTR + c * NpP + nd];
-        al[c] = sL[e * ESTR + c * NpP + nd];
-      }
-      if (nb >= 0) {
-        const int kn = nb >> 2, nd2 = fmask<N>(nb & 3, Nfp - 1 - dd);
-        float bh[NF], bl[NF];
-        if (kn >= k0 && kn < k0 + ne) {
+      for (int f = 0; f < 3; ++f) {
+        const int nb = f == 0 ? nb4.x : (f == 1 ? nb4.y : nb4.z);
+        const int nd = fmask<N>(f, dd);
+        float ah[NF], al[NF];
 #pragma unroll
-          for (int c = 0; c < NF; ++c) {
-            bh[c] = sH[(kn - k0) * ESTR + c * NpP + nd2];
-            bl[c] = sL[(kn - k0) * ESTR + c * NpP + nd2];
-          }
-        } else {
-          const size_t o = (size_t)kn * ESTR + nd2;
-#pragma unroll
-          for (int c = 0; c < NF; ++c) {
-            bh[c] = __ldg(qhi + o + c * NpP);
-            bl[c] = __ldg(qlo + o + c * NpP);
-          }
+        for (int c = 0; c < NF; ++c) {
+          ah[c] = sH[e * ESTR + c * NpP + nd];
+          al[c] = sL[e * ESTR + c * NpP + nd];
         }
+        if (nb >= 0) {
+          const int kn = nb >> 2, nd2 = fmask<N>(nb & 3, Nfp - 1 - dd);
+          float bh[NF], bl[NF];
+          if (kn >= k0 && kn < k0 + ne) {
 #pragma unroll
-        for (int c = 0; c < NF; ++c) d[c] = __fadd_rn(__fsub_rn(bh[c], ah[c]), __fsub_rn(bl[c], al[c]));
-      } else if (P == PHYS_ADV) {
-        const int bf = -1 - nb;
-        const double xx = p.bxy[((size_t)bf * Nfp + dd) * 2], yy = p.bxy[((size_t)bf * Nfp + dd) * 2 + 1];
-        d[0] = (float)((adv_exact(p, tnow, xx, yy) - (double)ah[0]) - (double)al[0]);
-      } else if (P == PHYS_TM) {  // PEC: H+ = H-, Ez+ = -Ez-
-        d[0] = 0.0f; d[1] = 0.0f; d[2] = -2.0f * ah[2] - 2.0f * al[2];
-      } else {                    // PEC: E+ = -E-, Hz+ = Hz-
-        d[0] = -2.0f * ah[0] - 2.0f * al[0]; d[1] = -2.0f * ah[1] - 2.0f * al[1]; d[2] = 0.0f;
+            for (int c = 0; c < NF; ++c) {
+              bh[c] = sH[(kn - k0) * ESTR + c * NpP + nd2];
+              bl[c] = sL[(kn - k0) * ESTR + c * NpP + nd2];
+            }
+          } else {
+            const size_t o = (size_t)kn * ESTR + nd2;
+#pragma unroll
+            for (int c = 0; c < NF; ++c) {
+              bh[c] = __ldg(qhi + o + c * NpP);
+              bl[c] = __ldg(qlo + o + c * NpP);
+            }
+          }
+#pragma unroll
+          for (int c = 0; c < NF; ++c) d[f][c] = __fadd_rn(__fsub_rn(bh[c], ah[c]), __fsub_rn(bl[c], al[c]));
+        } else if (P == PHYS_ADV) {
+          const int bf = -1 - nb;
+          const double xx = p.bxy[((size_t)bf * Nfp + dd) * 2], yy = p.bxy[((size_t)bf * Nfp + dd) * 2 + 1];
+          d[f][0] = (float)((adv_exact(p, tnow, xx, yy) - (double)ah[0]) - (double)al[0]);
+        } else if (P == PHYS_TM) {  // PEC: H+ = H-, Ez+ = -Ez-
+          d[f][0] = 0.0f; d[f][1] = 0.0f; d[f][2] = -2.0f * ah[2] - 2.0f * al[2];
+        } else {                    // PEC: E+ = -E-, Hz+ = Hz-
+          d[f][0] = -2.0f * ah[0] - 2.0f * al[0]; d[f][1] = -2.0f * ah[1] - 2.0f * al[1]; d[f][2] = 0.0f;
+        }
       }
       const float* g = sG + e * 16;
-      const float nx = g[8 + f], ny = g[11 + f];
-      const float sc = g[5 + f] * g[4];  // -faceJ / J
-      float* fo = sF + e * NF * FSTR + fm;
-      if (P == PHYS_ADV) {
-        const float an = cax * nx + cay * ny;
-        fo[0] = an < 0.0f ? an * d[0] * sc : 0.0f;
-      } else if (P == PHYS_TM) {
-        const float w = d[2] - ny * d[0] + nx * d[1];
-        fo[0] = 0.5f * ny * w * sc;
-        fo[FSTR] = -0.5f * nx * w * sc;
-        fo[2 * FSTR] = 0.5f * (ny * d[0] - nx * d[1] - d[2]) * sc;
-      } else {
-        const float w = d[2] + ny * d[0] - nx * d[1];
-        fo[0] = -0.5f * ny * w * sc;
-        fo[FSTR] = 0.5f * nx * w * sc;
-        fo[2 * FSTR] = 0.5f * (nx * d[1] - ny * d[0] - d[2]) * sc;
+      const float mJ = g[4];
+#pragma unroll
+      for (int f = 0; f < 3; ++f) {
+        const float nx = g[8 + f], ny = g[11 + f];
+        const float sc = g[5 + f] * mJ;  // -faceJ / J
+        const float* df = d[f];
+        float* fo = sF + e * NF * FSTR + f * Nfp + dd;
+        if (P == PHYS_ADV) {
+          const float an = cax * nx + cay * ny;
+          fo[0] = an < 0.0f ? an * df[0] * sc : 0.0f;
+        } else if (P == PHYS_TM) {
+          const float w = df[2] - ny * df[0] + nx * df[1];
+          fo[0] = 0.5f * ny * w * sc;
+          fo[FSTR] = -0.5f * nx * w * sc;
+          fo[2 * FSTR] = 0.5f * (ny * df[0] - nx * df[1] - df[2]) * sc;
+        } else {
+          const float w = df[2] + ny * df[0] - nx * df[1];
+          fo[0] = -0.5f * ny * w * sc;
+          fo[FSTR] = 0.5f * nx * w * sc;
+          fo[2 * FSTR] = 0.5f * (nx * df[1] - ny * df[0] - df[2]) * sc;
+        }
       }
     }
     __syncthreads();
@@ -229,52 +240,76 @@ __global__ void __launch_bounds__(X2Config<N, P>::kThreads, X2Config<N, P>::kMin
       float cm[NF];
 #pragma unroll
       for (int c = 0; c < NF; ++c) cm[c] = qe[c * NpP];
-      float ur[NF][4], us[NF][4];
+      const float4 g0 = *reinterpret_cast<const float4*>(sG + slot * 16);  // rx ry sx sy
+      const float rx = g0.x, ry = g0.y, sx = g0.z, sy = g0.w;
+      float rh[NF][4];
+      if constexpr (P == PHYS_ADV) {
+        float ur[4] = {0.0f, 0.0f, 0.0f, 0.0f}, us[4] = {0.0f, 0.0f, 0.0f, 0.0f};
 #pragma unroll
-      for (int c = 0; c < NF; ++c)
+        for (int j0 = 0; j0 < Np; j0 += 4) {
+          float4 a = *reinterpret_cast<const float4*>(qe + j0);
+          a.x -= cm[0]; a.y -= cm[0]; a.z -= cm[0]; a.w -= cm[0];
 #pragma unroll
-        for (int n = 0; n < 4; ++n) ur[c][n] = us[c][n] = 0.0f;
-#pragma unroll
-      for (int j0 = 0; j0 < Np; j0 += 4) {
-        float4 a[NF];
-#pragma unroll
-        for (int c = 0; c < NF; ++c) {
-          a[c] = *reinterpret_cast<const float4*>(qe + c * NpP + j0);
-          a[c].x -= cm[c]; a[c].y -= cm[c]; a[c].z -= cm[c]; a[c].w -= cm[c];
+          for (int jj = 0; jj < 4; ++jj) {
+            if (j0 + jj >= Np) break;
+            const float4 br = *reinterpret_cast<const float4*>(bR + (j0 + jj) * NpP);
+            const float4 bs = *reinterpret_cast<const float4*>(bS + (j0 + jj) * NpP);
+            const float v = f4c(a, jj);
+            ur[0] = fmaf(br.x, v, ur[0]); us[0] = fmaf(bs.x, v, us[0]);
+            ur[1] = fmaf(br.y, v, ur[1]); us[1] = fmaf(bs.y, v, us[1]);
+            ur[2] = fmaf(br.z, v, ur[2]); us[2] = fmaf(bs.z, v, us[2]);
+            ur[3] = fmaf(br.w, v, ur[3]); us[3] = fmaf(bs.w, v, us[3]);
+          }
         }
 #pragma unroll
-        for (int jj = 0; jj < 4; ++jj) {
-          if (j0 + jj >= Np) break;
-          const float4 br = *reinterpret_cast<const float4*>(bR + (j0 + jj) * NpP);
-          const float4 bs = *reinterpret_cast<const float4*>(bS + (j0 + jj) * NpP);
+        for (int n = 0; n < 4; ++n) {  // -(a.grad u)
+          const float dx = rx * ur[n] + sx * us[n], dy = ry * ur[n] + sy * us[n];
+          rh[0][n] = -(cax * dx + cay * dy);
+        }
+      } else {
+        // the curl term of the third field is one product pair Dr u + Ds v,
+        // u and v the geometric combinations of the first two fields (both
+        // taken as hi - c):
+        //   TE  Hz' = Dy Ex - Dx Ey = Dr (ry Ex - rx Ey) + Ds (sy Ex - sx Ey),
+        //   TM  Ez' = Dx Hy - Dy Hx = Dr (rx Hy - ry Hx) + Ds (sx Hy - sy Hx);
+        // the gradient of the third field needs Dr q2 and Ds q2.
+        float gr[4] = {0.0f, 0.0f, 0.0f, 0.0f}, gs[4] = {0.0f, 0.0f, 0.0f, 0.0f}, cu[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+        for (int j0 = 0; j0 < Np; j0 += 4) {
+          float4 a[NF];
 #pragma unroll
           for (int c = 0; c < NF; ++c) {
-            const float v = f4c(a[c], jj);
-            ur[c][0] = fmaf(br.x, v, ur[c][0]); us[c][0] = fmaf(bs.x, v, us[c][0]);
-            ur[c][1] = fmaf(br.y, v, ur[c][1]); us[c][1] = fmaf(bs.y, v, us[c][1]);
-            ur[c][2] = fmaf(br.z, v, ur[c][2]); us[c][2] = fmaf(bs.z, v, us[c][2]);
-            ur[c][3] = fmaf(br.w, v, ur[c][3]); us[c][3] = fmaf(bs.w, v, us[c][3]);
+            a[c] = *reinterpret_cast<const float4*>(qe + c * NpP + j0);
+            a[c].x -= cm[c]; a[c].y -= cm[c]; a[c].z -= cm[c]; a[c].w -= cm[c];
+          }
+#pragma unroll
+          for (int jj = 0; jj < 4; ++jj) {
+            if (j0 + jj >= Np) break;
+            const float4 br = *reinterpret_cast<const float4*>(bR + (j0 + jj) * NpP);
+            const float4 bs = *reinterpret_cast<const float4*>(bS + (j0 + jj) * NpP);
+            const float q0 = f4c(a[0], jj), q1 = f4c(a[1], jj), v = f4c(a[2], jj);
+            const float u = (P == PHYS_TE) ? ry * q0 - rx * q1 : rx * q1 - ry * q0;
+            const float w = (P == PHYS_TE) ? sy * q0 - sx * q1 : sx * q1 - sy * q0;
+            gr[0] = fmaf(br.x, v, gr[0]); gs[0] = fmaf(bs.x, v, gs[0]);
+            gr[1] = fmaf(br.y, v, gr[1]); gs[1] = fmaf(bs.y, v, gs[1]);
+            gr[2] = fmaf(br.z, v, gr[2]); gs[2] = fmaf(bs.z, v, gs[2]);
+            gr[3] = fmaf(br.w, v, gr[3]); gs[3] = fmaf(bs.w, v, gs[3]);
+            cu[0] = fmaf(br.x, u, fmaf(bs.x, w, cu[0]));
+            cu[1] = fmaf(br.y, u, fmaf(bs.y, w, cu[1]));
+            cu[2] = fmaf(br.z, u, fmaf(bs.z, w, cu[2]));
+            cu[3] = fmaf(br.w, u, fmaf(bs.w, w, cu[3]));
           }
         }
-      }
-      float rh[NF][4];
-      {
-        const float4 g0 = *reinterpret_cast<const float4*>(sG + slot * 16);  // rx ry sx sy
-        const float rx = g0.x, ry = g0.y, sx = g0.z, sy = g0.w;
 #pragma unroll
         for (int n = 0; n < 4; ++n) {
-          if (P == PHYS_ADV) {  // -(a.grad u)
-            const float dx = rx * ur[0][n] + sx * us[0][n], dy = ry * ur[0][n] + sy * us[0][n];
-            rh[0][n] = -(cax * dx + cay * dy);
-          } else if (P == PHYS_TM) {  // Hx' = -Dy Ez, Hy' = Dx Ez, Ez' = Dx Hy - Dy Hx
-            rh[0][n] = -(ry * ur[2][n] + sy * us[2][n]);
-            rh[1][n] = rx * ur[2][n] + sx * us[2][n];
-            rh[2][n] = (rx * ur[1][n] + sx * us[1][n]) - (ry * ur[0][n] + sy * us[0][n]);
-          } else {                    // Ex' = Dy Hz, Ey' = -Dx Hz, Hz' = Dy Ex - Dx Ey
-            rh[0][n] = ry * ur[2][n] + sy * us[2][n];
-            rh[1][n] = -(rx * ur[2][n] + sx * us[2][n]);
-            rh[2][n] = (ry * ur[0][n] + sy * us[0][n]) - (rx * ur[1][n] + sx * us[1][n]);
+          if (P == PHYS_TM) {  // Hx' = -Dy Ez, Hy' = Dx Ez
+            rh[0][n] = -(ry * gr[n] + sy * gs[n]);
+            rh[1][n] = rx * gr[n] + sx * gs[n];
+          } else {             // Ex' = Dy Hz, Ey' = -Dx Hz
+            rh[0][n] = ry * gr[n] + sy * gs[n];
+            rh[1][n] = -(rx * gr[n] + sx * gs[n]);
           }
+          rh[2][n] = cu[n];
         }
       }
 #pragma unroll

@@ -18,7 +18,7 @@ struct LaunchInfo {
 
 // Launch of a stage kernel that calls grid_dep_wait before it touches the
 // previous launch's data (dg_rhs_blk_kernel, dg_rhs_tcp_kernel,
-// dg_rhs_x2_kernel): with programmatic stream serialization its CTAs are
+// dg_rhs_x2_kernel, dg_batch_kernel): with programmatic stream serialization its CTAs are
 // scheduled, and run their set-up (barriers, operator copies, tensor memory),
 // while the previous kernel of the stream finishes.  DGC_STAGE_OVERLAP=0 in the
 // environment launches them without the attribute.
@@ -30,8 +30,8 @@ inline bool stage_overlap_enabled() {
   return on;
 }
 
-inline cudaError_t launch_stage(void (*kern)(RhsParams), int grid, int threads, size_t smem, cudaStream_t s,
-                                const RhsParams& p) {
+template <typename Arg>
+cudaError_t launch_stage(void (*kern)(Arg), int grid, int threads, size_t smem, cudaStream_t s, const Arg& p) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)grid);
   cfg.blockDim = dim3((unsigned)threads);

@@ -76,9 +76,12 @@ def rhs_x2(hi, lo, t, geo64=False):
     f = [-h * ny * w, h * nx * w, h * (nx * d[1] - ny * d[0] - d[2])]
     L, sc = c(ops["Ls"].T), gc(g["sc"])
     qv = hi - hi[:, :, :1]
-    ur, us = qv @ c(ops["Drs"].T), qv @ c(ops["Dss"].T)
     rx, ry, sx, sy = (gc(g[k]) for k in ("rx", "ry", "sx", "sy"))
-    vol = [ry * ur[2] + sy * us[2], -(rx * ur[2] + sx * us[2]), (ry * ur[0] + sy * us[0]) - (rx * ur[1] + sx * us[1])]
+    Dr, Ds = c(ops["Drs"].T), c(ops["Dss"].T)
+    ur, us = qv[2] @ Dr, qv[2] @ Ds
+    # the curl term as one product pair: Dr (ry Ex - rx Ey) + Ds (sy Ex - sx Ey)
+    u, w = (ry * qv[0] - rx * qv[1]).astype(F32), (sy * qv[0] - sx * qv[1]).astype(F32)
+    vol = [ry * ur + sy * us, -(rx * ur + sx * us), u @ Dr + w @ Ds]
     return np.stack([(v + (fi * sc) @ L).astype(F32) for v, fi in zip(vol, f)])
 
 
