@@ -904,8 +904,7 @@ def measure_equal_error(dg, meshes):
             row = {"n": n, "num_cells": 2 * n * n, "order": N}
             for tag, prec in (("fp64", dg.F64), ("fp32", dg.F32), ("fp32c", dg.F32C)):
                 D = dg.Discretization(m, "maxwell_te", N, prec)
-                if prec == dg.F32:
-                    D.autotune(reps=5)
+                variant = D.autotune(reps=5)[0] if prec == dg.F32 else None
                 x, y = D.node_xy()
                 dt0 = 0.5 * D.info.min_edge / (N + 1) ** 2
                 ns = int(np.ceil(1.0 / dt0))
@@ -925,6 +924,8 @@ def measure_equal_error(dg, meshes):
                 row["steps"] = ns
                 row[tag] = {"rel_l2": err, "ms_to_t1": ms,
                             "gdofs": 3 * D.Np * D.K * 5 * ns / (ms * 1e-3) / 1e9}
+                if variant is not None:
+                    row[tag]["variant"] = variant
                 del D, qa, qb, res, fin
             rows.append(row)
     same = []

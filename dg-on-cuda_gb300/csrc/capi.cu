@@ -107,7 +107,11 @@ __global__ void k_layout_x2(int K, int Nf, int Np, int NpP, int layout, int to_n
   }
 }
 
-__global__ void k_clock(double* t, double dt) { t[0] += dt; }
+__global__ void k_clock(double* t, double dt) {
+  dgk::grid_dep_launch();
+  dgk::grid_dep_wait();  // the step's last stage has read the time
+  t[0] += dt;
+}
 
 template <typename R>
 std::vector<R> pack_mats(const dgc::RefElement& re, const std::vector<double>& Dr, const std::vector<double>& Ds,
@@ -603,8 +607,7 @@ int lserk4_launches(dgc_handle h, void* q_in, void* q_out, void* res, double t, 
     if (int rc = launch(h, p, s)) return rc;
   }
   if (dev_time) {
-    k_clock<<<1, 1, 0, s>>>(h->d_time, dt);
-    CK(cudaGetLastError());
+    CK(dgk::launch_stage(k_clock, 1, 1, 0, s, h->d_time, dt));
     ++h->launches;
   }
   return DGC_OK;

@@ -156,6 +156,98 @@ __global__ void __launch_bounds__(X2Config<N, P>::kThreads, X2Config<N, P>::kMin
     const float* sG = bufG(b);
     const int4* sN = bufN(b);
 
+    // ---- volume (on hi - c): nodes 4 grp .. 4 grp + 3 of element slot.  It
+    //      needs no face data, so it runs first; the residual loads for the
+    //      epilogue are issued after it and complete behind the face phase.
+    const bool mine = slot < TE && slot < ne;
+    float* aux = static_cast<float*>(p.aux);
+    float rh[NF][4];
+    float4 res4[NF];
+    if (mine) {
+      const float* bR = sB + 4 * grp;
+      const float* bS = bR + Np * NpP;
+      const float* qe = sH + slot * ESTR;
+      float cm[NF];
+#pragma unroll
+      for (int c = 0; c < NF; ++c) cm[c] = qe[c * NpP];
+      const float4 g0 = *reinterpret_cast<const float4*>(sG + slot * 16);  // rx ry sx sy
+      const float rx = g0.x, ry = g0.y, sx = g0.z, sy = g0.w;
+      if constexpr (P == PHYS_ADV) {
+        float ur[4] = {0.0f, 0.0f, 0.0f, 0.0f}, us[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+        for (int j0 = 0; j0 < Np; j0 += 4) {
+          float4 a = *reinterpret_cast<const float4*>(qe + j0);
+          a.x -= cm[0]; a.y -= cm[0]; a.z -= cm[0]; a.w -= cm[0];
+#pragma unroll
+          for (int jj = 0; jj < 4; ++jj) {
+            if (j0 + jj >= Np) break;
+            const float4 br = *reinterpret_cast<const float4*>(bR + (j0 + jj) * NpP);
+            const float4 bs = *reinterpret_cast<const float4*>(bS + (j0 + jj) * NpP);
+            const float v = f4c(a, jj);
+            ur[0] = fmaf(br.x, v, ur[0]); us[0] = fmaf(bs.x, v, us[0]);
+            ur[1] = fmaf(br.y, v, ur[1]); us[1] = fmaf(bs.y, v, us[1]);
+            ur[2] = fmaf(br.z, v, ur[2]); us[2] = fmaf(bs.z, v, us[2]);
+            ur[3] = fmaf(br.w, v, ur[3]); us[3] = fmaf(bs.w, v, us[3]);
+          }
+        }
+#pragma unroll
+        for (int n = 0; n < 4; ++n) {  // -(a.grad u)
+          const float dx = rx * ur[n] + sx * us[n], dy = ry * ur[n] + sy * us[n];
+          rh[0][n] = -(cax * dx + cay * dy);
+        }
+      } else {
+        // the curl term of the third field is one product pair Dr u + Ds v,
+        // u and v the geometric combinations of the first two fields (both
+        // taken as hi - c):
+        //   TE  Hz' = Dy Ex - Dx Ey = Dr (ry Ex - rx Ey) + Ds (sy Ex - sx Ey),
+        //   TM  Ez' = Dx Hy - Dy Hx = Dr (rx Hy - ry Hx) + Ds (sx Hy - sy Hx);
+        // the gradient of the third field needs Dr q2 and Ds q2.
+        float gr[4] = {0.0f, 0.0f, 0.0f, 0.0f}, gs[4] = {0.0f, 0.0f, 0.0f, 0.0f}, cu[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+        for (int j0 = 0; j0 < Np; j0 += 4) {
+          float4 a[NF];
+#pragma unroll
+          for (int c = 0; c < NF; ++c) {
+            a[c] = *reinterpret_cast<const float4*>(qe + c * NpP + j0);
+            a[c].x -= cm[c]; a[c].y -= cm[c]; a[c].z -= cm[c]; a[c].w -= cm[c];
+          }
+#pragma unroll
+          for (int jj = 0; jj < 4; ++jj) {
+            if (j0 + jj >= Np) break;
+            const float4 br = *reinterpret_cast<const float4*>(bR + (j0 + jj) * NpP);
+            const float4 bs = *reinterpret_cast<const float4*>(bS + (j0 + jj) * NpP);
+            const float q0 = f4c(a[0], jj), q1 = f4c(a[1], jj), v = f4c(a[2], jj);
+            const float u = (P == PHYS_TE) ? ry * q0 - rx * q1 : rx * q1 - ry * q0;
+            const float w = (P == PHYS_TE) ? sy * q0 - sx * q1 : sx * q1 - sy * q0;
+            gr[0] = fmaf(br.x, v, gr[0]); gs[0] = fmaf(bs.x, v, gs[0]);
+            gr[1] = fmaf(br.y, v, gr[1]); gs[1] = fmaf(bs.y, v, gs[1]);
+            gr[2] = fmaf(br.z, v, gr[2]); gs[2] = fmaf(bs.z, v, gs[2]);
+            gr[3] = fmaf(br.w, v, gr[3]); gs[3] = fmaf(bs.w, v, gs[3]);
+            cu[0] = fmaf(br.x, u, fmaf(bs.x, w, cu[0]));
+            cu[1] = fmaf(br.y, u, fmaf(bs.y, w, cu[1]));
+            cu[2] = fmaf(br.z, u, fmaf(bs.z, w, cu[2]));
+            cu[3] = fmaf(br.w, u, fmaf(bs.w, w, cu[3]));
+          }
+        }
+#pragma unroll
+        for (int n = 0; n < 4; ++n) {
+          if (P == PHYS_TM) {  // Hx' = -Dy Ez, Hy' = Dx Ez
+            rh[0][n] = -(ry * gr[n] + sy * gs[n]);
+            rh[1][n] = rx * gr[n] + sx * gs[n];
+          } else {             // Ex' = Dy Hz, Ey' = -Dx Hz
+            rh[0][n] = ry * gr[n] + sy * gs[n];
+            rh[1][n] = -(rx * gr[n] + sx * gs[n]);
+          }
+          rh[2][n] = cu[n];
+        }
+      }
+      if (p.mode == MODE_LSERK) {
+#pragma unroll
+        for (int c = 0; c < NF; ++c)
+          res4[c] = *reinterpret_cast<const float4*>(aux + (size_t)(k0 + slot) * ESTR + c * NpP + 4 * grp);
+      }
+    }
+
     // ---- face nodes: jumps d = q+ - q- from the hi and lo parts, then the
     // strong-form flux differences, pre-scaled by -faceJ / J.  Item (element
     // e, face-node index dd) takes node dd of the three faces of e.
@@ -231,87 +323,9 @@ __global__ void __launch_bounds__(X2Config<N, P>::kThreads, X2Config<N, P>::kMin
     }
     __syncthreads();
 
-    // ---- volume (on hi - c) + lift + epilogue: nodes 4 grp .. 4 grp + 3 of element slot
-    if (slot < TE && slot < ne) {
-      const float* bR = sB + 4 * grp;
-      const float* bS = bR + Np * NpP;
-      const float* bL = bR + 2 * Np * NpP;
-      const float* qe = sH + slot * ESTR;
-      float cm[NF];
-#pragma unroll
-      for (int c = 0; c < NF; ++c) cm[c] = qe[c * NpP];
-      const float4 g0 = *reinterpret_cast<const float4*>(sG + slot * 16);  // rx ry sx sy
-      const float rx = g0.x, ry = g0.y, sx = g0.z, sy = g0.w;
-      float rh[NF][4];
-      if constexpr (P == PHYS_ADV) {
-        float ur[4] = {0.0f, 0.0f, 0.0f, 0.0f}, us[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-#pragma unroll
-        for (int j0 = 0; j0 < Np; j0 += 4) {
-          float4 a = *reinterpret_cast<const float4*>(qe + j0);
-          a.x -= cm[0]; a.y -= cm[0]; a.z -= cm[0]; a.w -= cm[0];
-#pragma unroll
-          for (int jj = 0; jj < 4; ++jj) {
-            if (j0 + jj >= Np) break;
-            const float4 br = *reinterpret_cast<const float4*>(bR + (j0 + jj) * NpP);
-            const float4 bs = *reinterpret_cast<const float4*>(bS + (j0 + jj) * NpP);
-            const float v = f4c(a, jj);
-            ur[0] = fmaf(br.x, v, ur[0]); us[0] = fmaf(bs.x, v, us[0]);
-            ur[1] = fmaf(br.y, v, ur[1]); us[1] = fmaf(bs.y, v, us[1]);
-            ur[2] = fmaf(br.z, v, ur[2]); us[2] = fmaf(bs.z, v, us[2]);
-            ur[3] = fmaf(br.w, v, ur[3]); us[3] = fmaf(bs.w, v, us[3]);
-          }
-        }
-#pragma unroll
-        for (int n = 0; n < 4; ++n) {  // -(a.grad u)
-          const float dx = rx * ur[n] + sx * us[n], dy = ry * ur[n] + sy * us[n];
-          rh[0][n] = -(cax * dx + cay * dy);
-        }
-      } else {
-        // the curl term of the third field is one product pair Dr u + Ds v,
-        // u and v the geometric combinations of the first two fields (both
-        // taken as hi - c):
-        //   TE  Hz' = Dy Ex - Dx Ey = Dr (ry Ex - rx Ey) + Ds (sy Ex - sx Ey),
-        //   TM  Ez' = Dx Hy - Dy Hx = Dr (rx Hy - ry Hx) + Ds (sx Hy - sy Hx);
-        // the gradient of the third field needs Dr q2 and Ds q2.
-        float gr[4] = {0.0f, 0.0f, 0.0f, 0.0f}, gs[4] = {0.0f, 0.0f, 0.0f, 0.0f}, cu[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-#pragma unroll
-        for (int j0 = 0; j0 < Np; j0 += 4) {
-          float4 a[NF];
-#pragma unroll
-          for (int c = 0; c < NF; ++c) {
-            a[c] = *reinterpret_cast<const float4*>(qe + c * NpP + j0);
-            a[c].x -= cm[c]; a[c].y -= cm[c]; a[c].z -= cm[c]; a[c].w -= cm[c];
-          }
-#pragma unroll
-          for (int jj = 0; jj < 4; ++jj) {
-            if (j0 + jj >= Np) break;
-            const float4 br = *reinterpret_cast<const float4*>(bR + (j0 + jj) * NpP);
-            const float4 bs = *reinterpret_cast<const float4*>(bS + (j0 + jj) * NpP);
-            const float q0 = f4c(a[0], jj), q1 = f4c(a[1], jj), v = f4c(a[2], jj);
-            const float u = (P == PHYS_TE) ? ry * q0 - rx * q1 : rx * q1 - ry * q0;
-            const float w = (P == PHYS_TE) ? sy * q0 - sx * q1 : sx * q1 - sy * q0;
-            gr[0] = fmaf(br.x, v, gr[0]); gs[0] = fmaf(bs.x, v, gs[0]);
-            gr[1] = fmaf(br.y, v, gr[1]); gs[1] = fmaf(bs.y, v, gs[1]);
-            gr[2] = fmaf(br.z, v, gr[2]); gs[2] = fmaf(bs.z, v, gs[2]);
-            gr[3] = fmaf(br.w, v, gr[3]); gs[3] = fmaf(bs.w, v, gs[3]);
-            cu[0] = fmaf(br.x, u, fmaf(bs.x, w, cu[0]));
-            cu[1] = fmaf(br.y, u, fmaf(bs.y, w, cu[1]));
-            cu[2] = fmaf(br.z, u, fmaf(bs.z, w, cu[2]));
-            cu[3] = fmaf(br.w, u, fmaf(bs.w, w, cu[3]));
-          }
-        }
-#pragma unroll
-        for (int n = 0; n < 4; ++n) {
-          if (P == PHYS_TM) {  // Hx' = -Dy Ez, Hy' = Dx Ez
-            rh[0][n] = -(ry * gr[n] + sy * gs[n]);
-            rh[1][n] = rx * gr[n] + sx * gs[n];
-          } else {             // Ex' = Dy Hz, Ey' = -Dx Hz
-            rh[0][n] = ry * gr[n] + sy * gs[n];
-            rh[1][n] = -(rx * gr[n] + sx * gs[n]);
-          }
-          rh[2][n] = cu[n];
-        }
-      }
+    // ---- lift + epilogue
+    if (mine) {
+      const float* bL = sB + 4 * grp + 2 * Np * NpP;
 #pragma unroll
       for (int m0 = 0; m0 < NFACE; m0 += 4) {
         float4 fv[NF];
@@ -335,7 +349,6 @@ __global__ void __launch_bounds__(X2Config<N, P>::kThreads, X2Config<N, P>::kMin
       // ---- epilogue
       float* ohi = static_cast<float*>(p.out);
       float* olo = ohi + nvec;
-      float* aux = static_cast<float*>(p.aux);
       const int nvalid = Np - 4 * grp;
 #pragma unroll
       for (int c = 0; c < NF; ++c) {
@@ -343,7 +356,7 @@ __global__ void __launch_bounds__(X2Config<N, P>::kThreads, X2Config<N, P>::kMin
         float r[4] = {rh[c][0], rh[c][1], rh[c][2], rh[c][3]};
         float h[4] = {0.0f, 0.0f, 0.0f, 0.0f}, l[4] = {0.0f, 0.0f, 0.0f, 0.0f};
         if (p.mode == MODE_LSERK) {
-          const float4 av = *reinterpret_cast<const float4*>(aux + o);
+          const float4 av = res4[c];
           const float4 hv = *reinterpret_cast<const float4*>(sH + slot * ESTR + c * NpP + 4 * grp);
           const float4 lv = *reinterpret_cast<const float4*>(sL + slot * ESTR + c * NpP + 4 * grp);
           const float a4[4] = {av.x, av.y, av.z, av.w};

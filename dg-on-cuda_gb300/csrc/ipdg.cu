@@ -84,8 +84,20 @@ cudaError_t ipdg_blk_launch_n(int kind, const IpdgParams& p, int sm, cudaStream_
   const int ntiles = (p.K + B::TE - 1) / B::TE;
   int grid = sm * (bps[kind] > 0 ? bps[kind] : 1);
   if (grid > ntiles) grid = ntiles;
+  // programmatic dependent launch: the kernels wait (grid_dep_wait) before
+  // their first access to the CG scalars and vectors
   void* args[] = {const_cast<IpdgParams*>(&p)};
-  return cudaLaunchKernel(fn, dim3(grid), dim3(256), args, smem, s);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3(256);
+  cfg.dynamicSmemBytes = (size_t)smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = stage_overlap_enabled() ? 1 : 0;
+  return cudaLaunchKernelExC(&cfg, fn, args);
 }
 
 cudaError_t ipdg_blk_launch(int N, int kind, const IpdgParams& p, int sm, cudaStream_t s) {
@@ -273,6 +285,8 @@ __global__ void k_cg_start(CgScalars* cg, double tol2, int maxit) {
 }
 // convergence bookkeeping, one thread: done when rr <= tol2 * bb or iters >= maxit
 __global__ void k_cg_check(CgScalars* cg, int slot) {
+  grid_dep_launch();
+  grid_dep_wait();  // the update's sums are the previous launch's output
   if (cg->done) return;
   cg->iters += 1;
   if (cg->rr[slot] <= cg->tol2 * cg->bb) cg->done = 1;
@@ -645,8 +659,7 @@ int cg_iteration(dgc_handle_s* h, int cgi, int slot, int first, cudaStream_t s) 
   p.z = wv<R>(h, W_Z);
   p.Ap = wv<R>(h, W_AP);
   if (int rc = run(dgk::IK_UPDATE, dgk::IB_UPDATE)) return rc;
-  dgk::k_cg_check<<<1, 1, 0, s>>>(h->ipdg->cg + cgi, (slot + 1) % 3);
-  CKI(cudaGetLastError());
+  CKI(dgk::launch_stage(dgk::k_cg_check, 1, 1, 0, s, h->ipdg->cg + cgi, (slot + 1) % 3));
   ++h->launches;
   return DGC_OK;
 }

@@ -96,7 +96,7 @@ __global__ void __launch_bounds__(256, 4) ipdg_grad_blk_kernel(const IpdgParams 
   constexpr int Np = B::Np, NpP = B::NpP, Nfp = B::Nfp, NFACE = B::NFACE, NG = B::NG, TE = B::TE;
   constexpr int FSTR = B::FSTR, FS = B::FSG;
   extern __shared__ __align__(128) unsigned char smem[];
-  if (p.cg->done) return;
+  grid_dep_launch();  // the next launch may be scheduled; it waits for this grid before its reads
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem + B::oBar);
   const float4* ops4 = reinterpret_cast<const float4*>(smem + B::oOps);
   float* sF = reinterpret_cast<float*>(smem + B::oFluxG);
@@ -127,12 +127,6 @@ __global__ void __launch_bounds__(256, 4) ipdg_grad_blk_kernel(const IpdgParams 
     bulk_g2s(bufN(b), p.nbr + k0, bn, &bar[b]);
   };
   if (tid == 0) {
-    s_beta = 0.0f;
-    if (!p.first) {
-      const int s = p.slot, sp = (s + 2) % 3;
-      s_beta = (float)(p.cg->rz[s] / p.cg->rz[sp]);
-    }
-    if (blockIdx.x == 0) p.cg->pAp = 0.0;
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
     mbar_init(&bar[2], 1);
@@ -144,9 +138,22 @@ __global__ void __launch_bounds__(256, 4) ipdg_grad_blk_kernel(const IpdgParams 
   if (tid == 0) {
     mbar_arrive_expect_tx(&bar[2], B::kOps);
     bulk_g2s(const_cast<float4*>(ops4), p.mats_blk, B::kOps, &bar[2]);
+  }
+  // the CG scalars and vectors are earlier launches' output; the operators
+  // are set-up data (their copy is in flight already)
+  grid_dep_wait();
+  const bool done = p.cg->done != 0;
+  if (tid == 0 && !done) {
+    s_beta = 0.0f;
+    if (!p.first) {
+      const int s = p.slot, sp = (s + 2) % 3;
+      s_beta = (float)(p.cg->rz[s] / p.cg->rz[sp]);
+    }
+    if (blockIdx.x == 0) p.cg->pAp = 0.0;
     if ((int)blockIdx.x < ntiles) issue(blockIdx.x, 0);
   }
   if (!__syncthreads_and(mbar_wait(&bar[2], 0, p.status))) return;
+  if (done) return;  // converged: nothing in flight once the operators have landed
   const float beta = s_beta;
   uint32_t ph[2] = {0, 0};
   int it = 0;
@@ -280,7 +287,7 @@ __global__ void __launch_bounds__(256, 4) ipdg_div_blk_kernel(const IpdgParams p
   constexpr int Np = B::Np, NpP = B::NpP, Nfp = B::Nfp, NFACE = B::NFACE, NG = B::NG, TE = B::TE;
   constexpr int FS = B::FSD;
   extern __shared__ __align__(128) unsigned char smem[];
-  if (p.cg->done) return;
+  grid_dep_launch();  // the next launch may be scheduled; it waits for this grid before its reads
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem + B::oBar);
   const float4* ops4 = reinterpret_cast<const float4*>(smem + B::oOps);
   const float4* mass4 = reinterpret_cast<const float4*>(smem + B::oMassD);
@@ -318,11 +325,6 @@ __global__ void __launch_bounds__(256, 4) ipdg_div_blk_kernel(const IpdgParams p
     bulk_g2s(bufT(b), static_cast<const float*>(p.tau) + (size_t)k0 * 4, bt, &bar[b]);
   };
   if (tid == 0) {
-    if (blockIdx.x == 0) {
-      const int s1 = (p.slot + 1) % 3;
-      p.cg->rz[s1] = 0.0;
-      p.cg->rr[s1] = 0.0;
-    }
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
     mbar_init(&bar[2], 1);
@@ -334,9 +336,21 @@ __global__ void __launch_bounds__(256, 4) ipdg_div_blk_kernel(const IpdgParams p
     mbar_arrive_expect_tx(&bar[2], B::kOps + B::kMass);
     bulk_g2s(const_cast<float4*>(ops4), p.mats_blk, B::kOps, &bar[2]);
     bulk_g2s(const_cast<float4*>(mass4), p.mass_blk, B::kMass, &bar[2]);
+  }
+  // the CG scalars and vectors are earlier launches' output; the operators
+  // are set-up data (their copy is in flight already)
+  grid_dep_wait();
+  const bool done = p.cg->done != 0;
+  if (tid == 0 && !done) {
+    if (blockIdx.x == 0) {
+      const int s1 = (p.slot + 1) % 3;
+      p.cg->rz[s1] = 0.0;
+      p.cg->rr[s1] = 0.0;
+    }
     if ((int)blockIdx.x < ntiles) issue(blockIdx.x, 0);
   }
   if (!__syncthreads_and(mbar_wait(&bar[2], 0, p.status))) return;
+  if (done) return;  // converged: nothing in flight once the operators have landed
   double dot = 0.0;
   uint32_t ph[2] = {0, 0};
   int it = 0;
@@ -490,7 +504,7 @@ __global__ void __launch_bounds__(256, 2) pcg_update_blk_kernel(const IpdgParams
   constexpr int Np = B::Np, NpP = B::NpP, NG = B::NG, TE = B::TE, PK = B::PK;
   extern __shared__ __align__(128) unsigned char smem[];
   CgScalars* cg = p.cg;
-  if (cg->done) return;
+  grid_dep_launch();  // the next launch may be scheduled; it waits for this grid before its reads
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
   double* red = reinterpret_cast<double*>(smem + B::oBufU + 2 * B::kBufU);
   auto buf = [&](int b, int f) { return reinterpret_cast<float*>(smem + B::oBufU + b * B::kBufU + f * B::kF); };
@@ -525,11 +539,14 @@ __global__ void __launch_bounds__(256, 2) pcg_update_blk_kernel(const IpdgParams
     tab[q] = (uint16_t)(i >= Np ? 0 : (i <= j ? pk_row<Np>(i) + (j - i) : pk_row<Np>(j) + (i - j)));
   }
   if (tid == 0) {
-    s_alpha = (float)(cg->rz[s] / cg->pAp);  // one FP64 division per CTA
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
     fence_barrier_init();
   }
+  // the CG scalars and vectors are earlier launches' output
+  grid_dep_wait();
+  if (cg->done) return;  // nothing issued yet
+  if (tid == 0) s_alpha = (float)(cg->rz[s] / cg->pAp);  // one FP64 division per CTA
   __syncthreads();
   if (tid == 0 && (int)blockIdx.x < ntiles) issue(blockIdx.x, 0);
   const float alpha = s_alpha;

@@ -7,6 +7,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <utility>
 
 #include "dg_rhs.cuh"
 
@@ -18,7 +19,7 @@ struct LaunchInfo {
 
 // Launch of a stage kernel that calls grid_dep_wait before it touches the
 // previous launch's data (dg_rhs_blk_kernel, dg_rhs_tcp_kernel,
-// dg_rhs_x2_kernel, dg_batch_kernel): with programmatic stream serialization its CTAs are
+// dg_rhs_x2_kernel, dg_batch_kernel, the FP32 CG kernels): with programmatic stream serialization its CTAs are
 // scheduled, and run their set-up (barriers, operator copies, tensor memory),
 // while the previous kernel of the stream finishes.  DGC_STAGE_OVERLAP=0 in the
 // environment launches them without the attribute.
@@ -30,8 +31,8 @@ inline bool stage_overlap_enabled() {
   return on;
 }
 
-template <typename Arg>
-cudaError_t launch_stage(void (*kern)(Arg), int grid, int threads, size_t smem, cudaStream_t s, const Arg& p) {
+template <typename... Args, typename... Act>
+cudaError_t launch_stage(void (*kern)(Args...), int grid, int threads, size_t smem, cudaStream_t s, Act&&... args) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)grid);
   cfg.blockDim = dim3((unsigned)threads);
@@ -42,7 +43,7 @@ cudaError_t launch_stage(void (*kern)(Arg), int grid, int threads, size_t smem, 
   at[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = at;
   cfg.numAttrs = stage_overlap_enabled() ? 1 : 0;
-  return cudaLaunchKernelEx(&cfg, kern, p);
+  return cudaLaunchKernelEx(&cfg, kern, std::forward<Act>(args)...);
 }
 
 template <typename R, int N, int P>
