@@ -129,9 +129,8 @@ __global__ void __launch_bounds__(256, 3) dg_batch_kernel(const BatchLaunch b) {
 }
 
 // advance each instance's device time by its step
+// a plain launch: it ends the overlap chain of one step's stage launches
 __global__ void k_batch_clock(int n, double* const* t, const double* dt) {
-  grid_dep_launch();
-  grid_dep_wait();  // the step's last stage has read the times
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) t[i][0] += dt[i];
 }
@@ -365,8 +364,7 @@ extern "C" int dgc_batch_lserk4_run(dgc_batch b, void* const* qa, void* const* q
     const int rc = launch_step(b, cs);
     b->d_params = saved;
     if (rc) return rc;
-    CKB(dgk::launch_stage(dgk::k_batch_clock, (n + 127) / 128, 128, 0, cs, n, (double* const*)b->d_time_ptrs,
-                          (const double*)b->d_dt));
+    dgk::k_batch_clock<<<(n + 127) / 128, 128, 0, cs>>>(n, b->d_time_ptrs, b->d_dt);
     CKB(cudaGetLastError());
     ++b->launches;
     return DGC_OK;

@@ -107,11 +107,10 @@ __global__ void k_layout_x2(int K, int Nf, int Np, int NpP, int layout, int to_n
   }
 }
 
-__global__ void k_clock(double* t, double dt) {
-  dgk::grid_dep_launch();
-  dgk::grid_dep_wait();  // the step's last stage has read the time
-  t[0] += dt;
-}
+// a plain launch: it ends the overlap chain of one step's stage launches, so
+// the next step's launches are not scheduled before this step has finished
+// (an early chain across steps made small meshes ~30 % slower per stage)
+__global__ void k_clock(double* t, double dt) { t[0] += dt; }
 
 template <typename R>
 std::vector<R> pack_mats(const dgc::RefElement& re, const std::vector<double>& Dr, const std::vector<double>& Ds,
@@ -607,7 +606,8 @@ int lserk4_launches(dgc_handle h, void* q_in, void* q_out, void* res, double t, 
     if (int rc = launch(h, p, s)) return rc;
   }
   if (dev_time) {
-    CK(dgk::launch_stage(k_clock, 1, 1, 0, s, h->d_time, dt));
+    k_clock<<<1, 1, 0, s>>>(h->d_time, dt);
+    CK(cudaGetLastError());
     ++h->launches;
   }
   return DGC_OK;

@@ -284,9 +284,8 @@ __global__ void k_cg_start(CgScalars* cg, double tol2, int maxit) {
   if (cg->rr[0] == 0.0) cg->done = 1;
 }
 // convergence bookkeeping, one thread: done when rr <= tol2 * bb or iters >= maxit
+// a plain launch: it ends the overlap chain of one iteration's launches
 __global__ void k_cg_check(CgScalars* cg, int slot) {
-  grid_dep_launch();
-  grid_dep_wait();  // the update's sums are the previous launch's output
   if (cg->done) return;
   cg->iters += 1;
   if (cg->rr[slot] <= cg->tol2 * cg->bb) cg->done = 1;
@@ -659,7 +658,8 @@ int cg_iteration(dgc_handle_s* h, int cgi, int slot, int first, cudaStream_t s) 
   p.z = wv<R>(h, W_Z);
   p.Ap = wv<R>(h, W_AP);
   if (int rc = run(dgk::IK_UPDATE, dgk::IB_UPDATE)) return rc;
-  CKI(dgk::launch_stage(dgk::k_cg_check, 1, 1, 0, s, h->ipdg->cg + cgi, (slot + 1) % 3));
+  dgk::k_cg_check<<<1, 1, 0, s>>>(h->ipdg->cg + cgi, (slot + 1) % 3);
+  CKI(cudaGetLastError());
   ++h->launches;
   return DGC_OK;
 }
