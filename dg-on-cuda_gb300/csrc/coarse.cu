@@ -96,6 +96,12 @@ __global__ void k_coarse_axpy(int64_t n, const double* x, double w, const double
   }
 }
 
+// out = x - w z with z in FP32 (an FP32 operator's output, no FP64 round trip)
+__global__ void k_coarse_axpy_z32(int64_t n, const double* x, double w, const float* __restrict__ z, double* out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = x[i] - w * (double)z[i];
+}
+
 // FP32 copy of an FP64 vector, and back
 __global__ void k_coarse_to_f32(int64_t n, const double* __restrict__ x, float* __restrict__ y) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -184,7 +190,7 @@ __global__ void k_coarse_step_dev(int64_t n, const double* __restrict__ p, const
 // rounding inside the coarse term); t = (r.r, z.r, z.q) of the new residual.  The
 // new z.r goes to the other parity slot: no block reads what another writes.
 __global__ void k_coarse_dir_dev(int64_t n, const double* __restrict__ z, double* __restrict__ p, double* sc,
-                                 const double* __restrict__ t, int cur, int nxt, int first) {
+                                 const double* __restrict__ t, int cur, int nxt, int first, float* __restrict__ p32) {
   __shared__ double s_beta;
   if (threadIdx.x == 0) {
     const double rzo = sc[cur];
@@ -192,8 +198,11 @@ __global__ void k_coarse_dir_dev(int64_t n, const double* __restrict__ z, double
   }
   __syncthreads();
   const double beta = s_beta;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    p[i] = first ? z[i] : z[i] + beta * p[i];
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double v = first ? z[i] : z[i] + beta * p[i];
+    p[i] = v;
+    if (p32) p32[i] = (float)v;  // the next FP32 operator apply's input
+  }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     sc[nxt] = t[1];
     sc[3] = t[0];
@@ -250,11 +259,14 @@ __global__ void k_coarse_gemv(int n, const double* __restrict__ A, const double*
 
 // z[k][j] (+)= xc[agg[k]] on the valid nodes
 __global__ void k_coarse_prolong(int64_t n, int npp, int np, const int32_t* __restrict__ agg,
-                                 const double* __restrict__ xc, int add, double* __restrict__ z) {
+                                 const double* __restrict__ xc, int add, double* __restrict__ z,
+                                 float* __restrict__ z32) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t k = i / npp;
     const double v = (int)(i - k * npp) < np ? xc[agg[k]] : 0.0;
-    z[i] = add ? z[i] + v : v;
+    const double o = add ? z[i] + v : v;
+    z[i] = o;
+    if (z32) z32[i] = (float)o;  // the next FP32 operator apply's input
   }
 }
 
@@ -546,7 +558,7 @@ extern "C" int dgc_coarse_build(dgc_handle h, int cells_per_aggregate, void* str
 }
 
 int dgc::coarse_apply(dgc_handle_s* h, const double* r, const double* binv_r, double* z, bool add, bool fp32,
-                      cudaStream_t s) {
+                      cudaStream_t s, bool binv_r32_ready) {
   CoarseSpace* c = h->coarse;
   if (!c) return set_error(DGC_ERR_ARG, "no coarse space: call dgc_coarse_build first");
   if (c->shift != ipdg_shift(h)) return set_error(DGC_ERR_ARG, "the shift changed since dgc_coarse_build");
@@ -554,31 +566,48 @@ int dgc::coarse_apply(dgc_handle_s* h, const double* r, const double* binv_r, do
   double *w0 = c->d_w[0], *w1 = c->d_w[1], *w2 = c->d_w[2];
   float *f0 = c->d_f[0], *f1 = c->d_f[1];
   const double om = c->omega;
-  // out = S u in FP64, or through the FP32 kernels (the smoothing steps of a preconditioner)
-  auto S = [&](const double* u, double* out) -> int {
-    if (!fp32) return dgc_laplace_spd_apply(h, u, out, s);
-    dgk::k_coarse_to_f32<<<grid1(n), 256, 0, s>>>(n, u, f0);
+  if (fp32) {
+    // the FP32 path keeps the operator's inputs and outputs in FP32 between
+    // kernels: each conversion happens once, inside the kernel that produces
+    // or consumes the value (same values as converting through FP64 vectors)
+    if (!binv_r) {
+      if (int rc = ipdg_block_jacobi_apply_f32(h, r, nullptr, w0, f0, s)) return rc;
+      binv_r = w0;
+    } else if (!binv_r32_ready) {
+      dgk::k_coarse_to_f32<<<grid1(n), 256, 0, s>>>(n, binv_r, f0);
+      ++h->launches;
+    }
+    // P^T r = P0^T (r - w S Binv r)
     if (int rc = ipdg_spd_apply_f32(h, f0, f1, s)) return rc;
-    dgk::k_coarse_to_f64<<<grid1(n), 256, 0, s>>>(n, f1, out);
+    dgk::k_coarse_axpy_z32<<<grid1(n), 256, 0, s>>>(n, r, om, f1, w1);
+    dgk::k_coarse_restrict<<<(c->nagg * 32 + 255) / 256, 256, 0, s>>>(c->nagg, h->NpP, h->Np, c->d_ptr, c->d_cells,
+                                                                    w1, c->d_rc);
+    dgk::k_coarse_gemv<<<(c->nagg * 32 + 255) / 256, 256, 0, s>>>(c->nagg, c->d_ainv, c->d_rc, c->d_xc);
+    // y = P0 x_c;  z (+)= y - w Binv S y
+    dgk::k_coarse_prolong<<<grid1(n), 256, 0, s>>>(n, h->NpP, h->Np, c->d_agg, c->d_xc, 0, w1, f0);
     CKC(cudaGetLastError(), "apply");
-    h->launches += 2;
+    if (int rc = ipdg_spd_apply_f32(h, f0, f1, s)) return rc;
+    if (int rc = ipdg_block_jacobi_apply_f32(h, nullptr, f1, w0, nullptr, s)) return rc;
+    dgk::k_coarse_axpy<<<grid1(n), 256, 0, s>>>(n, w1, om, w0, z, add ? 1 : 0);
+    CKC(cudaGetLastError(), "apply");
+    h->launches += 5;
     return DGC_OK;
-  };
+  }
   // P^T r = P0^T (r - w S Binv r)
   if (!binv_r) {
-    if (int rc = ipdg_block_jacobi_apply(h, r, w0, s, fp32)) return rc;
+    if (int rc = ipdg_block_jacobi_apply(h, r, w0, s, false)) return rc;
     binv_r = w0;
   }
-  if (int rc = S(binv_r, w1)) return rc;
+  if (int rc = dgc_laplace_spd_apply(h, binv_r, w1, s)) return rc;
   dgk::k_coarse_axpy<<<grid1(n), 256, 0, s>>>(n, r, om, w1, w1, 0);
   dgk::k_coarse_restrict<<<(c->nagg * 32 + 255) / 256, 256, 0, s>>>(c->nagg, h->NpP, h->Np, c->d_ptr, c->d_cells, w1,
                                                                   c->d_rc);
   dgk::k_coarse_gemv<<<(c->nagg * 32 + 255) / 256, 256, 0, s>>>(c->nagg, c->d_ainv, c->d_rc, c->d_xc);
   // y = P0 x_c;  z (+)= y - w Binv S y
-  dgk::k_coarse_prolong<<<grid1(n), 256, 0, s>>>(n, h->NpP, h->Np, c->d_agg, c->d_xc, 0, w1);
+  dgk::k_coarse_prolong<<<grid1(n), 256, 0, s>>>(n, h->NpP, h->Np, c->d_agg, c->d_xc, 0, w1, nullptr);
   CKC(cudaGetLastError(), "apply");
-  if (int rc = S(w1, w2)) return rc;
-  if (int rc = ipdg_block_jacobi_apply(h, w2, w0, s, fp32)) return rc;
+  if (int rc = dgc_laplace_spd_apply(h, w1, w2, s)) return rc;
+  if (int rc = ipdg_block_jacobi_apply(h, w2, w0, s, false)) return rc;
   dgk::k_coarse_axpy<<<grid1(n), 256, 0, s>>>(n, w1, om, w0, z, add ? 1 : 0);
   CKC(cudaGetLastError(), "apply");
   h->launches += 5;
@@ -617,8 +646,8 @@ int dgc::two_level_pcg(dgc_handle_s* h, double* x, double* r, double tol2, int m
   // along them until S x loses its accuracy, so z is kept at zero mean.
   const bool singular = !h->desc.dirichlet && c->shift == 0.0;
   auto precondition = [&]() -> int {  // z = Binv r + P A_c^-1 P^T r, Binv and the coarse term in FP32
-    if (int rc = ipdg_block_jacobi_apply(h, r, z, s, true)) return rc;
-    if (int rc = coarse_apply(h, r, z, z, true, true, s)) return rc;
+    if (int rc = ipdg_block_jacobi_apply_f32(h, r, nullptr, z, c->d_f[0], s)) return rc;
+    if (int rc = coarse_apply(h, r, z, z, true, true, s, true)) return rc;
     if (singular) {
       CKC(cudaMemsetAsync(t + 3, 0, 8, s), "mean");
       dgk::k_coarse_valid_sum<<<gr, 256, 0, s>>>(n, h->NpP, h->Np, z, t + 3);
@@ -629,13 +658,15 @@ int dgc::two_level_pcg(dgc_handle_s* h, double* x, double* r, double tol2, int m
     return DGC_OK;
   };
   // q = S p in FP64, or through the FP32 kernels (the caller refines on the FP64 residual)
+  // (FP32: the direction kernel leaves an FP32 copy of p in the first FP32
+  // work vector, which nothing else writes before this apply reads it)
+  float* p32 = op32 ? c->d_f[0] : nullptr;
   auto apply = [&]() -> int {
     if (!op32) return dgc_laplace_spd_apply(h, p, q, s);
-    dgk::k_coarse_to_f32<<<gd, 256, 0, s>>>(n, p, c->d_f[0]);
-    if (int rc = ipdg_spd_apply_f32(h, c->d_f[0], c->d_f[1], s)) return rc;
+    if (int rc = ipdg_spd_apply_f32(h, p32, c->d_f[1], s)) return rc;
     dgk::k_coarse_to_f64<<<gd, 256, 0, s>>>(n, c->d_f[1], q);
     CKC(cudaGetLastError(), "apply");
-    h->launches += 2;
+    h->launches += 1;
     return DGC_OK;
   };
   // read r.r and the stop flag (synchronises the stream)
@@ -650,7 +681,7 @@ int dgc::two_level_pcg(dgc_handle_s* h, double* x, double* r, double tol2, int m
   CKC(cudaMemsetAsync(sc, 0, 8 * 8, s), "scalars");
   if (int rc = precondition()) return rc;
   if (int rc = dots({{r, z, nullptr}, {r, r, nullptr}})) return rc;
-  dgk::k_coarse_dir_dev<<<gd, 256, 0, s>>>(n, z, p, sc, t, 0, 0, 1);  // p = z, sc[0] = z.r, sc[3] = r.r
+  dgk::k_coarse_dir_dev<<<gd, 256, 0, s>>>(n, z, p, sc, t, 0, 0, 1, p32);  // p = z, sc[0] = z.r, sc[3] = r.r
   CKC(cudaGetLastError(), "start");
   double rr = 0.0;
   bool stop = false;
@@ -666,7 +697,7 @@ int dgc::two_level_pcg(dgc_handle_s* h, double* x, double* r, double tol2, int m
     dgk::k_coarse_step_dev<<<gd, 256, 0, s>>>(n, p, q, x, r, sc, t, cur);
     if (int rc = precondition()) return rc;
     if (int rc = dots({{r, z, z}, {r, r, q}})) return rc;
-    dgk::k_coarse_dir_dev<<<gd, 256, 0, s>>>(n, z, p, sc, t, cur, cur ^ 1, 0);
+    dgk::k_coarse_dir_dev<<<gd, 256, 0, s>>>(n, z, p, sc, t, cur, cur ^ 1, 0, p32);
     CKC(cudaGetLastError(), "update");
     h->launches += 2;
     ++it;

@@ -68,13 +68,19 @@ void ipdg_operators_changed(dgc_handle_s* h);
 // (FP64 vectors; the blocks and sums in FP32 with fp32)
 int ipdg_build_preconditioner(dgc_handle_s* h, cudaStream_t s);
 int ipdg_block_jacobi_apply(dgc_handle_s* h, const double* r, double* z, cudaStream_t s, bool fp32 = false);
+// z = Binv r with the FP32 blocks, r given in FP64 (r64) or FP32 (r32, used when
+// non-null); z32, when non-null, receives an FP32 copy of z
+int ipdg_block_jacobi_apply_f32(dgc_handle_s* h, const double* r64, const float* r32, double* z, float* z32,
+                                cudaStream_t s);
 // the SPD form's shift, and whether the boundary types are the handle's uniform ones
 double ipdg_shift(const dgc_handle_s* h);
 bool ipdg_uniform_bc(const dgc_handle_s* h);
 // coarse space (csrc/coarse.cu): z (+)= P A_c^-1 P^T r (binv_r = Binv r when the
-// caller has it, else NULL; fp32: the two smoothing applies of S in FP32); freeing
+// caller has it, else NULL; fp32: the two smoothing applies of S in FP32, and
+// binv_r32, when non-null, an FP32 copy of binv_r the caller already holds in
+// the coarse space's first FP32 work vector); freeing
 int coarse_apply(dgc_handle_s* h, const double* r, const double* binv_r, double* z, bool add, bool fp32,
-                 cudaStream_t s);
+                 cudaStream_t s, bool binv_r32_ready = false);
 void coarse_free(CoarseSpace* c);
 // flexible PCG with M = Binv + coarse term from the residual r (updated) on x, until
 // r.r <= tol2 or maxit iterations; op32: S applied through the FP32 kernels

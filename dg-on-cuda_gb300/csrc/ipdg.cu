@@ -422,9 +422,12 @@ int ipdg_build_preconditioner(dgc_handle_s* h, cudaStream_t s) {
 // E * NpP) and stages r once per node in shared memory, in B's type: converted
 // per (node, j) instead, the FP32 form took as long as the FP64 one (FP64 work,
 // conversions included, is slow on GB300).
-template <typename B>
+// The residual may also come as an FP32 vector (RIn = float: the two-level
+// cycle's FP32 operator output, no FP64 round trip), and z32, when given,
+// receives an FP32 copy of z (the input of the next FP32 operator apply).
+template <typename B, typename RIn = double>
 __global__ void k_bj_apply(int K, int Np, int NpP, int bstr, const B* __restrict__ binv,
-                           const double* __restrict__ r, double* __restrict__ z) {
+                           const RIn* __restrict__ r, double* __restrict__ z, float* __restrict__ z32) {
   __shared__ B rs[256];
   const int E = blockDim.x / NpP;
   const int t = threadIdx.x, e = t / NpP, i = t - e * NpP;
@@ -440,6 +443,7 @@ __global__ void k_bj_apply(int K, int Np, int NpP, int bstr, const B* __restrict
     for (int j = 0; j < Np; ++j) s += Bk[j * Np + i] * rk[j];
   }
   z[k * NpP + i] = (double)s;
+  if (z32) z32[k * NpP + i] = (float)s;
 }
 
 int ipdg_block_jacobi_apply(dgc_handle_s* h, const double* r, double* z, cudaStream_t s, bool fp32) {
@@ -448,9 +452,24 @@ int ipdg_block_jacobi_apply(dgc_handle_s* h, const double* r, double* z, cudaStr
   const int E = 256 / h->NpP;  // whole elements per CTA (NpP <= 48)
   const unsigned grid = (unsigned)((h->K + E - 1) / E), block = (unsigned)(E * h->NpP);
   if (fp32)
-    k_bj_apply<float><<<grid, block, 0, s>>>(h->K, h->Np, h->NpP, st->bstr, st->binv32, r, z);
+    k_bj_apply<float><<<grid, block, 0, s>>>(h->K, h->Np, h->NpP, st->bstr, st->binv32, r, z, nullptr);
   else
-    k_bj_apply<double><<<grid, block, 0, s>>>(h->K, h->Np, h->NpP, st->bstr, st->binv64, r, z);
+    k_bj_apply<double><<<grid, block, 0, s>>>(h->K, h->Np, h->NpP, st->bstr, st->binv64, r, z, nullptr);
+  CKI(cudaGetLastError());
+  ++h->launches;
+  return DGC_OK;
+}
+
+int ipdg_block_jacobi_apply_f32(dgc_handle_s* h, const double* r64, const float* r32, double* z, float* z32,
+                                cudaStream_t s) {
+  if (int rc = ipdg_build_preconditioner(h, s)) return rc;
+  const IpdgState* st = h->ipdg;
+  const int E = 256 / h->NpP;
+  const unsigned grid = (unsigned)((h->K + E - 1) / E), block = (unsigned)(E * h->NpP);
+  if (r32)
+    k_bj_apply<float, float><<<grid, block, 0, s>>>(h->K, h->Np, h->NpP, st->bstr, st->binv32, r32, z, z32);
+  else
+    k_bj_apply<float, double><<<grid, block, 0, s>>>(h->K, h->Np, h->NpP, st->bstr, st->binv32, r64, z, z32);
   CKI(cudaGetLastError());
   ++h->launches;
   return DGC_OK;
