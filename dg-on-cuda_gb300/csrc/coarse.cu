@@ -53,7 +53,9 @@ struct CoarseSpace {
   int32_t* d_cells = nullptr;         // [K]
   int32_t* d_agg = nullptr;           // [K]
   double* d_ainv = nullptr;           // [nagg][nagg] A_c^-1
+  float* d_ainv32 = nullptr;          // FP32 copy of A_c^-1 (the FP32 coarse cycle)
   double* d_rc = nullptr;             // P^T r
+  float* d_rc32 = nullptr;            // FP32 copy of P^T r
   double* d_xc = nullptr;             // A_c^-1 P^T r
   double* d_w[3] = {};                // work vectors (K x NpP)
   float* d_f[2] = {};                 // FP32 work vectors of the FP32 smoothing applies
@@ -68,7 +70,7 @@ void coarse_free(CoarseSpace* c) {
   for (void* p : {(void*)c->d_ptr, (void*)c->d_cells, (void*)c->d_agg, (void*)c->d_ainv, (void*)c->d_rc,
                   (void*)c->d_xc, (void*)c->d_w[0], (void*)c->d_w[1], (void*)c->d_w[2], (void*)c->d_f[0],
                   (void*)c->d_f[1], (void*)c->d_pcg[0], (void*)c->d_pcg[1], (void*)c->d_pcg[2],
-                  (void*)c->d_dots, (void*)c->d_sc})
+                  (void*)c->d_dots, (void*)c->d_sc, (void*)c->d_ainv32, (void*)c->d_rc32})
     cudaFree(p);
   cudaFreeHost(c->h_sc);
   delete c;
@@ -231,7 +233,7 @@ __global__ void k_gj_elim(int n, int i, double* __restrict__ A, const double* __
 // rc[a] = sum of r over the valid nodes of the cells of aggregate a (fixed order)
 __global__ void k_coarse_restrict(int nagg, int npp, int np, const int32_t* __restrict__ ptr,
                                   const int32_t* __restrict__ cells, const double* __restrict__ r,
-                                  double* __restrict__ rc) {
+                                  double* __restrict__ rc, float* __restrict__ rc32) {
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (warp >= nagg) return;
   double s = 0.0;
@@ -241,7 +243,10 @@ __global__ void k_coarse_restrict(int nagg, int npp, int np, const int32_t* __re
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-  if (lane == 0) rc[warp] = s;
+  if (lane == 0) {
+    rc[warp] = s;
+    if (rc32) rc32[warp] = (float)s;
+  }
 }
 
 // xc = Ainv rc, one warp per row
@@ -255,6 +260,20 @@ __global__ void k_coarse_gemv(int n, const double* __restrict__ A, const double*
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
   if (lane == 0) y[row] = s;
+}
+
+// the same product with the FP32 copy of A_c^-1 and of x, FP32 sums (inside the
+// FP32 coarse cycle): half the bytes and no FP64 arithmetic
+__global__ void k_coarse_gemv32(int n, const float* __restrict__ A, const float* __restrict__ x,
+                                double* __restrict__ y) {
+  const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (row >= n) return;
+  const float* a = A + (size_t)row * n;
+  float s = 0.0f;
+  for (int c = lane; c < n; c += 32) s = fmaf(a[c], x[c], s);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) y[row] = (double)s;
 }
 
 // z[k][j] (+)= xc[agg[k]] on the valid nodes
@@ -549,9 +568,13 @@ extern "C" int dgc_coarse_build(dgc_handle h, int cells_per_aggregate, void* str
     dgk::k_gj_row<<<(nagg + 127) / 128, 128, 0, s>>>(nagg, i, c->d_ainv, c->d_rc);
     dgk::k_gj_elim<<<eg, 128, 0, s>>>(nagg, i, c->d_ainv, c->d_rc);
   }
+  if ((e = cudaMalloc(&c->d_ainv32, (size_t)nagg * nagg * 4)) != cudaSuccess ||
+      (e = cudaMalloc(&c->d_rc32, (size_t)nagg * 4)) != cudaSuccess)
+    return fail(cfail(e, "allocation"));
+  dgk::k_coarse_to_f32<<<grid1((int64_t)nagg * nagg), 256, 0, s>>>((int64_t)nagg * nagg, c->d_ainv, c->d_ainv32);
   if ((e = cudaGetLastError()) != cudaSuccess || (e = cudaStreamSynchronize(s)) != cudaSuccess)
     return fail(cfail(e, "inversion"));
-  h->launches += 3 * (int64_t)ncol + 3 * (int64_t)nagg;
+  h->launches += 3 * (int64_t)ncol + 3 * (int64_t)nagg + 1;
   cudaFree(d_color);
   h->coarse = c;
   return DGC_OK;
@@ -581,8 +604,8 @@ int dgc::coarse_apply(dgc_handle_s* h, const double* r, const double* binv_r, do
     if (int rc = ipdg_spd_apply_f32(h, f0, f1, s)) return rc;
     dgk::k_coarse_axpy_z32<<<grid1(n), 256, 0, s>>>(n, r, om, f1, w1);
     dgk::k_coarse_restrict<<<(c->nagg * 32 + 255) / 256, 256, 0, s>>>(c->nagg, h->NpP, h->Np, c->d_ptr, c->d_cells,
-                                                                    w1, c->d_rc);
-    dgk::k_coarse_gemv<<<(c->nagg * 32 + 255) / 256, 256, 0, s>>>(c->nagg, c->d_ainv, c->d_rc, c->d_xc);
+                                                                    w1, c->d_rc, c->d_rc32);
+    dgk::k_coarse_gemv32<<<(c->nagg * 32 + 255) / 256, 256, 0, s>>>(c->nagg, c->d_ainv32, c->d_rc32, c->d_xc);
     // y = P0 x_c;  z (+)= y - w Binv S y
     dgk::k_coarse_prolong<<<grid1(n), 256, 0, s>>>(n, h->NpP, h->Np, c->d_agg, c->d_xc, 0, w1, f0);
     CKC(cudaGetLastError(), "apply");
@@ -601,7 +624,7 @@ int dgc::coarse_apply(dgc_handle_s* h, const double* r, const double* binv_r, do
   if (int rc = dgc_laplace_spd_apply(h, binv_r, w1, s)) return rc;
   dgk::k_coarse_axpy<<<grid1(n), 256, 0, s>>>(n, r, om, w1, w1, 0);
   dgk::k_coarse_restrict<<<(c->nagg * 32 + 255) / 256, 256, 0, s>>>(c->nagg, h->NpP, h->Np, c->d_ptr, c->d_cells, w1,
-                                                                  c->d_rc);
+                                                                  c->d_rc, nullptr);
   dgk::k_coarse_gemv<<<(c->nagg * 32 + 255) / 256, 256, 0, s>>>(c->nagg, c->d_ainv, c->d_rc, c->d_xc);
   // y = P0 x_c;  z (+)= y - w Binv S y
   dgk::k_coarse_prolong<<<grid1(n), 256, 0, s>>>(n, h->NpP, h->Np, c->d_agg, c->d_xc, 0, w1, nullptr);

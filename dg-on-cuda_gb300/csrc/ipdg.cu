@@ -446,6 +446,44 @@ __global__ void k_bj_apply(int K, int Np, int NpP, int bstr, const B* __restrict
   if (z32) z32[k * NpP + i] = (float)s;
 }
 
+// z = Binv r with the packed FP32 blocks (upper triangles row by row, PK floats
+// per element: the layout the register-blocked CG update stages), for the
+// two-level cycle: 496 instead of 900 bytes of blocks per element at N = 4.
+// A CTA holds whole elements; it copies their packed blocks (contiguous) and
+// residuals into shared memory, and thread (element, node i) sums over j with
+// B(i, j) = B(min, max) through a per-CTA table of packed indices.
+template <typename RIn>
+__global__ void k_bj_apply_pk(int K, int Np, int NpP, int PK, const float* __restrict__ bpk,
+                              const RIn* __restrict__ r, double* __restrict__ z, float* __restrict__ z32) {
+  extern __shared__ __align__(16) float sm_pk[];
+  const int E = blockDim.x / NpP;
+  float* sB = sm_pk;                  // [E][PK]
+  float* sR = sB + E * PK;            // [E][NpP]
+  uint16_t* tab = reinterpret_cast<uint16_t*>(sR + E * NpP);  // [Np][NpP]
+  const int t = threadIdx.x, e = t / NpP, i = t - e * NpP;
+  const int64_t k0 = (int64_t)blockIdx.x * E;
+  const int ne = (int)min((int64_t)E, (int64_t)K - k0);
+  const float4* src = reinterpret_cast<const float4*>(bpk + k0 * PK);
+  for (int x = t; x < ne * PK / 4; x += blockDim.x) reinterpret_cast<float4*>(sB)[x] = src[x];
+  if (e < ne) sR[t] = (float)r[(k0 + e) * NpP + i];
+  for (int q = t; q < Np * NpP; q += blockDim.x) {
+    const int j = q / NpP, ii = q - j * NpP;
+    const int lo = ii < j ? ii : j, hi = ii < j ? j : ii;
+    tab[q] = (uint16_t)(ii >= Np ? 0 : lo * Np - lo * (lo - 1) / 2 + (hi - lo));
+  }
+  __syncthreads();
+  if (e >= ne) return;
+  float acc = 0.0f;
+  if (i < Np) {
+    const float* Bk = sB + e * PK;
+    const float* rk = sR + e * NpP;
+    for (int j = 0; j < Np; ++j) acc += Bk[tab[j * NpP + i]] * rk[j];
+  }
+  const int64_t o = (k0 + e) * NpP + i;
+  z[o] = (double)acc;
+  if (z32) z32[o] = acc;
+}
+
 int ipdg_block_jacobi_apply(dgc_handle_s* h, const double* r, double* z, cudaStream_t s, bool fp32) {
   if (int rc = ipdg_build_preconditioner(h, s)) return rc;
   const IpdgState* st = h->ipdg;
@@ -466,10 +504,12 @@ int ipdg_block_jacobi_apply_f32(dgc_handle_s* h, const double* r64, const float*
   const IpdgState* st = h->ipdg;
   const int E = 256 / h->NpP;
   const unsigned grid = (unsigned)((h->K + E - 1) / E), block = (unsigned)(E * h->NpP);
+  const int Np = h->Np, PK0 = (Np * (Np + 1) / 2 + 3) / 4 * 4, PK = (PK0 / 4) % 2 == 0 ? PK0 + 4 : PK0;
+  const size_t smem = (size_t)E * PK * 4 + (size_t)E * h->NpP * 4 + (size_t)Np * h->NpP * 2;
   if (r32)
-    k_bj_apply<float, float><<<grid, block, 0, s>>>(h->K, h->Np, h->NpP, st->bstr, st->binv32, r32, z, z32);
+    k_bj_apply_pk<float><<<grid, block, smem, s>>>(h->K, Np, h->NpP, PK, st->binv_pk32, r32, z, z32);
   else
-    k_bj_apply<float, double><<<grid, block, 0, s>>>(h->K, h->Np, h->NpP, st->bstr, st->binv32, r64, z, z32);
+    k_bj_apply_pk<double><<<grid, block, smem, s>>>(h->K, Np, h->NpP, PK, st->binv_pk32, r64, z, z32);
   CKI(cudaGetLastError());
   ++h->launches;
   return DGC_OK;
