@@ -22,6 +22,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -169,7 +170,16 @@ int bcuda(cudaError_t e, const char* what) {
     if (e_ != cudaSuccess) return bcuda(e_, #call);    \
   } while (0)
 
-constexpr int kChunk = 8;  // tiles per work item
+constexpr int kChunk = 8;  // tiles per work item (DGC_BATCH_CHUNK overrides, 1..64)
+
+int chunk_tiles() {
+  static const int c = [] {
+    const char* v = std::getenv("DGC_BATCH_CHUNK");
+    const int x = v ? std::atoi(v) : 0;
+    return x >= 1 && x <= 64 ? x : kChunk;
+  }();
+  return c;
+}
 
 int physics_kind(int phys) {
   return phys == DGC_ADVECTION ? dgk::PHYS_ADV : (phys == DGC_MAXWELL_TM ? dgk::PHYS_TM : dgk::PHYS_TE);
@@ -265,8 +275,9 @@ extern "C" int dgc_batch_create(const dgc_handle* handles, int n, dgc_batch* out
     b->smem = std::max(b->smem, li.smem);
     b->tile_size.push_back(te);
     const int ntiles = (h->K + te - 1) / te;
-    for (int t0 = 0; t0 < ntiles; t0 += kChunk) {
-      const int nt = std::min(kChunk, ntiles - t0);
+    const int chunk = chunk_tiles();
+    for (int t0 = 0; t0 < ntiles; t0 += chunk) {
+      const int nt = std::min(chunk, ntiles - t0);
       const int ne = std::min(nt * te, h->K - t0 * te);
       items.push_back({i, t0, nt, (double)ne * h->Nf * h->Np * (double)h->Np});
     }
