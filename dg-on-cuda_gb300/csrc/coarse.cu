@@ -141,6 +141,53 @@ __global__ void k_coarse_dots(int64_t n, Dot3 d, double* __restrict__ out) {
     atomicAdd(&out[threadIdx.x], v);
   }
 }
+// block sums of up to three partial dot products, one FP64 atomic per block and product
+__device__ __forceinline__ void block_dots_add(const double (&s)[3], int used, double* out) {
+  __shared__ double red[3][8];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    double v = s[j];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) red[j][w] = v;
+  }
+  __syncthreads();
+  if ((int)threadIdx.x < used) {
+    double v = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) v += red[threadIdx.x][q];
+    atomicAdd(&out[threadIdx.x], v);
+  }
+}
+// q = x32 in FP64 and out[0] += p.q (the FP32 operator output of the two-level
+// iteration, and the dot product its step needs)
+__global__ void k_coarse_to_f64_dot(int64_t n, const float* __restrict__ x32, double* __restrict__ q,
+                                    const double* __restrict__ p, double* out) {
+  double s[3] = {0.0, 0.0, 0.0};
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double v = (double)x32[i];
+    q[i] = v;
+    s[0] += p[i] * v;
+  }
+  block_dots_add(s, 1, out);
+}
+// z += x - w y, then out += (r.r, z.r, z.q) with the new z (the last kernel of the
+// two-level preconditioner and the dot products of the direction update)
+__global__ void k_coarse_axpy_dots(int64_t n, const double* __restrict__ x, double w, const double* __restrict__ y,
+                                   double* __restrict__ z, const double* __restrict__ r,
+                                   const double* __restrict__ q, double* out) {
+  double s[3] = {0.0, 0.0, 0.0};
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double zi = z[i] + (x[i] - w * y[i]);
+    z[i] = zi;
+    const double ri = r[i];
+    s[0] += ri * ri;
+    s[1] += zi * ri;
+    s[2] += zi * q[i];
+  }
+  block_dots_add(s, 3, out);
+}
+
 // out += sum of z over the valid nodes; z -= *out / count on the valid nodes
 __global__ void k_coarse_valid_sum(int64_t n, int npp, int np, const double* __restrict__ z, double* out) {
   double v = 0.0;
@@ -581,7 +628,7 @@ extern "C" int dgc_coarse_build(dgc_handle h, int cells_per_aggregate, void* str
 }
 
 int dgc::coarse_apply(dgc_handle_s* h, const double* r, const double* binv_r, double* z, bool add, bool fp32,
-                      cudaStream_t s, bool binv_r32_ready) {
+                      cudaStream_t s, bool binv_r32_ready, const CoarseDots* dots) {
   CoarseSpace* c = h->coarse;
   if (!c) return set_error(DGC_ERR_ARG, "no coarse space: call dgc_coarse_build first");
   if (c->shift != ipdg_shift(h)) return set_error(DGC_ERR_ARG, "the shift changed since dgc_coarse_build");
@@ -611,7 +658,12 @@ int dgc::coarse_apply(dgc_handle_s* h, const double* r, const double* binv_r, do
     CKC(cudaGetLastError(), "apply");
     if (int rc = ipdg_spd_apply_f32(h, f0, f1, s)) return rc;
     if (int rc = ipdg_block_jacobi_apply_f32(h, nullptr, f1, w0, nullptr, s)) return rc;
-    dgk::k_coarse_axpy<<<grid1(n), 256, 0, s>>>(n, w1, om, w0, z, add ? 1 : 0);
+    if (dots && add) {
+      CKC(cudaMemsetAsync(dots->out, 0, 3 * 8, s), "dots");
+      dgk::k_coarse_axpy_dots<<<dots->grid, 256, 0, s>>>(n, w1, om, w0, z, dots->r, dots->q, dots->out);
+    } else {
+      dgk::k_coarse_axpy<<<grid1(n), 256, 0, s>>>(n, w1, om, w0, z, add ? 1 : 0);
+    }
     CKC(cudaGetLastError(), "apply");
     h->launches += 5;
     return DGC_OK;
@@ -668,9 +720,12 @@ int dgc::two_level_pcg(dgc_handle_s* h, double* x, double* r, double tol2, int m
   // FP32 smoothing leaks a little of them into the coarse term; unchecked, x drifts
   // along them until S x loses its accuracy, so z is kept at zero mean.
   const bool singular = !h->desc.dirichlet && c->shift == 0.0;
-  auto precondition = [&]() -> int {  // z = Binv r + P A_c^-1 P^T r, Binv and the coarse term in FP32
+  // with `fused`, the preconditioner's last kernel also forms (r.r, z.r, z.q)
+  // in t (not for the singular system, whose z changes once more afterwards)
+  auto precondition = [&](bool fused) -> int {  // z = Binv r + P A_c^-1 P^T r, Binv and the coarse term in FP32
     if (int rc = ipdg_block_jacobi_apply_f32(h, r, nullptr, z, c->d_f[0], s)) return rc;
-    if (int rc = coarse_apply(h, r, z, z, true, true, s, true)) return rc;
+    const CoarseDots cd{t, r, q, gr};
+    if (int rc = coarse_apply(h, r, z, z, true, true, s, true, fused && !singular ? &cd : nullptr)) return rc;
     if (singular) {
       CKC(cudaMemsetAsync(t + 3, 0, 8, s), "mean");
       dgk::k_coarse_valid_sum<<<gr, 256, 0, s>>>(n, h->NpP, h->Np, z, t + 3);
@@ -687,7 +742,9 @@ int dgc::two_level_pcg(dgc_handle_s* h, double* x, double* r, double tol2, int m
   auto apply = [&]() -> int {
     if (!op32) return dgc_laplace_spd_apply(h, p, q, s);
     if (int rc = ipdg_spd_apply_f32(h, p32, c->d_f[1], s)) return rc;
-    dgk::k_coarse_to_f64<<<gd, 256, 0, s>>>(n, c->d_f[1], q);
+    // q back in FP64, with t[0] = p.q for the step
+    CKC(cudaMemsetAsync(t, 0, 3 * 8, s), "dots");
+    dgk::k_coarse_to_f64_dot<<<gr, 256, 0, s>>>(n, c->d_f[1], q, p, t);
     CKC(cudaGetLastError(), "apply");
     h->launches += 1;
     return DGC_OK;
@@ -702,7 +759,7 @@ int dgc::two_level_pcg(dgc_handle_s* h, double* x, double* r, double tol2, int m
     return DGC_OK;
   };
   CKC(cudaMemsetAsync(sc, 0, 8 * 8, s), "scalars");
-  if (int rc = precondition()) return rc;
+  if (int rc = precondition(false)) return rc;
   if (int rc = dots({{r, z, nullptr}, {r, r, nullptr}})) return rc;
   dgk::k_coarse_dir_dev<<<gd, 256, 0, s>>>(n, z, p, sc, t, 0, 0, 1, p32);  // p = z, sc[0] = z.r, sc[3] = r.r
   CKC(cudaGetLastError(), "start");
@@ -716,10 +773,12 @@ int dgc::two_level_pcg(dgc_handle_s* h, double* x, double* r, double tol2, int m
   while (rr > tol2 && !stop && it < maxit) {
     const int cur = it & 1;
     if (int rc = apply()) return rc;
-    if (int rc = dots({{p, nullptr, nullptr}, {q, nullptr, nullptr}})) return rc;
+    if (!op32)  // the FP32 apply forms p.q while it converts q
+      if (int rc = dots({{p, nullptr, nullptr}, {q, nullptr, nullptr}})) return rc;
     dgk::k_coarse_step_dev<<<gd, 256, 0, s>>>(n, p, q, x, r, sc, t, cur);
-    if (int rc = precondition()) return rc;
-    if (int rc = dots({{r, z, z}, {r, r, q}})) return rc;
+    if (int rc = precondition(true)) return rc;
+    if (singular)
+      if (int rc = dots({{r, z, z}, {r, r, q}})) return rc;
     dgk::k_coarse_dir_dev<<<gd, 256, 0, s>>>(n, z, p, sc, t, cur, cur ^ 1, 0, p32);
     CKC(cudaGetLastError(), "update");
     h->launches += 2;

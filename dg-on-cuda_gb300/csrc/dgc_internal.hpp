@@ -79,8 +79,16 @@ bool ipdg_uniform_bc(const dgc_handle_s* h);
 // caller has it, else NULL; fp32: the two smoothing applies of S in FP32, and
 // binv_r32, when non-null, an FP32 copy of binv_r the caller already holds in
 // the coarse space's first FP32 work vector); freeing
+// dots, when non-null (FP32 path with add), makes the last kernel also form
+// out = (r.r, z.r, z.q) with the new z, on `grid` blocks
+struct CoarseDots {
+  double* out;
+  const double* r;
+  const double* q;
+  int grid;
+};
 int coarse_apply(dgc_handle_s* h, const double* r, const double* binv_r, double* z, bool add, bool fp32,
-                 cudaStream_t s, bool binv_r32_ready = false);
+                 cudaStream_t s, bool binv_r32_ready = false, const CoarseDots* dots = nullptr);
 void coarse_free(CoarseSpace* c);
 // flexible PCG with M = Binv + coarse term from the residual r (updated) on x, until
 // r.r <= tol2 or maxit iterations; op32: S applied through the FP32 kernels

@@ -9,6 +9,7 @@
 #include <cstdio>
 #include <cstring>
 #include <mutex>
+#include <type_traits>
 #include <vector>
 
 #include "dgc_internal.hpp"
@@ -452,9 +453,12 @@ __global__ void k_bj_apply(int K, int Np, int NpP, int bstr, const B* __restrict
 // A CTA holds whole elements; it copies their packed blocks (contiguous) and
 // residuals into shared memory, and thread (element, node i) sums over j with
 // B(i, j) = B(min, max) through a per-CTA table of packed indices.
-template <typename RIn>
-__global__ void k_bj_apply_pk(int K, int Np, int NpP, int PK, const float* __restrict__ bpk,
-                              const RIn* __restrict__ r, double* __restrict__ z, float* __restrict__ z32) {
+template <int N, typename RIn>
+__global__ void k_bj_apply_pk(int K, const float* __restrict__ bpk, const RIn* __restrict__ r,
+                              double* __restrict__ z, float* __restrict__ z32) {
+  // compile-time sizes: the j loop unrolls, so the block and residual reads of
+  // a thread are independent loads issued back to back
+  constexpr int Np = dgk::IpdgBlk<N>::Np, NpP = dgk::IpdgBlk<N>::NpP, PK = dgk::IpdgBlk<N>::PK;
   extern __shared__ __align__(16) float sm_pk[];
   const int E = blockDim.x / NpP;
   float* sB = sm_pk;                  // [E][PK]
@@ -477,6 +481,7 @@ __global__ void k_bj_apply_pk(int K, int Np, int NpP, int PK, const float* __res
   if (i < Np) {
     const float* Bk = sB + e * PK;
     const float* rk = sR + e * NpP;
+#pragma unroll
     for (int j = 0; j < Np; ++j) acc += Bk[tab[j * NpP + i]] * rk[j];
   }
   const int64_t o = (k0 + e) * NpP + i;
@@ -504,12 +509,26 @@ int ipdg_block_jacobi_apply_f32(dgc_handle_s* h, const double* r64, const float*
   const IpdgState* st = h->ipdg;
   const int E = 256 / h->NpP;
   const unsigned grid = (unsigned)((h->K + E - 1) / E), block = (unsigned)(E * h->NpP);
-  const int Np = h->Np, PK0 = (Np * (Np + 1) / 2 + 3) / 4 * 4, PK = (PK0 / 4) % 2 == 0 ? PK0 + 4 : PK0;
-  const size_t smem = (size_t)E * PK * 4 + (size_t)E * h->NpP * 4 + (size_t)Np * h->NpP * 2;
-  if (r32)
-    k_bj_apply_pk<float><<<grid, block, smem, s>>>(h->K, Np, h->NpP, PK, st->binv_pk32, r32, z, z32);
-  else
-    k_bj_apply_pk<double><<<grid, block, smem, s>>>(h->K, Np, h->NpP, PK, st->binv_pk32, r64, z, z32);
+  auto go = [&](auto nc) {
+    constexpr int N = decltype(nc)::value;
+    constexpr int PK = dgk::IpdgBlk<N>::PK, Np = dgk::IpdgBlk<N>::Np, NpP = dgk::IpdgBlk<N>::NpP;
+    const size_t smem = (size_t)E * PK * 4 + (size_t)E * NpP * 4 + (size_t)Np * NpP * 2;
+    if (r32)
+      k_bj_apply_pk<N, float><<<grid, block, smem, s>>>(h->K, st->binv_pk32, r32, z, z32);
+    else
+      k_bj_apply_pk<N, double><<<grid, block, smem, s>>>(h->K, st->binv_pk32, r64, z, z32);
+  };
+  switch (h->N) {
+    case 1: go(std::integral_constant<int, 1>{}); break;
+    case 2: go(std::integral_constant<int, 2>{}); break;
+    case 3: go(std::integral_constant<int, 3>{}); break;
+    case 4: go(std::integral_constant<int, 4>{}); break;
+    case 5: go(std::integral_constant<int, 5>{}); break;
+    case 6: go(std::integral_constant<int, 6>{}); break;
+    case 7: go(std::integral_constant<int, 7>{}); break;
+    case 8: go(std::integral_constant<int, 8>{}); break;
+    default: return set_error(DGC_ERR_ARG, "order outside 1..8");
+  }
   CKI(cudaGetLastError());
   ++h->launches;
   return DGC_OK;
