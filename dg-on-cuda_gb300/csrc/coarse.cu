@@ -670,7 +670,7 @@ int dgc::coarse_apply(dgc_handle_s* h, const double* r, const double* binv_r, do
   }
   // P^T r = P0^T (r - w S Binv r)
   if (!binv_r) {
-    if (int rc = ipdg_block_jacobi_apply(h, r, w0, s, false)) return rc;
+    if (int rc = ipdg_block_jacobi_apply(h, r, w0, s)) return rc;
     binv_r = w0;
   }
   if (int rc = dgc_laplace_spd_apply(h, binv_r, w1, s)) return rc;
@@ -682,7 +682,7 @@ int dgc::coarse_apply(dgc_handle_s* h, const double* r, const double* binv_r, do
   dgk::k_coarse_prolong<<<grid1(n), 256, 0, s>>>(n, h->NpP, h->Np, c->d_agg, c->d_xc, 0, w1, nullptr);
   CKC(cudaGetLastError(), "apply");
   if (int rc = dgc_laplace_spd_apply(h, w1, w2, s)) return rc;
-  if (int rc = ipdg_block_jacobi_apply(h, w2, w0, s, false)) return rc;
+  if (int rc = ipdg_block_jacobi_apply(h, w2, w0, s)) return rc;
   dgk::k_coarse_axpy<<<grid1(n), 256, 0, s>>>(n, w1, om, w0, z, add ? 1 : 0);
   CKC(cudaGetLastError(), "apply");
   h->launches += 5;

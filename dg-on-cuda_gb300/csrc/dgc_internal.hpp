@@ -67,7 +67,7 @@ void ipdg_operators_changed(dgc_handle_s* h);
 // block-Jacobi inverse of the SPD laplace form (built once), and z = Binv r
 // (FP64 vectors; the blocks and sums in FP32 with fp32)
 int ipdg_build_preconditioner(dgc_handle_s* h, cudaStream_t s);
-int ipdg_block_jacobi_apply(dgc_handle_s* h, const double* r, double* z, cudaStream_t s, bool fp32 = false);
+int ipdg_block_jacobi_apply(dgc_handle_s* h, const double* r, double* z, cudaStream_t s);
 // z = Binv r with the FP32 blocks, r given in FP64 (r64) or FP32 (r32, used when
 // non-null); z32, when non-null, receives an FP32 copy of z
 int ipdg_block_jacobi_apply_f32(dgc_handle_s* h, const double* r64, const float* r32, double* z, float* z32,

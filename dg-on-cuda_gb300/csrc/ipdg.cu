@@ -418,11 +418,10 @@ int ipdg_build_preconditioner(dgc_handle_s* h, cudaStream_t s) {
 }
 
 // z = Binv r elementwise (FP64 vectors, native layout; padding nodes of z set to
-// 0), the blocks and the sums in B's type: FP64 for block-Jacobi PCG, FP32
-// inside the two-level preconditioner.  A CTA holds whole elements (blockDim =
-// E * NpP) and stages r once per node in shared memory, in B's type: converted
-// per (node, j) instead, the FP32 form took as long as the FP64 one (FP64 work,
-// conversions included, is slow on GB300).
+// 0), the blocks and the sums in B's type (FP64 here; the FP32 cycle of the
+// two-level preconditioner uses the packed blocks below).  A CTA holds whole
+// elements (blockDim = E * NpP) and stages r once per node in shared memory, in
+// B's type.
 // The residual may also come as an FP32 vector (RIn = float: the two-level
 // cycle's FP32 operator output, no FP64 round trip), and z32, when given,
 // receives an FP32 copy of z (the input of the next FP32 operator apply).
@@ -489,15 +488,12 @@ __global__ void k_bj_apply_pk(int K, const float* __restrict__ bpk, const RIn* _
   if (z32) z32[o] = acc;
 }
 
-int ipdg_block_jacobi_apply(dgc_handle_s* h, const double* r, double* z, cudaStream_t s, bool fp32) {
+int ipdg_block_jacobi_apply(dgc_handle_s* h, const double* r, double* z, cudaStream_t s) {
   if (int rc = ipdg_build_preconditioner(h, s)) return rc;
   const IpdgState* st = h->ipdg;
   const int E = 256 / h->NpP;  // whole elements per CTA (NpP <= 48)
   const unsigned grid = (unsigned)((h->K + E - 1) / E), block = (unsigned)(E * h->NpP);
-  if (fp32)
-    k_bj_apply<float><<<grid, block, 0, s>>>(h->K, h->Np, h->NpP, st->bstr, st->binv32, r, z, nullptr);
-  else
-    k_bj_apply<double><<<grid, block, 0, s>>>(h->K, h->Np, h->NpP, st->bstr, st->binv64, r, z, nullptr);
+  k_bj_apply<double><<<grid, block, 0, s>>>(h->K, h->Np, h->NpP, st->bstr, st->binv64, r, z, nullptr);
   CKI(cudaGetLastError());
   ++h->launches;
   return DGC_OK;
