@@ -249,6 +249,12 @@ __device__ __forceinline__ bool blk_tiles(const RhsParams& p, unsigned char* sme
       }
     }
 
+    // the next stage may be scheduled once every CTA is past the volume term of
+    // its last tile: its set-up then overlaps this tile's face, lift and
+    // epilogue phases, and the launches ahead never run more than one stage
+    // deep (it waits for this grid before its reads)
+    if (tile + tstep >= tend) grid_dep_launch();
+
     // ---- face nodes: item (element e, face-node index d) takes node d of the
     //      three faces of e; the own and neighbour values of all three are
     //      gathered first, then the three fluxes formed
@@ -402,7 +408,6 @@ __global__ void __launch_bounds__(BlkConfig<N, P, EPT_, MAP_>::kThreads, BlkConf
   using C = BlkConfig<N, P, EPT_, MAP_>;
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t* bar = reinterpret_cast<uint64_t*>(smem + C::oBar);
-  grid_dep_launch();  // the next stage may be scheduled; it waits for this grid before its reads
   if (threadIdx.x == 0) {
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);

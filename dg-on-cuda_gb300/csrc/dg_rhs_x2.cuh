@@ -110,7 +110,6 @@ __global__ void __launch_bounds__(X2Config<N, P>::kThreads, X2Config<N, P>::kMin
   const float* qlo = qhi + nvec;
   const float cax = p.fax, cay = p.fay, cca = p.fca, ccb = p.fcb, cdt = p.fdt;
 
-  grid_dep_launch();  // the next stage may be scheduled; it waits for this grid before its reads
   if (tid == 0) {
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
@@ -247,6 +246,10 @@ __global__ void __launch_bounds__(X2Config<N, P>::kThreads, X2Config<N, P>::kMin
           res4[c] = *reinterpret_cast<const float4*>(aux + (size_t)(k0 + slot) * ESTR + c * NpP + 4 * grp);
       }
     }
+
+    // the next stage may be scheduled once every CTA is past the volume term of
+    // its last tile (see dg_rhs_blk_kernel)
+    if (tile + (int)gridDim.x >= ntiles) grid_dep_launch();
 
     // ---- face nodes: jumps d = q+ - q- from the hi and lo parts, then the
     // strong-form flux differences, pre-scaled by -faceJ / J.  Item (element
