@@ -107,10 +107,13 @@ __global__ void k_layout_x2(int K, int Nf, int Np, int NpP, int layout, int to_n
   }
 }
 
-// a plain launch: it ends the overlap chain of one step's stage launches, so
-// the next step's launches are not scheduled before this step has finished
-// (an early chain across steps made small meshes ~30 % slower per stage)
-__global__ void k_clock(double* t, double dt) { t[0] += dt; }
+// launched with programmatic serialization like the stages: it waits for the
+// step's last stage, and the next step's first stage waits for it
+__global__ void k_clock(double* t, double dt) {
+  dgk::grid_dep_launch();
+  dgk::grid_dep_wait();
+  t[0] += dt;
+}
 
 template <typename R>
 std::vector<R> pack_mats(const dgc::RefElement& re, const std::vector<double>& Dr, const std::vector<double>& Ds,
@@ -606,8 +609,7 @@ int lserk4_launches(dgc_handle h, void* q_in, void* q_out, void* res, double t, 
     if (int rc = launch(h, p, s)) return rc;
   }
   if (dev_time) {
-    k_clock<<<1, 1, 0, s>>>(h->d_time, dt);
-    CK(cudaGetLastError());
+    CK(dgk::launch_stage(k_clock, 1, 1, 0, s, h->d_time, dt));
     ++h->launches;
   }
   return DGC_OK;
