@@ -195,7 +195,12 @@ int dgc_lserk4_step(dgc_handle h, void* q_in, void* q_out, void* res, double t, 
 
 /* One LSERK4 stage (stage in 0..4) as a single fused launch:
  * res = a_s res + dt L_h(q_in, t + c_s dt);  q_out = q_in + b_s res.
- * dgc_lserk4_step is these five stages with q_in / q_out alternating. */
+ * dgc_lserk4_step is these five stages with q_in / q_out alternating.
+ * The stage launches use programmatic stream serialization: a stage's set-up
+ * overlaps the end of the previous launch on the stream, and it waits for that
+ * launch's completion before it touches its data, so the caller's stream
+ * ordering is unchanged.  An event recorded between two stage launches cuts
+ * the overlap.  DGC_STAGE_OVERLAP=0 in the environment turns it off. */
 int dgc_lserk4_stage(dgc_handle h, int stage, const void* q_in, void* q_out, void* res, double t, double dt,
                      void* stream);
 
